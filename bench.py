@@ -1,0 +1,386 @@
+"""Benchmark of the pairwise Hamming-distance path on one GB300.
+
+Workload (the reference's headline matrix): n=20,000 aligned sequences of
+L=29,903 sites (seeded synthetic SARS-CoV-2-like alignment: substitution
+p=1e-3, '-' runs of 0-200 at both ends, N runs at rate 1e-4), 30% exact
+duplicates; from_fasta(use_gpu=True, remove_duplicates=True,
+max_distance=255) -> uint8 lower triangle of the ~14,000 unique rows + the
+sequence indices, plus fasta_reference_distances of the root sequence
+against all 20,000 records.
+
+One step = that whole pass. Metric = unique pairs x L / step time
+(Gpair-sites/s).
+  value : FASTA bytes already resident in HBM; parse + dedupe + pack +
+          distance kernel + reference distances, all on the device, results
+          left in HBM. Timed with CUDA events on the library's stream.
+  e2e   : the public API a user calls (hammingdist_gb300.from_fasta(file) +
+          .lt_array + fasta_reference_distances(root, file)): file -> pinned
+          host buffer -> device -> host results, every step.
+Inputs are larger than L2 (598 MB of FASTA text, 209 MB of packed rows), so
+no L2 flush is needed between steps.
+
+--impl reference times the reference's CPU algorithm (the oracle: the
+reference compiled from source where available, else the C restatement in
+oracle/) on the host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gpair-sites/s n=20k L=29903 (bit-exact)"
+N, L, P_SUB, DUP, SEED = 20000, 29903, 1e-3, 0.3, 2024
+WORKLOAD = "from_fasta(use_gpu=True, remove_duplicates=True, max_distance=255) + " \
+           "fasta_reference_distances; n=20000 (30% duplicates), L=29903, uint8"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class quiet_stdout:
+    """Silences file descriptor 1 (the library's progress lines) so that the
+    JSON result is the only line on stdout."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        self.null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(self.null, 1)
+
+    def __exit__(self, *exc):
+        sys.stdout.flush()
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+        os.close(self.null)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.proc, self.lines = device, None, []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(tmpdir):
+    from hammingdist_gb300 import synth
+
+    rows, root, _ = synth.alignment(N, L, p=P_SUB, seed=SEED, dup_frac=DUP)
+    fa = synth.to_fasta(rows)
+    path = os.path.join(tmpdir, "bench.fasta")
+    with open(path, "wb") as f:
+        f.write(fa)
+    return fa, root.tobytes(), path, rows
+
+
+def profile_traffic():
+    """DRAM bytes per pairwise launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "pairwise_n20000_L29903.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ------------------------------------------------------------------ CPU leg
+def cpu_sample_rows(rows, budget_s):
+    """Unique rows of a bounded sample sized to ~budget_s of oracle work."""
+    from oracle import hd_oracle as o
+
+    uniq = list(dict.fromkeys(r.tobytes() for r in rows))
+    cal = uniq[:600]
+    t = time.perf_counter()
+    o.lt_dense(cal)
+    dt = time.perf_counter() - t
+    rate = len(cal) * (len(cal) - 1) / 2 * L / dt  # pair-sites/s
+    n_s = int((2 * budget_s * rate / L) ** 0.5)
+    n_s = max(600, min(n_s, len(uniq)))
+    return uniq[:n_s], rate
+
+
+def cpu_baseline(rows, budget_s):
+    """The reference's CPU algorithm on the host cores, bounded sample."""
+    from oracle import hd_oracle as o
+
+    kind = "port"
+    sample, _ = cpu_sample_rows(rows, budget_s)
+    fa = b"".join(b">s\n" + s + b"\n" for s in sample)
+    t = time.perf_counter()
+    o.from_fasta_dense(fa, remove_duplicates=True)
+    dt = time.perf_counter() - t
+    n_s = len(sample)
+    ps = n_s * (n_s - 1) / 2 * L
+    return {"value": ps / dt / 1e9, "unit": "Gpair-sites/s", "cores": o.num_threads(),
+            "kind": kind,
+            "sample": f"{n_s} unique rows of the workload (L={L}): parse+dedupe+pack+dense "
+                      f"AND-rule lower triangle, {dt:.1f} s, OpenMP"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as d:
+        fa, root, path, rows = make_workload(d)
+        from oracle import hd_oracle as o
+
+        budget = max(3.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
+        sample, _ = cpu_sample_rows(rows, budget)
+        sfa = b"".join(b">s\n" + s + b"\n" for s in sample)
+        n_s = len(sample)
+        times = []
+        for k in range(args.warmup + args.steps):
+            t = time.perf_counter()
+            o.from_fasta_dense(sfa, remove_duplicates=True)
+            dt = time.perf_counter() - t
+            if k >= args.warmup:
+                times.append(dt)
+        ps = n_s * (n_s - 1) / 2 * L
+        mean = sum(times) / len(times)
+        value = ps / mean / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gpair-sites/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded generator; no public dataset)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample_rows": n_s, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": value, "unit": "Gpair-sites/s", "cores": o.num_threads(),
+                             "kind": "port",
+                             "sample": f"{n_s} unique rows per step (bounded sample of the "
+                                       f"workload), dense AND rule, OpenMP"},
+            "e2e": {"value": value, "unit": "Gpair-sites/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU leg
+def run_ours(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    os.environ["HAMMINGDIST_DEVICE"] = str(local)
+    import hammingdist_gb300 as hd
+    from hammingdist_gb300 import abi
+
+    ctx = abi.Context(local)
+    with tempfile.TemporaryDirectory() as d:
+        fa, root, path, rows = make_workload(d)
+        nbytes = len(fa)
+        d_fa = torch.frombuffer(bytearray(fa), dtype=torch.uint8).to(f"cuda:{local}")
+        stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+
+        # sizes from a first pass (also warms the pools)
+        aln = ctx.alignment_from_fasta(d_fa.data_ptr(), nbytes, on_device=True,
+                                       remove_duplicates=True)
+        n_u = aln.n_rows
+        pairs = n_u * (n_u - 1) // 2
+        aln.free()
+        d_lt = torch.empty(pairs, dtype=torch.uint8, device=f"cuda:{local}")
+        refq = root
+
+        def step():
+            a = ctx.alignment_from_fasta(d_fa.data_ptr(), nbytes, on_device=True,
+                                         remove_duplicates=True)
+            ctx.pairwise_lt(a, dtype=np.uint8, max_distance=255, out=d_lt.data_ptr(),
+                            out_on_device=True)
+            pair_ms, tiles = ctx.last_pairwise_timing()
+            rd = ctx.alignment_reference_distances(a, refq)
+            a.free()
+            return pair_ms, tiles, rd
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        clocks = Clocks(local)
+        clocks.start()
+        launches0 = ctx.kernel_launches
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        pair_ms = []
+        for _ in range(args.steps):
+            pm, tiles, rd = step()
+            pair_ms.append(pm)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        launches = ctx.kernel_launches - launches0
+        elapsed = ev0.elapsed_time(ev1) / 1e3
+        if ws > 1:
+            t = torch.tensor([elapsed], device=f"cuda:{local}")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            elapsed = float(t.item())
+            torch.distributed.barrier()
+        ms_step = elapsed / args.steps * 1e3
+        value = ws * pairs * L * args.steps / elapsed / 1e9
+
+        # parity on the final step's device results: sampled rows vs the oracle
+        from oracle import hd_oracle as o
+
+        uniq = list(dict.fromkeys(r.tobytes() for r in rows))
+        assert len(uniq) == n_u
+        rng = np.random.default_rng(1)
+        pick = np.sort(rng.choice(n_u, size=min(48, n_u), replace=False))
+        want = o.lt_dense([uniq[i] for i in pick])
+        lt_host = d_lt.cpu().numpy()
+        got = np.array([lt_host[pick[a] * (pick[a] - 1) // 2 + pick[b]]
+                        for a in range(len(pick)) for b in range(a)], dtype=np.uint8)
+        parity = bool(np.array_equal(got, want))
+        rd_want = o.reference_distances(root, fa)
+        parity = parity and bool(np.array_equal(rd, rd_want))
+
+        # e2e: the public API with host buffers (file -> pinned -> device -> host)
+        e2e_times = []
+        h2d = d2h = 0
+        for k in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            with quiet_stdout():
+                t = time.perf_counter()
+                ds = hd.from_fasta(path, use_gpu=True, remove_duplicates=True)
+                lt_arr = ds.lt_array
+                rd2 = hd.fasta_reference_distances(root.decode(), path)
+                torch.cuda.synchronize()
+                dt = time.perf_counter() - t
+            if k >= args.warmup:
+                e2e_times.append(dt)
+            h2d = 2 * nbytes  # the FASTA goes up for each of the two calls
+            d2h = lt_arr.nbytes + 8 * N + rd2.nbytes
+        parity = parity and bool(np.array_equal(np.asarray(lt_arr), lt_host)) and \
+            bool(np.array_equal(rd2, rd_want))
+        e2e_mean = sum(e2e_times) / len(e2e_times)
+        e2e_value = ws * pairs * L / e2e_mean / 1e9
+
+        # roofline of the dominant kernel: 4 LOP3 per 32 pair-sites
+        peaks = ctx.measure_int_peaks()
+        kern_s = statistics.mean(pair_ms) / 1e3
+        lop3_per_launch = pairs * L / 8.0
+        achieved = lop3_per_launch / kern_s / 1e12
+        peak = peaks["lop3_per_s"] / 1e12
+        traffic = profile_traffic()
+
+        if rank == 0:
+            line = {
+                "metric": METRIC, "value": value, "unit": "Gpair-sites/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+                "data": "synthetic (seeded generator; no public dataset)",
+                "config": {"workload": WORKLOAD, "unique_rows": n_u, "pairs": pairs,
+                           "nominal_value": ws * (N * (N - 1) // 2) * L * args.steps / elapsed / 1e9,
+                           "l2": "inputs larger than L2 (598 MB FASTA, 209 MB packed rows); no flush",
+                           "parallelism": "replicas" if ws > 1 else "single GPU"},
+                "parity": "bit-exact (sampled rows + all reference distances vs oracle)"
+                if parity else "MISMATCH",
+                "roofline": {"bound": "int_lop3", "achieved": achieved, "peak": peak,
+                             "unit": "TLOP3/s", "frac": achieved / peak, "traffic": traffic,
+                             "kernel_ms": kern_s * 1e3,
+                             "peak_source": "in-run LOP3 microbenchmark (hd_measure_int_peaks); "
+                                            "MEASURED_PEAKS.json has no integer-pipe figure",
+                             "popc_peak_T": peaks["popc_per_s"] / 1e12,
+                             "pair_sites_bound_T": peaks["mix_pair_sites_per_s"] / 1e12,
+                             "kernel_pair_sites_T": pairs * L / kern_s / 1e12,
+                             "hbm_write_GBs": pairs / kern_s / 1e9},
+                "e2e": {"value": e2e_value, "unit": "Gpair-sites/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h, "ms_per_step": e2e_mean * 1e3},
+                "gpu_launches": launches,
+                "clocks": clk,
+            }
+            if not args.no_cpu:
+                line["cpu_baseline"] = cpu_baseline(rows, args.cpu_seconds)
+            print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,239 @@
+"""ctypes binding of the libhd C ABI (include/hammingdist_gb300.h).
+
+This is the binding a Python caller (or the reference's own bindings) would
+add to reach the GPU path through plain pointers and sizes; the pybind11
+module ``hammingdist_gb300._C`` is the C++ equivalent. Device pointers may be
+passed as integers (e.g. ``torch.Tensor.data_ptr()``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import LIBHD_PATH
+
+u64, i64, vp, cp, ci = ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int
+P = ctypes.POINTER
+
+# name -> (restype, argtypes); every function declared in the header
+SIGNATURES = {
+    "hd_device_available": (ci, []),
+    "hd_ctx_create": (ci, [ci, P(vp)]),
+    "hd_ctx_destroy": (None, [vp]),
+    "hd_last_error": (cp, [vp]),
+    "hd_ctx_kernel_launches": (u64, [vp]),
+    "hd_host_alloc": (ci, [vp, ctypes.c_size_t, P(vp)]),
+    "hd_host_free": (None, [vp, vp]),
+    "hd_free": (None, [vp]),
+    "hd_ctx_synchronize": (ci, [vp]),
+    "hd_ctx_stream": (vp, [vp]),
+    "hd_alignment_from_fasta": (ci, [vp, vp, u64, ci, ci, u64, ci, ci, P(vp)]),
+    "hd_alignment_from_sequences": (ci, [vp, vp, vp, u64, ci, ci, P(vp)]),
+    "hd_alignment_info": (ci, [vp, P(u64), P(u64), P(u64), P(ci)]),
+    "hd_alignment_sequence_indices": (ci, [vp, vp]),
+    "hd_alignment_free": (None, [vp]),
+    "hd_pairwise_lt": (ci, [vp, vp, ci, i64, vp, ci]),
+    "hd_pairwise_lt_to_file": (ci, [vp, vp, i64, cp]),
+    "hd_write_lower_triangular": (ci, [vp, vp, u64, ci, cp]),
+    "hd_write_sparse": (ci, [vp, vp, u64, ci, i64, cp, P(u64)]),
+    "hd_reference_distances": (ci, [vp, vp, u64, vp, u64, ci, P(vp), P(u64)]),
+    "hd_alignment_reference_distances": (ci, [vp, vp, vp, u64, ci, vp]),
+    "hd_fasta_sequence_indices": (ci, [vp, vp, u64, u64, P(vp), P(u64)]),
+    "hd_distance": (ci, [vp, vp, u64, vp, u64, ci, P(ctypes.c_uint32)]),
+    "hd_measure_int_peaks": (ci, [vp, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
+    "hd_last_pairwise_timing": (ci, [vp, P(ctypes.c_double), P(u64)]),
+}
+
+SEM_GPU, SEM_CPU = 0, 1
+RULES = {0: "and", 1: "sparse", 2: "sparse_x"}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(LIBHD_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class HDError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+def _ptr(x):
+    """Host buffer (bytes / numpy) or device pointer (int) -> c_void_p."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return ctypes.c_void_p(x)
+    if isinstance(x, np.ndarray):
+        return ctypes.c_void_p(x.ctypes.data)
+    if isinstance(x, (bytes, bytearray)):
+        return ctypes.cast(ctypes.c_char_p(bytes(x)), ctypes.c_void_p)
+    raise TypeError(type(x))
+
+
+class Alignment:
+    def __init__(self, ctx: "Context", handle):
+        self.ctx, self.h = ctx, handle
+        n_rows, length, n_in, rule = u64(), u64(), u64(), ci()
+        ctx._check(lib().hd_alignment_info(handle, ctypes.byref(n_rows), ctypes.byref(length),
+                                           ctypes.byref(n_in), ctypes.byref(rule)))
+        self.n_rows, self.length, self.n_input = n_rows.value, length.value, n_in.value
+        self.rule = RULES[rule.value]
+
+    def sequence_indices(self) -> np.ndarray:
+        out = np.zeros(max(self.n_input, 1), dtype=np.uint64)
+        self.ctx._check(lib().hd_alignment_sequence_indices(self.h, out.ctypes.data))
+        return out[: self.n_input]
+
+    def free(self):
+        if self.h:
+            lib().hd_alignment_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        h = vp()
+        rc = lib().hd_ctx_create(device, ctypes.byref(h))
+        if rc != 0:
+            raise HDError(rc, f"hd_ctx_create failed ({rc})")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().hd_ctx_destroy(self.h)
+            self.h = None
+
+    def _check(self, rc):
+        if rc != 0:
+            raise HDError(rc, (lib().hd_last_error(self.h) or b"").decode())
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().hd_ctx_kernel_launches(self.h))
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t of the context (for torch.cuda.ExternalStream)."""
+        return int(lib().hd_ctx_stream(self.h) or 0)
+
+    def synchronize(self):
+        self._check(lib().hd_ctx_synchronize(self.h))
+
+    def alignment_from_fasta(self, data, nbytes=None, on_device=False, remove_duplicates=False,
+                             n=0, include_x=False, semantics=SEM_GPU) -> Alignment:
+        if nbytes is None:
+            nbytes = len(data)
+        a = vp()
+        self._check(lib().hd_alignment_from_fasta(self.h, _ptr(data), nbytes, int(on_device),
+                                                  int(remove_duplicates), n, int(include_x),
+                                                  semantics, ctypes.byref(a)))
+        return Alignment(self, a)
+
+    def alignment_from_sequences(self, seqs, include_x=False, semantics=SEM_GPU) -> Alignment:
+        seqs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+        raw = b"".join(seqs)
+        offs = np.zeros(len(seqs) + 1, dtype=np.uint64)
+        offs[1:] = np.cumsum([len(s) for s in seqs]) if seqs else []
+        a = vp()
+        self._check(lib().hd_alignment_from_sequences(self.h, _ptr(raw), offs.ctypes.data,
+                                                      len(seqs), int(include_x), semantics,
+                                                      ctypes.byref(a)))
+        return Alignment(self, a)
+
+    def pairwise_lt(self, aln: Alignment, dtype=np.uint8, max_distance=255, out=None,
+                    out_on_device=False):
+        """Host numpy result, or writes to a device pointer `out` (int)."""
+        dt = np.dtype(dtype)
+        n = aln.n_rows
+        if out is None:
+            out = np.zeros(max(n * (n - 1) // 2, 1), dtype=dt)
+            self._check(lib().hd_pairwise_lt(self.h, aln.h, dt.itemsize, int(max_distance),
+                                             out.ctypes.data, 0))
+            return out[: n * (n - 1) // 2]
+        self._check(lib().hd_pairwise_lt(self.h, aln.h, dt.itemsize, int(max_distance), _ptr(out),
+                                         int(out_on_device)))
+        return out
+
+    def pairwise_lt_to_file(self, aln: Alignment, max_distance: int, path: str):
+        self._check(lib().hd_pairwise_lt_to_file(self.h, aln.h, int(max_distance), path.encode()))
+
+    def write_lower_triangular(self, lt: np.ndarray, nsamples: int, path: str):
+        lt = np.ascontiguousarray(lt)
+        self._check(lib().hd_write_lower_triangular(self.h, lt.ctypes.data, nsamples,
+                                                    lt.dtype.itemsize, path.encode()))
+
+    def write_sparse(self, lt: np.ndarray, nsamples: int, threshold: int, path: str) -> int:
+        lt = np.ascontiguousarray(lt)
+        nl = u64()
+        self._check(lib().hd_write_sparse(self.h, lt.ctypes.data, nsamples, lt.dtype.itemsize,
+                                          threshold, path.encode(), ctypes.byref(nl)))
+        return nl.value
+
+    def reference_distances(self, ref, data: bytes, include_x=False) -> np.ndarray:
+        ref = ref.encode() if isinstance(ref, str) else bytes(ref)
+        out, n = vp(), u64()
+        self._check(lib().hd_reference_distances(self.h, _ptr(ref), len(ref),
+                                                 _ptr(data), len(data), int(include_x),
+                                                 ctypes.byref(out), ctypes.byref(n)))
+        return _take(out, n.value, np.uint32)
+
+    def alignment_reference_distances(self, aln: Alignment, ref) -> np.ndarray:
+        ref = ref.encode() if isinstance(ref, str) else bytes(ref)
+        out = np.zeros(max(aln.n_input, 1), dtype=np.uint32)
+        self._check(lib().hd_alignment_reference_distances(self.h, aln.h, _ptr(ref),
+                                                           len(ref), 0, out.ctypes.data))
+        return out[: aln.n_input]
+
+    def fasta_sequence_indices(self, data: bytes, n=0) -> np.ndarray:
+        out, cnt = vp(), u64()
+        self._check(lib().hd_fasta_sequence_indices(self.h, _ptr(data), len(data), n,
+                                                    ctypes.byref(out), ctypes.byref(cnt)))
+        return _take(out, cnt.value, np.uint64)
+
+    def distance(self, s0, s1, include_x=False) -> int:
+        s0 = s0.encode() if isinstance(s0, str) else bytes(s0)
+        s1 = s1.encode() if isinstance(s1, str) else bytes(s1)
+        d = ctypes.c_uint32()
+        self._check(lib().hd_distance(self.h, _ptr(s0), len(s0), _ptr(s1), len(s1),
+                                      int(include_x), ctypes.byref(d)))
+        return int(d.value)
+
+    def measure_int_peaks(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(lib().hd_measure_int_peaks(self.h, ctypes.byref(a), ctypes.byref(b),
+                                               ctypes.byref(c)))
+        return {"lop3_per_s": a.value, "popc_per_s": b.value, "mix_pair_sites_per_s": c.value}
+
+    def last_pairwise_timing(self):
+        ms, tiles = ctypes.c_double(), u64()
+        self._check(lib().hd_last_pairwise_timing(self.h, ctypes.byref(ms), ctypes.byref(tiles)))
+        return ms.value, tiles.value
+
+
+def _take(ptr: ctypes.c_void_p, n: int, dtype) -> np.ndarray:
+    if not ptr.value:
+        return np.zeros(0, dtype=dtype)
+    nbytes = n * np.dtype(dtype).itemsize
+    arr = np.frombuffer(ctypes.string_at(ptr.value, nbytes), dtype=dtype).copy() if n else \
+        np.zeros(0, dtype=dtype)
+    lib().hd_free(ptr)
+    return arr

@@ -1,0 +1,596 @@
+// The C ABI (include/hammingdist_gb300.h): argument checks, error mapping,
+// host<->device movement and the orchestration of the device stages.
+#include <fcntl.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <limits>
+
+#include "hd_internal.cuh"
+
+using hd::DevBuf;
+using hd::Error;
+using hd::fail;
+
+namespace {
+
+const char *kMsgEmpty = "Error: Empty sequence";
+const char *kMsgLength = "Error: Sequences do not all have the same length";
+const char *kMsgIncludeX = "use_gpu=True cannot be used if include_x=True, please set use_gpu=False";
+
+template <class F>
+int guard(hd_ctx *ctx, F &&f) {
+  try {
+    if (ctx) HD_CUDA(cudaSetDevice(ctx->device));
+    f();
+    return HD_OK;
+  } catch (const Error &e) {
+    if (ctx) ctx->err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    if (ctx) ctx->err = "out of host memory";
+    return HD_ERR_OOM;
+  } catch (const std::exception &e) {
+    if (ctx) ctx->err = e.what();
+    return HD_ERR_CUDA;
+  }
+}
+
+// safe_int_cast (include/hamming/hamming_impl.hh:37-45): above the dtype max
+// saturates, otherwise static_cast (negative values wrap).
+uint32_t clamp_max(int64_t max_distance, int dtype_bytes) {
+  if (dtype_bytes == 4) {
+    if (max_distance < 0) fail(HD_ERR_ARG, "max_distance must be >= 0 for 32-bit output");
+    return max_distance > 0xffffffffll ? 0xffffffffu : (uint32_t)max_distance;
+  }
+  const uint32_t tmax = dtype_bytes == 1 ? 0xffu : 0xffffu;
+  if (max_distance > (int64_t)tmax) return tmax;
+  return (uint32_t)((uint64_t)max_distance & tmax);
+}
+
+void check_dtype(int dtype_bytes) {
+  if (dtype_bytes != 1 && dtype_bytes != 2 && dtype_bytes != 4)
+    fail(HD_ERR_ARG, "dtype_bytes must be 1, 2 or 4");
+}
+
+void check_status(hd_ctx *ctx) {
+  int st = 0;
+  HD_CUDA(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st == hd::kStatusTmaTimeout) {
+    HD_CUDA(cudaMemset(ctx->d_status, 0, sizeof(int)));
+    fail(HD_ERR_TIMEOUT, "a device wait for a TMA transfer ran out (pairwise kernel)");
+  }
+}
+
+// Device copy of host (or pass-through of device) FASTA bytes; 16-byte aligned.
+const uint8_t *stage_input(hd_ctx *ctx, const char *bytes, uint64_t n, int on_device) {
+  if (on_device && (reinterpret_cast<uintptr_t>(bytes) & 15u) == 0)
+    return reinterpret_cast<const uint8_t *>(bytes);
+  if (ctx->file.bytes < n + 16) {
+    ctx->file.release();
+    ctx->file = DevBuf(hd::round_up(n + 16, 1 << 20), ctx->stream);
+  }
+  if (n)
+    HD_CUDA(cudaMemcpyAsync(ctx->file.p, bytes, n,
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                            ctx->stream));
+  return ctx->file.as<uint8_t>();
+}
+
+uint64_t words_for(uint64_t L) { return hd::round_up(hd::ceil_div(L ? L : 1, 32), 8); }
+
+// validate_data (src/hamming_impl.cc:80-91) + the include_x/use_gpu check
+// (include/hamming/hamming_impl.hh:99-102) + dedupe + rule choice + pack.
+hd_alignment *build_alignment(hd_ctx *ctx, hd::Records &rec, int remove_duplicates, int include_x,
+                              int semantics) {
+  if (rec.n == 0 || rec.len0 == 0) fail(HD_ERR_EMPTY, kMsgEmpty);
+  if (!rec.all_equal) fail(HD_ERR_LENGTH, kMsgLength);
+  if (semantics == HD_SEM_GPU && include_x) fail(HD_ERR_INCLUDE_X_GPU, kMsgIncludeX);
+  if (semantics != HD_SEM_GPU && semantics != HD_SEM_CPU) fail(HD_ERR_ARG, "bad semantics");
+  auto *aln = new hd_alignment();
+  try {
+    aln->ctx = ctx;
+    aln->n_input = rec.n;
+    aln->length = rec.len0;
+    aln->words = words_for(rec.len0);
+    DevBuf rows;
+    const uint64_t *d_rows = nullptr;
+    if (remove_duplicates) {
+      uint64_t nu = 0;
+      rows = hd::dedupe(ctx, rec, &nu, aln->seqidx);
+      d_rows = rows.as<uint64_t>();
+      aln->n_rows = nu;
+    } else {
+      aln->n_rows = rec.n;
+    }
+    int rule = HD_RULE_AND;
+    if (semantics == HD_SEM_CPU) {
+      if (include_x) {
+        rule = HD_RULE_SPARSE_X;
+      } else {
+        // include/hamming/hamming_impl.hh:104-118: sparse when fewer than 0.5%
+        // of all sites differ from the per-site consensus
+        const uint64_t total = aln->n_rows * aln->length;
+        const uint64_t same = hd::consensus_matches(ctx, rec, d_rows, aln->n_rows);
+        const double frac = (double)(total - same) / (double)total;
+        rule = frac < 0.005 ? HD_RULE_SPARSE : HD_RULE_AND;
+      }
+    }
+    aln->rule = rule;
+    aln->planes = hd::planes_of(rule);
+    aln->groups = aln->planes > 4 ? 2 : 1;
+    hd::pack_rows(ctx, rec, d_rows, aln);
+    if (!aln->seqidx.empty()) {
+      aln->d_seqidx = DevBuf(aln->seqidx.size() * 8, ctx->stream);
+      HD_CUDA(cudaMemcpyAsync(aln->d_seqidx.p, aln->seqidx.data(), aln->seqidx.size() * 8,
+                              cudaMemcpyHostToDevice, ctx->stream));
+    }
+    HD_CUDA(cudaStreamSynchronize(ctx->stream));
+  } catch (...) {
+    delete aln;
+    throw;
+  }
+  return aln;
+}
+
+// ---------------------------------------------------------------- file out
+struct OutFile {
+  int fd = -1;
+  std::string path;
+  OutFile(const char *p, bool truncate) : path(p) {
+    fd = ::open(p, O_WRONLY | O_CREAT | (truncate ? O_TRUNC : O_APPEND), 0644);
+    if (fd < 0) fail(HD_ERR_IO, "Error: Failed to open file '" + path + "'");
+  }
+  void write(const char *buf, uint64_t n) {
+    while (n) {
+      ssize_t w = ::write(fd, buf, n > (1ull << 30) ? (1ull << 30) : n);
+      if (w < 0) fail(HD_ERR_IO, "Error: Failed to write file '" + path + "'");
+      buf += w;
+      n -= (uint64_t)w;
+    }
+  }
+  ~OutFile() {
+    if (fd >= 0) ::close(fd);
+  }
+};
+
+// Pinned double buffer: the host writes one half while the device fills the
+// other.
+struct PinnedPair {
+  char *buf[2] = {nullptr, nullptr};
+  uint64_t cap = 0;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  explicit PinnedPair(uint64_t c) : cap(c) {
+    for (int k = 0; k < 2; ++k) {
+      HD_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&buf[k]), c ? c : 1, cudaHostAllocDefault));
+      HD_CUDA(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
+    }
+  }
+  ~PinnedPair() {
+    for (int k = 0; k < 2; ++k) {
+      if (buf[k]) cudaFreeHost(buf[k]);
+      if (ev[k]) cudaEventDestroy(ev[k]);
+    }
+  }
+};
+
+uint64_t tri(uint64_t i) { return i * (i - 1) / 2; }
+
+// Row ranges [r0, r1) whose lower-triangle entries stay under max_entries
+// (at least one row each). If align is set, boundaries are multiples of it.
+std::vector<std::pair<uint64_t, uint64_t>> row_chunks(uint64_t n, uint64_t max_entries,
+                                                      uint64_t align) {
+  std::vector<std::pair<uint64_t, uint64_t>> out;
+  uint64_t r0 = 0;
+  while (r0 < n) {
+    uint64_t r1 = r0 + align;
+    while (r1 < n && tri(std::min(r1 + align, n)) - tri(r0) <= max_entries) r1 += align;
+    r1 = std::min(r1, n);
+    out.emplace_back(r0, r1);
+    r0 = r1;
+  }
+  return out;
+}
+
+constexpr uint64_t kTextChunkBytes = 256ull << 20;  // text per streamed chunk (bound)
+
+// Streams lower-triangular text of rows [0, n) to `path`. `produce(r0, r1,
+// d_lt)` leaves the entries of rows [r0, r1) in d_lt (lt index tri(r0) at
+// d_lt[0]) on ctx->stream.
+template <class Produce>
+void stream_lt_text(hd_ctx *ctx, uint64_t n, int dtype_bytes, const char *path, uint64_t align,
+                    Produce &&produce) {
+  if (n < 2) return;  // no entries: the reference leaves the file untouched
+  const uint64_t per = dtype_bytes == 1 ? 4 : dtype_bytes == 2 ? 6 : 11;
+  const uint64_t max_entries = std::max<uint64_t>(kTextChunkBytes / per, 1);
+  auto chunks = row_chunks(n, max_entries, align);
+  uint64_t max_e = 0, max_text = 0;
+  for (auto &c : chunks) {
+    max_e = std::max(max_e, tri(c.second) - tri(std::max<uint64_t>(c.first, 1)));
+    max_text = std::max(max_text, hd::lt_text_bound(c.first, c.second, dtype_bytes));
+  }
+  DevBuf d_lt((max_e + 1) * dtype_bytes, ctx->stream), d_text(max_text + 16, ctx->stream);
+  PinnedPair pin(max_text + 16);
+  OutFile f(path, true);
+  uint64_t pending_bytes = 0;
+  int pending = -1;
+  for (size_t k = 0; k < chunks.size(); ++k) {
+    const uint64_t r0 = chunks[k].first, r1 = chunks[k].second;
+    produce(r0, r1, d_lt.p);
+    // write the previous chunk while this one computes
+    if (pending >= 0) {
+      HD_CUDA(cudaEventSynchronize(pin.ev[pending]));
+      f.write(pin.buf[pending], pending_bytes);
+      pending = -1;
+    }
+    const uint64_t nb = hd::format_lt_rows(ctx, d_lt.p, dtype_bytes, tri(r0), r0, r1, d_text.as<char>());
+    const int slot = (int)(k & 1);
+    if (nb)
+      HD_CUDA(cudaMemcpyAsync(pin.buf[slot], d_text.p, nb, cudaMemcpyDeviceToHost, ctx->stream));
+    HD_CUDA(cudaEventRecord(pin.ev[slot], ctx->stream));
+    pending = slot;
+    pending_bytes = nb;
+  }
+  if (pending >= 0) {
+    HD_CUDA(cudaEventSynchronize(pin.ev[pending]));
+    f.write(pin.buf[pending], pending_bytes);
+  }
+  check_status(ctx);
+}
+
+}  // namespace
+
+// =================================================================== ABI
+extern "C" {
+
+int hd_device_available(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n > 0 ? 1 : 0;
+}
+
+int hd_ctx_create(int device, hd_ctx **out) {
+  if (!out) return HD_ERR_ARG;
+  *out = nullptr;
+  if (!hd_device_available()) return HD_ERR_NO_DEVICE;
+  auto *ctx = new hd_ctx();
+  ctx->device = device;
+  int rc = guard(ctx, [&] {
+    HD_CUDA(cudaSetDevice(device));
+    HD_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
+    HD_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    HD_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+    HD_CUDA(cudaEventCreate(&ctx->ev_start));
+    HD_CUDA(cudaEventCreate(&ctx->ev_stop));
+    HD_CUDA(cudaMalloc(&ctx->d_status, 64));
+    HD_CUDA(cudaMemset(ctx->d_status, 0, 64));
+    cudaMemPool_t pool;
+    HD_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t thr = std::numeric_limits<uint64_t>::max();
+    HD_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    HD_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                             cudaEnableDefault, &q));
+    if (!fn || q != cudaDriverEntryPointSuccess) fail(HD_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    ctx->encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  });
+  if (rc != HD_OK) {
+    hd_ctx_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return HD_OK;
+}
+
+void hd_ctx_destroy(hd_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  ctx->file.release();
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->d_status) cudaFree(ctx->d_status);
+  if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+  if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
+  delete ctx;
+}
+
+const char *hd_last_error(const hd_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+uint64_t hd_ctx_kernel_launches(const hd_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int hd_host_alloc(hd_ctx *ctx, size_t bytes, void **out) {
+  return guard(ctx, [&] {
+    if (!out) fail(HD_ERR_ARG, "null output");
+    *out = nullptr;
+    HD_CUDA(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault));
+  });
+}
+
+void hd_host_free(hd_ctx *ctx, void *p) {
+  if (ctx) cudaSetDevice(ctx->device);
+  if (p) cudaFreeHost(p);
+}
+
+void hd_free(void *p) { std::free(p); }
+
+void *hd_ctx_stream(const hd_ctx *ctx) { return ctx ? static_cast<void *>(ctx->stream) : nullptr; }
+
+int hd_ctx_synchronize(hd_ctx *ctx) {
+  return guard(ctx, [&] { HD_CUDA(cudaStreamSynchronize(ctx->stream)); });
+}
+
+int hd_alignment_from_fasta(hd_ctx *ctx, const char *fasta, uint64_t nbytes, int fasta_on_device,
+                            int remove_duplicates, uint64_t n_limit, int include_x, int semantics,
+                            hd_alignment **out) {
+  if (!ctx || !out || (!fasta && nbytes)) return HD_ERR_ARG;
+  *out = nullptr;
+  return guard(ctx, [&] {
+    const uint8_t *d = stage_input(ctx, fasta, nbytes, fasta_on_device);
+    hd::Records rec = hd::parse_fasta(ctx, d, nbytes, n_limit);
+    *out = build_alignment(ctx, rec, remove_duplicates, include_x, semantics);
+  });
+}
+
+int hd_alignment_from_sequences(hd_ctx *ctx, const char *bytes, const uint64_t *offsets, uint64_t n,
+                                int include_x, int semantics, hd_alignment **out) {
+  if (!ctx || !out || (n && !offsets)) return HD_ERR_ARG;
+  *out = nullptr;
+  return guard(ctx, [&] {
+    const uint64_t nbytes = n ? offsets[n] - offsets[0] : 0;
+    const uint8_t *d = stage_input(ctx, bytes ? bytes + (n ? offsets[0] : 0) : bytes, nbytes, 0);
+    hd::Records rec = hd::records_from_offsets(ctx, d, offsets, n);
+    *out = build_alignment(ctx, rec, 0, include_x, semantics);
+  });
+}
+
+int hd_alignment_info(const hd_alignment *aln, uint64_t *n_rows, uint64_t *length,
+                      uint64_t *n_input, int *rule) {
+  if (!aln) return HD_ERR_ARG;
+  if (n_rows) *n_rows = aln->n_rows;
+  if (length) *length = aln->length;
+  if (n_input) *n_input = aln->n_input;
+  if (rule) *rule = aln->rule;
+  return HD_OK;
+}
+
+int hd_alignment_sequence_indices(const hd_alignment *aln, uint64_t *out) {
+  if (!aln || !out) return HD_ERR_ARG;
+  if (aln->seqidx.empty())
+    for (uint64_t k = 0; k < aln->n_input; ++k) out[k] = k;
+  else
+    std::memcpy(out, aln->seqidx.data(), aln->seqidx.size() * 8);
+  return HD_OK;
+}
+
+void hd_alignment_free(hd_alignment *aln) {
+  if (!aln) return;
+  if (aln->ctx) cudaSetDevice(aln->ctx->device);
+  delete aln;
+}
+
+int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, int64_t max_distance,
+                   void *out, int out_on_device) {
+  if (!ctx || !aln) return HD_ERR_ARG;
+  return guard(ctx, [&] {
+    check_dtype(dtype_bytes);
+    const uint32_t md = clamp_max(max_distance, dtype_bytes);
+    const uint64_t n = aln->n_rows, entries = n < 2 ? 0 : tri(n);
+    ctx->last_pair_ms = 0;
+    ctx->last_pair_tiles = 0;
+    if (!entries) return;
+    if (!out) fail(HD_ERR_ARG, "null output");
+    DevBuf tmp;
+    void *d_out = out;
+    if (!out_on_device) {
+      tmp = DevBuf(entries * dtype_bytes, ctx->stream);
+      d_out = tmp.p;
+    }
+    const uint32_t nb = (uint32_t)hd::ceil_div(n, hd::kTile);
+    HD_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
+    hd::pairwise_tiles(ctx, aln, dtype_bytes, md, d_out, 0, 0, nb);
+    HD_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
+    if (!out_on_device)
+      HD_CUDA(cudaMemcpyAsync(out, d_out, entries * dtype_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    HD_CUDA(cudaStreamSynchronize(ctx->stream));
+    float ms = 0;
+    HD_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+    ctx->last_pair_ms = ms;
+    check_status(ctx);
+  });
+}
+
+int hd_pairwise_lt_to_file(hd_ctx *ctx, const hd_alignment *aln, int64_t max_distance,
+                           const char *path) {
+  if (!ctx || !aln || !path) return HD_ERR_ARG;
+  return guard(ctx, [&] {
+    // distances_cuda_to_lower_triangular: uint16, max above 65535 -> 65535
+    const uint32_t md = clamp_max(max_distance, 2);
+    stream_lt_text(ctx, aln->n_rows, 2, path, hd::kTile,
+                   [&](uint64_t r0, uint64_t r1, void *d_lt) {
+                     hd::pairwise_tiles(ctx, aln, 2, md, d_lt, tri(std::max<uint64_t>(r0, 1)),
+                                        (uint32_t)(r0 / hd::kTile),
+                                        (uint32_t)hd::ceil_div(r1, hd::kTile));
+                   });
+  });
+}
+
+int hd_write_lower_triangular(hd_ctx *ctx, const void *lt, uint64_t nsamples, int dtype_bytes,
+                              const char *path) {
+  if (!ctx || !path || (!lt && nsamples > 1)) return HD_ERR_ARG;
+  return guard(ctx, [&] {
+    check_dtype(dtype_bytes);
+    stream_lt_text(ctx, nsamples, dtype_bytes, path, 1, [&](uint64_t r0, uint64_t r1, void *d_lt) {
+      const uint64_t e0 = tri(std::max<uint64_t>(r0, 1)), e1 = tri(r1);
+      if (e1 > e0)
+        HD_CUDA(cudaMemcpyAsync(d_lt, static_cast<const char *>(lt) + e0 * dtype_bytes,
+                                (e1 - e0) * dtype_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    });
+  });
+}
+
+int hd_write_sparse(hd_ctx *ctx, const void *lt, uint64_t nsamples, int dtype_bytes,
+                    int64_t threshold, const char *path, uint64_t *n_lines) {
+  if (!ctx || !path || (!lt && nsamples > 1)) return HD_ERR_ARG;
+  return guard(ctx, [&] {
+    check_dtype(dtype_bytes);
+    OutFile f(path, true);  // the reference always (re)creates the file
+    uint64_t lines_total = 0;
+    if (nsamples >= 2) {
+      // bytes per line <= 2 * digits(n) + digits(dtype max) + 3
+      uint64_t dn = 1;
+      for (uint64_t v = nsamples; v >= 10; v /= 10) ++dn;
+      const uint64_t per = 2 * dn + (dtype_bytes == 1 ? 3 : dtype_bytes == 2 ? 5 : 10) + 3;
+      const uint64_t max_entries = std::max<uint64_t>(kTextChunkBytes / per, 1);
+      auto chunks = row_chunks(nsamples, max_entries, 1);
+      uint64_t max_e = 0, max_rows = 0;
+      for (auto &c : chunks) {
+        max_e = std::max(max_e, tri(c.second) - tri(std::max<uint64_t>(c.first, 1)));
+        max_rows = std::max(max_rows, c.second - c.first);
+      }
+      DevBuf d_lt((max_e + 1) * dtype_bytes, ctx->stream), d_text(max_e * per + 16, ctx->stream);
+      DevBuf rb((max_rows + 1) * 8, ctx->stream), rl((max_rows + 1) * 8, ctx->stream),
+          tot(8, ctx->stream);
+      PinnedPair pin(max_e * per + 16);
+      int pending = -1;
+      uint64_t pending_bytes = 0;
+      for (size_t k = 0; k < chunks.size(); ++k) {
+        const uint64_t r0 = std::max<uint64_t>(chunks[k].first, 1), r1 = chunks[k].second;
+        if (r1 <= r0) continue;
+        const uint64_t e0 = tri(r0), e1 = tri(r1);
+        HD_CUDA(cudaMemcpyAsync(d_lt.p, static_cast<const char *>(lt) + e0 * dtype_bytes,
+                                (e1 - e0) * dtype_bytes, cudaMemcpyHostToDevice, ctx->stream));
+        hd::sparse_row_sizes(ctx, d_lt.p, dtype_bytes, e0, r0, r1, threshold, rb.as<uint64_t>(),
+                             rl.as<uint64_t>());
+        if (pending >= 0) {
+          HD_CUDA(cudaEventSynchronize(pin.ev[pending]));
+          f.write(pin.buf[pending], pending_bytes);
+          pending = -1;
+        }
+        uint64_t lines = 0;
+        hd::scan_exclusive<uint64_t>(ctx, rl.as<uint64_t>(), rl.as<uint64_t>(), r1 - r0,
+                                     tot.as<uint64_t>());
+        HD_CUDA(cudaMemcpyAsync(&lines, tot.p, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        const uint64_t nb = hd::format_sparse_rows(ctx, d_lt.p, dtype_bytes, e0, r0, r1, threshold,
+                                                   rb.as<uint64_t>(), d_text.as<char>());
+        lines_total += lines;
+        const int slot = (int)(k & 1);
+        if (nb)
+          HD_CUDA(cudaMemcpyAsync(pin.buf[slot], d_text.p, nb, cudaMemcpyDeviceToHost, ctx->stream));
+        HD_CUDA(cudaEventRecord(pin.ev[slot], ctx->stream));
+        pending = slot;
+        pending_bytes = nb;
+      }
+      if (pending >= 0) {
+        HD_CUDA(cudaEventSynchronize(pin.ev[pending]));
+        f.write(pin.buf[pending], pending_bytes);
+      }
+    }
+    if (n_lines) *n_lines = lines_total;
+  });
+}
+
+int hd_reference_distances(hd_ctx *ctx, const char *ref, uint64_t ref_len, const char *fasta,
+                           uint64_t nbytes, int include_x, uint32_t **out, uint64_t *n_out) {
+  if (!ctx || !out || !n_out || (!ref && ref_len) || (!fasta && nbytes)) return HD_ERR_ARG;
+  *out = nullptr;
+  *n_out = 0;
+  return guard(ctx, [&] {
+    const uint8_t *d = stage_input(ctx, fasta, nbytes, 0);
+    hd::Records rec = hd::parse_fasta(ctx, d, nbytes, 0);
+    if (rec.max_len > ref_len)
+      fail(HD_ERR_REF_LENGTH, "Error: a sequence is longer than the reference sequence");
+    uint32_t *h = static_cast<uint32_t *>(std::malloc((rec.n ? rec.n : 1) * 4));
+    if (!h) throw std::bad_alloc();
+    try {
+      if (rec.n) {
+        DevBuf d_ref(ref_len + 16, ctx->stream), d_out(rec.n * 4, ctx->stream);
+        if (ref_len)
+          HD_CUDA(cudaMemcpyAsync(d_ref.p, ref, ref_len, cudaMemcpyHostToDevice, ctx->stream));
+        hd::reference_distances_device(ctx, rec, d_ref.as<uint8_t>(), include_x, d_out.as<uint32_t>());
+        HD_CUDA(cudaMemcpyAsync(h, d_out.p, rec.n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        HD_CUDA(cudaStreamSynchronize(ctx->stream));
+      }
+    } catch (...) {
+      std::free(h);
+      throw;
+    }
+    *out = h;
+    *n_out = rec.n;
+  });
+}
+
+int hd_alignment_reference_distances(hd_ctx *ctx, const hd_alignment *aln, const char *ref,
+                                     uint64_t ref_len, int include_x, uint32_t *out) {
+  if (!ctx || !aln || !ref || !out) return HD_ERR_ARG;
+  return guard(ctx, [&] {
+    if (include_x || aln->rule != HD_RULE_AND)
+      fail(HD_ERR_ARG, "resident reference queries need an AND-rule alignment and include_x=False");
+    if (ref_len != aln->length) fail(HD_ERR_LENGTH, kMsgLength);
+    DevBuf d_ref(ref_len + 16, ctx->stream), d_rows(aln->n_rows * 4, ctx->stream);
+    HD_CUDA(cudaMemcpyAsync(d_ref.p, ref, ref_len, cudaMemcpyHostToDevice, ctx->stream));
+    hd::alignment_query_distances(ctx, aln, d_ref.as<uint8_t>(), d_rows.as<uint32_t>());
+    std::vector<uint32_t> rows(aln->n_rows);
+    HD_CUDA(cudaMemcpy(rows.data(), d_rows.p, aln->n_rows * 4, cudaMemcpyDeviceToHost));
+    for (uint64_t k = 0; k < aln->n_input; ++k)
+      out[k] = rows[aln->seqidx.empty() ? k : aln->seqidx[k]];
+  });
+}
+
+int hd_fasta_sequence_indices(hd_ctx *ctx, const char *fasta, uint64_t nbytes, uint64_t n_limit,
+                              uint64_t **out, uint64_t *n_out) {
+  if (!ctx || !out || !n_out || (!fasta && nbytes)) return HD_ERR_ARG;
+  *out = nullptr;
+  *n_out = 0;
+  return guard(ctx, [&] {
+    const uint8_t *d = stage_input(ctx, fasta, nbytes, 0);
+    hd::Records rec = hd::parse_fasta(ctx, d, nbytes, n_limit);
+    std::vector<uint64_t> idx;
+    uint64_t nu = 0;
+    DevBuf rows = hd::dedupe(ctx, rec, &nu, idx);
+    uint64_t *h = static_cast<uint64_t *>(std::malloc((idx.size() ? idx.size() : 1) * 8));
+    if (!h) throw std::bad_alloc();
+    if (!idx.empty()) std::memcpy(h, idx.data(), idx.size() * 8);
+    *out = h;
+    *n_out = idx.size();
+  });
+}
+
+int hd_distance(hd_ctx *ctx, const char *s0, uint64_t l0, const char *s1, uint64_t l1,
+                int include_x, uint32_t *out) {
+  if (!ctx || !out || (!s0 && l0) || (!s1 && l1)) return HD_ERR_ARG;
+  return guard(ctx, [&] {
+    if (l0 != l1) fail(HD_ERR_LENGTH, kMsgLength);
+    *out = 0;
+    if (!l0) return;
+    DevBuf d(2 * l0 + 32, ctx->stream), d_out(4, ctx->stream);
+    HD_CUDA(cudaMemcpyAsync(d.p, s0, l0, cudaMemcpyHostToDevice, ctx->stream));
+    HD_CUDA(cudaMemcpyAsync(d.as<char>() + l0 + 16, s1, l1, cudaMemcpyHostToDevice, ctx->stream));
+    uint64_t offs[2] = {0, l1};
+    hd::Records rec = hd::records_from_offsets(ctx, d.as<uint8_t>() + l0 + 16, offs, 1);
+    hd::reference_distances_device(ctx, rec, d.as<uint8_t>(), include_x, d_out.as<uint32_t>());
+    HD_CUDA(cudaMemcpyAsync(out, d_out.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    HD_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int hd_measure_int_peaks(hd_ctx *ctx, double *lop3_per_s, double *popc_per_s,
+                         double *mix_pair_sites_per_s) {
+  if (!ctx) return HD_ERR_ARG;
+  return guard(ctx, [&] { hd::measure_int_peaks(ctx, lop3_per_s, popc_per_s, mix_pair_sites_per_s); });
+}
+
+int hd_last_pairwise_timing(const hd_ctx *ctx, double *ms, uint64_t *tiles) {
+  if (!ctx) return HD_ERR_ARG;
+  if (ms) *ms = ctx->last_pair_ms;
+  if (tiles) *tiles = ctx->last_pair_tiles;
+  return HD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,218 @@
+// Device-side text writers.
+//
+// Replaces lower_triangular_lines / partial_write_lower_triangular
+// (include/hamming/hamming_utils.hh:19-104) and DataSet::dump_sparse
+// (include/hamming/hamming.hh:79-114), which format on the CPU with fmt.
+// One warp per row: the row's entries are contiguous in the lower triangle;
+// per 32 entries each lane computes its text length, a warp prefix sum places
+// it, and the lane writes its digits. Row starts come from a device scan of
+// per-row text lengths.
+#include "hd_internal.cuh"
+
+namespace hd {
+
+__device__ inline uint32_t ndig(uint32_t v) {
+  return v < 10u ? 1 : v < 100u ? 2 : v < 1000u ? 3 : v < 10000u ? 4 : v < 100000u ? 5
+       : v < 1000000u ? 6 : v < 10000000u ? 7 : v < 100000000u ? 8 : v < 1000000000u ? 9 : 10;
+}
+
+__device__ inline void put_dec(char *dst, uint32_t v, uint32_t nd) {
+  for (int k = (int)nd - 1; k >= 0; --k) {
+    dst[k] = (char)('0' + v % 10u);
+    v /= 10u;
+  }
+}
+
+__host__ __device__ inline uint64_t row_index(uint64_t i) { return i * (i - 1) / 2; }
+
+// --------------------------------------------------- lower-triangular text
+// Row i (i >= 1): "d(i,0),d(i,1),...,d(i,i-1)\n".
+template <typename T>
+__global__ void k_lt_len(const T *lt, uint64_t lt_base, uint64_t i_lo, uint64_t rows,
+                         uint64_t *row_len) {
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t q = wid; q < rows; q += nwarps) {
+    const uint64_t i = i_lo + q;
+    const T *rp = lt + (row_index(i) - lt_base);
+    uint64_t len = 0;
+    for (uint64_t j = lane; j < i; j += 32) len += ndig((uint32_t)rp[j]) + 1;
+    len = warp_sum(len);
+    if (lane == 0) row_len[q] = len;
+  }
+}
+
+template <typename T>
+__global__ void k_lt_write(const T *lt, uint64_t lt_base, uint64_t i_lo, uint64_t rows,
+                           const uint64_t *row_off, char *text) {
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t q = wid; q < rows; q += nwarps) {
+    const uint64_t i = i_lo + q;
+    const T *rp = lt + (row_index(i) - lt_base);
+    uint64_t pos = row_off[q];
+    for (uint64_t j0 = 0; j0 < i; j0 += 32) {
+      const uint64_t j = j0 + lane;
+      const bool on = j < i;
+      const uint32_t v = on ? (uint32_t)rp[j] : 0u;
+      const uint32_t nd = on ? ndig(v) : 0u;
+      const uint32_t len = on ? nd + 1 : 0u;
+      const uint32_t inc = warp_incl_scan(len);
+      if (on) {
+        char *dst = text + pos + inc - len;
+        put_dec(dst, v, nd);
+        dst[nd] = (j + 1 == i) ? '\n' : ',';
+      }
+      pos += __shfl_sync(0xffffffffu, inc, 31);
+    }
+  }
+}
+
+static unsigned warp_grid(hd_ctx *ctx, uint64_t rows) {
+  uint64_t g = ceil_div(rows * 32, 256);
+  uint64_t cap = (uint64_t)ctx->sm_count * 16;
+  return (unsigned)(g < cap ? (g ? g : 1) : cap);
+}
+
+uint64_t lt_text_bound(uint64_t i_lo, uint64_t i_hi, int dtype_bytes) {
+  if (i_lo < 1) i_lo = 1;
+  if (i_hi <= i_lo) return 0;
+  const uint64_t entries = row_index(i_hi) - row_index(i_lo);
+  const uint64_t per = dtype_bytes == 1 ? 4 : dtype_bytes == 2 ? 6 : 11;
+  return entries * per;
+}
+
+uint64_t format_lt_rows(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint64_t lt_base,
+                        uint64_t i_lo, uint64_t i_hi, char *d_text) {
+  if (i_lo < 1) i_lo = 1;
+  if (i_hi <= i_lo) return 0;
+  const uint64_t rows = i_hi - i_lo;
+  cudaStream_t st = ctx->stream;
+  DevBuf len(rows * 8, st), off(rows * 8, st), tot(8, st);
+  const unsigned g = warp_grid(ctx, rows);
+  if (dtype_bytes == 1)
+    k_lt_len<uint8_t><<<g, 256, 0, st>>>((const uint8_t *)d_lt, lt_base, i_lo, rows, len.as<uint64_t>());
+  else if (dtype_bytes == 2)
+    k_lt_len<uint16_t><<<g, 256, 0, st>>>((const uint16_t *)d_lt, lt_base, i_lo, rows, len.as<uint64_t>());
+  else
+    k_lt_len<uint32_t><<<g, 256, 0, st>>>((const uint32_t *)d_lt, lt_base, i_lo, rows, len.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+  scan_exclusive<uint64_t>(ctx, len.as<uint64_t>(), off.as<uint64_t>(), rows, tot.as<uint64_t>());
+  if (dtype_bytes == 1)
+    k_lt_write<uint8_t><<<g, 256, 0, st>>>((const uint8_t *)d_lt, lt_base, i_lo, rows, off.as<uint64_t>(), d_text);
+  else if (dtype_bytes == 2)
+    k_lt_write<uint16_t><<<g, 256, 0, st>>>((const uint16_t *)d_lt, lt_base, i_lo, rows, off.as<uint64_t>(), d_text);
+  else
+    k_lt_write<uint32_t><<<g, 256, 0, st>>>((const uint32_t *)d_lt, lt_base, i_lo, rows, off.as<uint64_t>(), d_text);
+  HD_LAUNCHED(ctx);
+  uint64_t total = 0;
+  HD_CUDA(cudaMemcpyAsync(&total, tot.p, 8, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  return total;
+}
+
+// ----------------------------------------------------------- sparse text
+// Lines "i j d\n" for j < i with d <= threshold (integer compare, as the
+// reference's `*d <= threshold`).
+template <typename T>
+__global__ void k_sp_len(const T *lt, uint64_t lt_base, uint64_t i_lo, uint64_t rows, int64_t thr,
+                         uint64_t *row_bytes, uint64_t *row_lines) {
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t q = wid; q < rows; q += nwarps) {
+    const uint64_t i = i_lo + q;
+    const T *rp = lt + (row_index(i) - lt_base);
+    const uint32_t ndi = ndig((uint32_t)i);
+    uint64_t bytes = 0, lines = 0;
+    for (uint64_t j = lane; j < i; j += 32) {
+      const uint32_t d = rp[j];
+      if ((int64_t)d <= thr) {
+        bytes += ndi + ndig((uint32_t)j) + ndig(d) + 3;
+        ++lines;
+      }
+    }
+    bytes = warp_sum(bytes);
+    lines = warp_sum(lines);
+    if (lane == 0) {
+      row_bytes[q] = bytes;
+      if (row_lines) row_lines[q] = lines;
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_sp_write(const T *lt, uint64_t lt_base, uint64_t i_lo, uint64_t rows, int64_t thr,
+                           const uint64_t *row_off, char *text) {
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t q = wid; q < rows; q += nwarps) {
+    const uint64_t i = i_lo + q;
+    const T *rp = lt + (row_index(i) - lt_base);
+    const uint32_t ndi = ndig((uint32_t)i);
+    uint64_t pos = row_off[q];
+    for (uint64_t j0 = 0; j0 < i; j0 += 32) {
+      const uint64_t j = j0 + lane;
+      const uint32_t d = j < i ? (uint32_t)rp[j] : 0u;
+      const bool on = j < i && (int64_t)d <= thr;
+      const uint32_t ndj = ndig((uint32_t)j), ndd = ndig(d);
+      const uint32_t len = on ? ndi + ndj + ndd + 3 : 0u;
+      const uint32_t inc = warp_incl_scan(len);
+      if (on) {
+        char *dst = text + pos + inc - len;
+        put_dec(dst, (uint32_t)i, ndi);
+        dst[ndi] = ' ';
+        put_dec(dst + ndi + 1, (uint32_t)j, ndj);
+        dst[ndi + 1 + ndj] = ' ';
+        put_dec(dst + ndi + ndj + 2, d, ndd);
+        dst[ndi + ndj + ndd + 2] = '\n';
+      }
+      pos += __shfl_sync(0xffffffffu, inc, 31);
+    }
+  }
+}
+
+void sparse_row_sizes(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint64_t lt_base,
+                      uint64_t i_lo, uint64_t i_hi, int64_t threshold, uint64_t *d_row_bytes,
+                      uint64_t *d_row_lines) {
+  if (i_lo < 1) i_lo = 1;
+  if (i_hi <= i_lo) return;
+  const uint64_t rows = i_hi - i_lo;
+  const unsigned g = warp_grid(ctx, rows);
+  cudaStream_t st = ctx->stream;
+  if (dtype_bytes == 1)
+    k_sp_len<uint8_t><<<g, 256, 0, st>>>((const uint8_t *)d_lt, lt_base, i_lo, rows, threshold, d_row_bytes, d_row_lines);
+  else if (dtype_bytes == 2)
+    k_sp_len<uint16_t><<<g, 256, 0, st>>>((const uint16_t *)d_lt, lt_base, i_lo, rows, threshold, d_row_bytes, d_row_lines);
+  else
+    k_sp_len<uint32_t><<<g, 256, 0, st>>>((const uint32_t *)d_lt, lt_base, i_lo, rows, threshold, d_row_bytes, d_row_lines);
+  HD_LAUNCHED(ctx);
+}
+
+uint64_t format_sparse_rows(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint64_t lt_base,
+                            uint64_t i_lo, uint64_t i_hi, int64_t threshold,
+                            const uint64_t *d_row_bytes, char *d_text) {
+  if (i_lo < 1) i_lo = 1;
+  if (i_hi <= i_lo) return 0;
+  const uint64_t rows = i_hi - i_lo;
+  cudaStream_t st = ctx->stream;
+  DevBuf off(rows * 8, st), tot(8, st);
+  scan_exclusive<uint64_t>(ctx, d_row_bytes, off.as<uint64_t>(), rows, tot.as<uint64_t>());
+  const unsigned g = warp_grid(ctx, rows);
+  if (dtype_bytes == 1)
+    k_sp_write<uint8_t><<<g, 256, 0, st>>>((const uint8_t *)d_lt, lt_base, i_lo, rows, threshold, off.as<uint64_t>(), d_text);
+  else if (dtype_bytes == 2)
+    k_sp_write<uint16_t><<<g, 256, 0, st>>>((const uint16_t *)d_lt, lt_base, i_lo, rows, threshold, off.as<uint64_t>(), d_text);
+  else
+    k_sp_write<uint32_t><<<g, 256, 0, st>>>((const uint32_t *)d_lt, lt_base, i_lo, rows, threshold, off.as<uint64_t>(), d_text);
+  HD_LAUNCHED(ctx);
+  uint64_t total = 0;
+  HD_CUDA(cudaMemcpyAsync(&total, tot.p, 8, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  return total;
+}
+
+}  // namespace hd

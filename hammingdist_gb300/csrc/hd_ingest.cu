@@ -1,0 +1,708 @@
+// Device FASTA ingest: newline index, record table, duplicate removal,
+// consensus counts, bit-plane packing and reference distances.
+//
+// Replaces (ssciwr/hammingdist 1.4.0): read_fasta src/hamming_impl.cc:200-242,
+// validate_data :80-91, to_dense_data/from_string :190-198/:244-267, the
+// consensus of get_reference_expression :142-168 as used by the heuristic of
+// include/hamming/hamming_impl.hh:104-118, and fasta_reference_distances /
+// fasta_sequence_indices src/hamming.cc:76-141.
+#include "hd_internal.cuh"
+
+namespace hd {
+
+// ------------------------------------------------------------ code tables
+// Bit p of a code = membership in bit plane p. A pair of sites matches when
+// their codes share a bit, so '-' (all ones) matches everything and a code of
+// 0 matches nothing.
+//  kCodesAnd:     the reference's 4-bit codes (src/hamming_impl.cc:23-44 with
+//                 include_x = false): A C G T one-hot, '-' = 1111, else 0000.
+//  kCodesSparse:  the sparse rule (src/hamming_impl.cc:93-129) with X invalid:
+//                 codes differ and neither is '-' <=> no shared bit, with a
+//                 fifth plane for the class of all invalid bytes.
+//  kCodesSparseX: the same with X a symbol of its own (6 planes).
+void code_table(int table, uint8_t out[256]) {
+  for (int c = 0; c < 256; ++c) out[c] = 0;
+  if (table == kCodesSparse)
+    for (int c = 0; c < 256; ++c) out[c] = 0x10;
+  if (table == kCodesSparseX)
+    for (int c = 0; c < 256; ++c) out[c] = 0x20;
+  out['A'] = 0x1;
+  out['C'] = 0x2;
+  out['G'] = 0x4;
+  out['T'] = 0x8;
+  if (table == kCodesAnd) out['-'] = 0x0f;
+  if (table == kCodesSparse) out['-'] = 0x1f;
+  if (table == kCodesSparseX) {
+    out['X'] = 0x10;
+    out['-'] = 0x3f;
+  }
+}
+
+struct Table256 {
+  uint8_t v[256];
+};
+
+// ------------------------------------------------------------ newline index
+constexpr int kNlThreads = 256;
+constexpr int kNlIters = 16;
+constexpr uint64_t kNlWarpBytes = 32ull * 16 * kNlIters;                  // 8 KB
+constexpr uint64_t kNlBlockBytes = kNlWarpBytes * (kNlThreads / 32);      // 64 KB
+
+__device__ inline uint32_t nl_nibble(uint32_t w) {
+  uint32_t e = __vcmpeq4(w, 0x0a0a0a0au) & 0x01010101u;
+  return (e | (e >> 7) | (e >> 14) | (e >> 21)) & 0xfu;
+}
+
+// 16-bit mask of '\n' bytes in p[off, off+16).
+__device__ inline uint32_t nl_mask16(const uint8_t *p, uint64_t off, uint64_t n) {
+  if (off + 16 <= n) {
+    uint4 v = __ldg(reinterpret_cast<const uint4 *>(p + off));
+    return nl_nibble(v.x) | (nl_nibble(v.y) << 4) | (nl_nibble(v.z) << 8) | (nl_nibble(v.w) << 12);
+  }
+  uint32_t m = 0;
+  for (int k = 0; k < 16; ++k)
+    if (off + k < n && p[off + k] == '\n') m |= 1u << k;
+  return m;
+}
+
+__global__ void k_nl_count(const uint8_t *p, uint64_t n, uint64_t *counts) {
+  __shared__ uint64_t tmp[33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t base = blockIdx.x * kNlBlockBytes + warp * kNlWarpBytes + lane * 16;
+  uint64_t c = 0;
+#pragma unroll 4
+  for (int it = 0; it < kNlIters; ++it) c += __popc(nl_mask16(p, base + it * 512ull, n));
+  uint64_t tot;
+  block_excl_scan<uint64_t>(c, tmp, tot);
+  if (threadIdx.x == 0) counts[blockIdx.x] = tot;
+}
+
+// Writes the positions of every '\n' in increasing order.
+__global__ void k_nl_write(const uint8_t *p, uint64_t n, const uint64_t *block_off, uint64_t *nl) {
+  __shared__ uint64_t wt[kNlThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t wbase = blockIdx.x * kNlBlockBytes + warp * kNlWarpBytes;
+  uint32_t c = 0;
+  for (int it = 0; it < kNlIters; ++it) c += __popc(nl_mask16(p, wbase + it * 512ull + lane * 16, n));
+  c = warp_sum(c);
+  if (lane == 0) wt[warp] = c;
+  __syncthreads();
+  uint64_t off = block_off[blockIdx.x];
+  for (int w = 0; w < warp; ++w) off += wt[w];
+  for (int it = 0; it < kNlIters; ++it) {
+    uint64_t at = wbase + it * 512ull + lane * 16;
+    uint32_t m = nl_mask16(p, at, n);
+    uint32_t cnt = __popc(m);
+    uint32_t inc = warp_incl_scan(cnt);
+    uint64_t pos = off + inc - cnt;
+    while (m) {
+      int k = __ffs(m) - 1;
+      nl[pos++] = at + k;
+      m &= m - 1;
+    }
+    off += __shfl_sync(0xffffffffu, inc, 31);
+  }
+}
+
+struct ParseSummary {
+  unsigned long long m_nl;      // newlines
+  unsigned long long lines;     // M
+  unsigned long long R;         // records before the n limit
+  unsigned long long Rk;        // records kept
+  unsigned long long max_len;
+  unsigned long long len0;
+  unsigned int unterminated;    // the last line has no '\n'
+  unsigned int unequal;
+  unsigned int multi;           // some record spans several non-empty lines
+  unsigned int pad;
+};
+
+__global__ void k_nl_summary(const uint8_t *p, uint64_t n, const uint64_t *m_nl, ParseSummary *s) {
+  s->m_nl = *m_nl;
+  s->unterminated = (n > 0 && p[n - 1] != '\n') ? 1u : 0u;
+  s->lines = *m_nl + s->unterminated;
+}
+
+__device__ inline void line_range(uint64_t k, const uint64_t *nl, uint64_t m_nl, uint64_t n,
+                                  uint64_t &start, uint64_t &end) {
+  start = k ? nl[k - 1] + 1 : 0;
+  end = k < m_nl ? nl[k] : n;
+}
+
+// hdr[k] = line k (k >= 1) is a header: non-empty and starting with '>'.
+__global__ void k_lines(const uint8_t *p, uint64_t n, const uint64_t *nl, uint64_t m_nl, uint64_t M,
+                        uint32_t *hdr) {
+  uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (k >= M) return;
+  uint64_t s, e;
+  line_range(k, nl, m_nl, n, s, e);
+  hdr[k] = (k >= 1 && e > s && p[s] == '>') ? 1u : 0u;
+}
+
+// Number of records the getline loop of read_fasta produces
+// (src/hamming_impl.cc:216-233): the first line is skipped; every later
+// header closes a record; the loop ends when the stream reaches its end,
+// which happens on reading an unterminated last line.
+__global__ void k_rec_count(const uint64_t *H_total, const uint32_t *hdr, uint64_t n_limit,
+                            ParseSummary *s) {
+  uint64_t M = s->lines, R;
+  if (M == 0) R = 0;
+  else if (M == 1) R = s->unterminated ? 0 : 1;
+  else R = *H_total + 1 - ((hdr[M - 1] && s->unterminated) ? 1 : 0);
+  s->R = R;
+  s->Rk = (n_limit && n_limit < R) ? n_limit : R;
+}
+
+__global__ void k_records(const uint8_t *p, uint64_t n, const uint64_t *nl, uint64_t m_nl,
+                          uint64_t M, const uint32_t *hdr, const uint64_t *H, const ParseSummary *s,
+                          unsigned long long *rec_len, unsigned int *rec_nseg,
+                          uint64_t *rec_start) {
+  uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (k == 0 || k >= M || hdr[k]) return;
+  uint64_t r = H[k];
+  if (r >= s->Rk) return;
+  uint64_t st, e;
+  line_range(k, nl, m_nl, n, st, e);
+  if (e == st) return;
+  atomicAdd(&rec_len[r], (unsigned long long)(e - st));
+  atomicAdd(&rec_nseg[r], 1u);
+  rec_start[r] = st;
+}
+
+__global__ void k_validate(const unsigned long long *rec_len, const unsigned int *rec_nseg,
+                           ParseSummary *s) {
+  uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (r >= s->Rk) return;
+  unsigned long long l = rec_len[r];
+  if (r == 0) s->len0 = l;
+  if (l != rec_len[0]) atomicOr(&s->unequal, 1u);
+  if (rec_nseg[r] > 1) atomicOr(&s->multi, 1u);
+  atomicMax(&s->max_len, l);
+}
+
+// Gather of multi-line records: masked line lengths, then line copies.
+__global__ void k_seqline_len(const uint64_t *nl, uint64_t m_nl, uint64_t n, uint64_t M,
+                              const uint32_t *hdr, const uint64_t *H, const ParseSummary *s,
+                              uint64_t *len) {
+  uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (k >= M) return;
+  uint64_t st, e;
+  line_range(k, nl, m_nl, n, st, e);
+  len[k] = (k >= 1 && !hdr[k] && H[k] < s->Rk) ? e - st : 0;
+}
+
+__global__ void k_gather_lines(const uint8_t *p, const uint64_t *nl, uint64_t m_nl, uint64_t n,
+                               uint64_t M, const uint64_t *len, const uint64_t *dst_off,
+                               uint8_t *dst) {
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t k = wid; k < M; k += nwarps) {
+    uint64_t l = len[k];
+    if (!l) continue;
+    uint64_t st = k ? nl[k - 1] + 1 : 0;
+    for (uint64_t i = lane; i < l; i += 32) dst[dst_off[k] + i] = p[st + i];
+  }
+}
+
+static unsigned grid_for(uint64_t n, int threads) {
+  uint64_t g = ceil_div(n ? n : 1, threads);
+  return (unsigned)(g > 0x7fffffffull ? 0x7fffffffull : g);
+}
+
+Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_t n_limit) {
+  cudaStream_t st = ctx->stream;
+  Records rec;
+  uint64_t nblk = ceil_div(nbytes ? nbytes : 1, kNlBlockBytes);
+  DevBuf counts(nblk * 8, st), offs(nblk * 8, st), total(8, st), sumbuf(sizeof(ParseSummary), st);
+  ParseSummary *d_sum = sumbuf.as<ParseSummary>();
+  HD_CUDA(cudaMemsetAsync(d_sum, 0, sizeof(ParseSummary), st));
+  k_nl_count<<<(unsigned)nblk, kNlThreads, 0, st>>>(d_file, nbytes, counts.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+  scan_exclusive<uint64_t>(ctx, counts.as<uint64_t>(), offs.as<uint64_t>(), nblk,
+                           total.as<uint64_t>());
+  k_nl_summary<<<1, 1, 0, st>>>(d_file, nbytes, total.as<uint64_t>(), d_sum);
+  HD_LAUNCHED(ctx);
+  ParseSummary hs;
+  HD_CUDA(cudaMemcpyAsync(&hs, d_sum, sizeof(hs), cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  const uint64_t m_nl = hs.m_nl, M = hs.lines;
+  DevBuf nl((m_nl + 1) * 8, st);
+  if (m_nl) {
+    k_nl_write<<<(unsigned)nblk, kNlThreads, 0, st>>>(d_file, nbytes, offs.as<uint64_t>(),
+                                                       nl.as<uint64_t>());
+    HD_LAUNCHED(ctx);
+  }
+  DevBuf hdr((M + 1) * 4, st), H((M + 1) * 8, st), htot(8, st);
+  HD_CUDA(cudaMemsetAsync(htot.p, 0, 8, st));
+  if (M) {
+    k_lines<<<grid_for(M, 256), 256, 0, st>>>(d_file, nbytes, nl.as<uint64_t>(), m_nl, M,
+                                              hdr.as<uint32_t>());
+    HD_LAUNCHED(ctx);
+    scan_exclusive<uint32_t>(ctx, hdr.as<uint32_t>(), H.as<uint64_t>(), M, htot.as<uint64_t>());
+  }
+  k_rec_count<<<1, 1, 0, st>>>(htot.as<uint64_t>(), hdr.as<uint32_t>(), n_limit, d_sum);
+  HD_LAUNCHED(ctx);
+  const uint64_t cap = M + 1;  // records <= lines
+  rec.rec_len = DevBuf(cap * 8, st);
+  rec.rec_start = DevBuf(cap * 8, st);
+  DevBuf nseg(cap * 4, st);
+  HD_CUDA(cudaMemsetAsync(rec.rec_len.p, 0, cap * 8, st));
+  HD_CUDA(cudaMemsetAsync(rec.rec_start.p, 0, cap * 8, st));
+  HD_CUDA(cudaMemsetAsync(nseg.p, 0, cap * 4, st));
+  if (M) {
+    k_records<<<grid_for(M, 256), 256, 0, st>>>(
+        d_file, nbytes, nl.as<uint64_t>(), m_nl, M, hdr.as<uint32_t>(), H.as<uint64_t>(), d_sum,
+        rec.rec_len.as<unsigned long long>(), nseg.as<unsigned int>(), rec.rec_start.as<uint64_t>());
+    HD_LAUNCHED(ctx);
+    k_validate<<<grid_for(cap, 256), 256, 0, st>>>(rec.rec_len.as<unsigned long long>(),
+                                                   nseg.as<unsigned int>(), d_sum);
+    HD_LAUNCHED(ctx);
+  }
+  HD_CUDA(cudaMemcpyAsync(&hs, d_sum, sizeof(hs), cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  rec.n = hs.Rk;
+  rec.len0 = hs.len0;
+  rec.max_len = hs.max_len;
+  rec.all_equal = hs.unequal == 0;
+  rec.base = d_file;
+  if (hs.multi) {
+    // records spanning several lines: concatenate them into one buffer
+    DevBuf len(M * 8, st), dst(M * 8, st), gtot(8, st);
+    k_seqline_len<<<grid_for(M, 256), 256, 0, st>>>(nl.as<uint64_t>(), m_nl, nbytes, M,
+                                                    hdr.as<uint32_t>(), H.as<uint64_t>(), d_sum,
+                                                    len.as<uint64_t>());
+    HD_LAUNCHED(ctx);
+    scan_exclusive<uint64_t>(ctx, len.as<uint64_t>(), dst.as<uint64_t>(), M, gtot.as<uint64_t>());
+    uint64_t total_bytes = 0;
+    HD_CUDA(cudaMemcpyAsync(&total_bytes, gtot.p, 8, cudaMemcpyDeviceToHost, st));
+    HD_CUDA(cudaStreamSynchronize(st));
+    rec.gathered = DevBuf(total_bytes + 16, st);
+    k_gather_lines<<<grid_for(M * 32, 256), 256, 0, st>>>(d_file, nl.as<uint64_t>(), m_nl, nbytes,
+                                                          M, len.as<uint64_t>(),
+                                                          dst.as<uint64_t>(),
+                                                          rec.gathered.as<uint8_t>());
+    HD_LAUNCHED(ctx);
+    if (rec.n)
+      scan_exclusive<uint64_t>(ctx, rec.rec_len.as<uint64_t>(), rec.rec_start.as<uint64_t>(),
+                               rec.n, gtot.as<uint64_t>());
+    rec.base = rec.gathered.as<uint8_t>();
+  }
+  return rec;
+}
+
+Records records_from_offsets(hd_ctx *ctx, const uint8_t *d_bytes, const uint64_t *h_offsets,
+                             uint64_t n) {
+  Records rec;
+  rec.n = n;
+  rec.base = d_bytes;
+  std::vector<uint64_t> start(n ? n : 1), len(n ? n : 1);
+  for (uint64_t k = 0; k < n; ++k) {
+    start[k] = h_offsets[k] - h_offsets[0];
+    len[k] = h_offsets[k + 1] - h_offsets[k];
+    rec.max_len = len[k] > rec.max_len ? len[k] : rec.max_len;
+    if (len[k] != len[0]) rec.all_equal = false;
+  }
+  rec.len0 = n ? len[0] : 0;
+  rec.rec_start = DevBuf(start.size() * 8, ctx->stream);
+  rec.rec_len = DevBuf(len.size() * 8, ctx->stream);
+  HD_CUDA(cudaMemcpyAsync(rec.rec_start.p, start.data(), start.size() * 8, cudaMemcpyHostToDevice,
+                          ctx->stream));
+  HD_CUDA(cudaMemcpyAsync(rec.rec_len.p, len.data(), len.size() * 8, cudaMemcpyHostToDevice,
+                          ctx->stream));
+  HD_CUDA(cudaStreamSynchronize(ctx->stream));  // host vectors go out of scope
+  return rec;
+}
+
+// ---------------------------------------------------------------- dedupe
+__device__ inline uint64_t mix64(uint64_t x) {
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  x ^= x >> 31;
+  return x;
+}
+
+constexpr unsigned long long kEmpty = ~0ull;
+
+// Hash of each record's bytes: a sum of position-keyed 64-bit mixes of its
+// 4-byte groups (any two different records collide with probability ~2^-64;
+// equal hashes are verified byte by byte).
+__global__ void k_hash(const uint8_t *base, const uint64_t *rs, const uint64_t *rl, uint64_t R,
+                       uint64_t *out) {
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t r = wid; r < R; r += nwarps) {
+    const uint8_t *p = base + rs[r];
+    const uint64_t len = rl[r];
+    uint64_t h = 0;
+    for (uint64_t s = (uint64_t)lane * 4; s < len; s += 128) {
+      uint32_t w = p[s];
+      if (s + 1 < len) w |= (uint32_t)p[s + 1] << 8;
+      if (s + 2 < len) w |= (uint32_t)p[s + 2] << 16;
+      if (s + 3 < len) w |= (uint32_t)p[s + 3] << 24;
+      h += mix64(((s >> 2) << 32) ^ w ^ 0x9e3779b97f4a7c15ull);
+    }
+    h = warp_sum(h);
+    if (lane == 0) {
+      uint64_t v = mix64(h ^ (len * 0xd6e8feb86659fd93ull));
+      out[r] = v == kEmpty ? v - 1 : v;
+    }
+  }
+}
+
+__device__ inline uint64_t slot_of(uint64_t h, uint64_t mask) { return (h ^ (h >> 29)) & mask; }
+
+__global__ void k_tab_insert(const uint64_t *hash, const uint64_t *list, uint64_t cnt,
+                             unsigned long long *keys, unsigned long long *mins, uint64_t mask) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  uint64_t r = list ? list[i] : i;
+  unsigned long long h = hash[r];
+  uint64_t slot = slot_of(h, mask);
+  for (;;) {
+    unsigned long long prev = atomicCAS(&keys[slot], kEmpty, h);
+    if (prev == kEmpty || prev == h) {
+      atomicMin(&mins[slot], (unsigned long long)r);
+      return;
+    }
+    slot = (slot + 1) & mask;
+  }
+}
+
+// Each record against the lowest-index record of equal hash: equal bytes ->
+// duplicate; different bytes (a hash collision) -> next round.
+__global__ void k_tab_verify(const uint8_t *base, const uint64_t *rs, const uint64_t *rl,
+                             const uint64_t *hash, const uint64_t *list, uint64_t cnt,
+                             const unsigned long long *keys, const unsigned long long *mins,
+                             uint64_t mask, uint64_t *dup, uint64_t *next,
+                             unsigned long long *next_cnt) {
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t i = wid; i < cnt; i += nwarps) {
+    uint64_t r = list ? list[i] : i;
+    uint64_t rep = 0;
+    if (lane == 0) {
+      unsigned long long h = hash[r];
+      uint64_t slot = slot_of(h, mask);
+      while (keys[slot] != h) slot = (slot + 1) & mask;
+      rep = mins[slot];
+    }
+    rep = __shfl_sync(0xffffffffu, rep, 0);
+    if (rep == r) {
+      if (lane == 0) dup[r] = r;
+      continue;
+    }
+    bool eq = rl[r] == rl[rep];
+    if (eq) {
+      const uint8_t *a = base + rs[r], *b = base + rs[rep];
+      const uint64_t len = rl[r];
+      for (uint64_t s = lane; s < len; s += 32) {
+        if (__any_sync(__activemask(), a[s] != b[s])) {
+          eq = false;
+          break;
+        }
+      }
+      eq = __all_sync(0xffffffffu, eq);
+    }
+    if (lane == 0) {
+      if (eq) {
+        dup[r] = rep;
+      } else {
+        unsigned long long at = atomicAdd(next_cnt, 1ull);
+        next[at] = r;
+      }
+    }
+  }
+}
+
+__global__ void k_unique_flags(const uint64_t *dup, uint64_t R, uint32_t *flag) {
+  uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (r < R) flag[r] = dup[r] == r ? 1u : 0u;
+}
+
+__global__ void k_number(const uint64_t *dup, const uint64_t *uidx, uint64_t R, uint64_t *seqidx,
+                         uint64_t *unique_rec) {
+  uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  seqidx[r] = uidx[dup[r]];
+  if (dup[r] == r) unique_rec[uidx[r]] = r;
+}
+
+DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<uint64_t> &seqidx) {
+  cudaStream_t st = ctx->stream;
+  const uint64_t R = rec.n;
+  seqidx.assign(R, 0);
+  DevBuf unique_rec((R ? R : 1) * 8, st);
+  if (R == 0) {
+    *n_unique = 0;
+    return unique_rec;
+  }
+  uint64_t T = 64;
+  while (T < 2 * R) T <<= 1;
+  DevBuf hash(R * 8, st), dup(R * 8, st), keys(T * 8, st), mins(T * 8, st);
+  DevBuf lists[2] = {DevBuf(R * 8, st), DevBuf(R * 8, st)};
+  DevBuf cnt(8, st);
+  unsigned warps_grid = grid_for(R * 32, 256);
+  k_hash<<<warps_grid, 256, 0, st>>>(rec.base, rec.rec_start.as<uint64_t>(),
+                                     rec.rec_len.as<uint64_t>(), R, hash.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+  uint64_t todo = R;
+  const uint64_t *list = nullptr;
+  for (int round = 0; todo; ++round) {
+    uint64_t *next = lists[round & 1].as<uint64_t>();
+    HD_CUDA(cudaMemsetAsync(keys.p, 0xff, T * 8, st));
+    HD_CUDA(cudaMemsetAsync(mins.p, 0xff, T * 8, st));
+    HD_CUDA(cudaMemsetAsync(cnt.p, 0, 8, st));
+    k_tab_insert<<<grid_for(todo, 256), 256, 0, st>>>(hash.as<uint64_t>(), list, todo,
+                                                      keys.as<unsigned long long>(),
+                                                      mins.as<unsigned long long>(), T - 1);
+    HD_LAUNCHED(ctx);
+    k_tab_verify<<<grid_for(todo * 32, 256), 256, 0, st>>>(
+        rec.base, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(), hash.as<uint64_t>(),
+        list, todo, keys.as<unsigned long long>(), mins.as<unsigned long long>(), T - 1,
+        dup.as<uint64_t>(), next, cnt.as<unsigned long long>());
+    HD_LAUNCHED(ctx);
+    uint64_t left = 0;
+    HD_CUDA(cudaMemcpyAsync(&left, cnt.p, 8, cudaMemcpyDeviceToHost, st));
+    HD_CUDA(cudaStreamSynchronize(st));
+    if (left >= todo) fail(HD_ERR_CUDA, "duplicate removal made no progress");
+    todo = left;
+    list = next;
+  }
+  DevBuf flag(R * 4, st), uidx(R * 8, st), tot(8, st), d_seqidx(R * 8, st);
+  k_unique_flags<<<grid_for(R, 256), 256, 0, st>>>(dup.as<uint64_t>(), R, flag.as<uint32_t>());
+  HD_LAUNCHED(ctx);
+  scan_exclusive<uint32_t>(ctx, flag.as<uint32_t>(), uidx.as<uint64_t>(), R, tot.as<uint64_t>());
+  k_number<<<grid_for(R, 256), 256, 0, st>>>(dup.as<uint64_t>(), uidx.as<uint64_t>(), R,
+                                             d_seqidx.as<uint64_t>(), unique_rec.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+  HD_CUDA(cudaMemcpyAsync(n_unique, tot.p, 8, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaMemcpyAsync(seqidx.data(), d_seqidx.p, R * 8, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  return unique_rec;
+}
+
+// -------------------------------------------------------------- consensus
+constexpr int kColRows = 128;
+
+__global__ void k_colcount(const uint8_t *base, const uint64_t *rs, const uint64_t *rows,
+                           uint64_t n_rows, uint64_t L, unsigned int *counts) {
+  uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (s >= L) return;
+  uint64_t u0 = (uint64_t)blockIdx.y * kColRows;
+  uint64_t u1 = u0 + kColRows < n_rows ? u0 + kColRows : n_rows;
+  unsigned a = 0, c = 0, g = 0, t = 0;
+  for (uint64_t u = u0; u < u1; ++u) {
+    uint64_t r = rows ? rows[u] : u;
+    uint8_t ch = base[rs[r] + s];
+    a += ch == 'A';
+    c += ch == 'C';
+    g += ch == 'G';
+    t += ch == 'T';
+  }
+  if (a) atomicAdd(&counts[4 * s + 0], a);
+  if (c) atomicAdd(&counts[4 * s + 1], c);
+  if (g) atomicAdd(&counts[4 * s + 2], g);
+  if (t) atomicAdd(&counts[4 * s + 3], t);
+}
+
+__global__ void k_colmax_sum(const unsigned int *counts, uint64_t L, unsigned long long *sum) {
+  __shared__ uint64_t tmp[33];
+  uint64_t v = 0;
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < L;
+       s += (uint64_t)gridDim.x * blockDim.x) {
+    unsigned m = max(max(counts[4 * s], counts[4 * s + 1]), max(counts[4 * s + 2], counts[4 * s + 3]));
+    v += m;
+  }
+  uint64_t tot;
+  block_excl_scan<uint64_t>(v, tmp, tot);
+  if (threadIdx.x == 0) atomicAdd(sum, (unsigned long long)tot);
+}
+
+uint64_t consensus_matches(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows,
+                           uint64_t n_rows) {
+  cudaStream_t st = ctx->stream;
+  const uint64_t L = rec.len0;
+  if (!L || !n_rows) return 0;
+  DevBuf counts(L * 16, st), sum(8, st);
+  HD_CUDA(cudaMemsetAsync(counts.p, 0, L * 16, st));
+  HD_CUDA(cudaMemsetAsync(sum.p, 0, 8, st));
+  uint64_t chunks = ceil_div(n_rows, kColRows);
+  for (uint64_t c0 = 0; c0 < chunks; c0 += 65535) {
+    uint64_t cn = chunks - c0 < 65535 ? chunks - c0 : 65535;
+    dim3 grid((unsigned)ceil_div(L, 256), (unsigned)cn);
+    const uint64_t *rows = d_rows ? d_rows + c0 * kColRows : nullptr;
+    // without a row list the rows are records [c0*kColRows, ...): shift the starts
+    const uint64_t *rs = rec.rec_start.as<uint64_t>() + (d_rows ? 0 : c0 * kColRows);
+    k_colcount<<<grid, 256, 0, st>>>(rec.base, rs, rows, n_rows - c0 * kColRows, L,
+                                     counts.as<unsigned int>());
+    HD_LAUNCHED(ctx);
+  }
+  k_colmax_sum<<<(unsigned)(ctx->sm_count * 4), 256, 0, st>>>(counts.as<unsigned int>(), L,
+                                                             sum.as<unsigned long long>());
+  HD_LAUNCHED(ctx);
+  uint64_t h = 0;
+  HD_CUDA(cudaMemcpyAsync(&h, sum.p, 8, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  return h;
+}
+
+// ------------------------------------------------------------------- pack
+// One warp packs 32 words (1024 sites) of one row: each lane holds one site's
+// code, one ballot per plane collects 32 sites into a plane word, and lane i
+// keeps word i. Sites past L get the '-' code, which matches everything, so
+// padding never counts (the reference pads with '-' too, src/hamming_impl.cc:
+// 256-264).
+template <int P>
+__global__ void k_pack(const uint8_t *base, const uint64_t *rs, const uint64_t *rows,
+                       uint64_t n_rows, uint64_t L, uint64_t words, Table256 table, uint4 *g0,
+                       uint4 *g1) {
+  __shared__ uint8_t tbl[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) tbl[i] = table.v[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const uint64_t chunks = (words + 31) / 32;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  const uint8_t pad = tbl['-'];
+  for (uint64_t job = wid; job < n_rows * chunks; job += nwarps) {
+    uint64_t u = job / chunks, q = job % chunks;
+    uint64_t r = rows ? rows[u] : u;
+    const uint8_t *src = base + rs[r];
+    uint32_t x[P];
+#pragma unroll
+    for (int p = 0; p < P; ++p) x[p] = 0;
+    for (int i = 0; i < 32; ++i) {
+      uint64_t w = q * 32 + i;
+      if (w >= words) break;
+      uint64_t s = w * 32 + lane;
+      uint8_t code = s < L ? tbl[src[s]] : pad;
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        uint32_t b = __ballot_sync(0xffffffffu, (code >> p) & 1u);
+        if (lane == i) x[p] = b;
+      }
+    }
+    uint64_t w = q * 32 + lane;
+    if (w < words) {
+      g0[u * words + w] = make_uint4(x[0], x[1], x[2], x[3]);
+      if (P > 4) g1[u * words + w] = make_uint4(x[4 % P], P > 5 ? x[5 % P] : 0u, 0u, 0u);
+    }
+  }
+}
+
+void pack_rows(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, hd_alignment *aln) {
+  Table256 t;
+  int table = aln->rule == HD_RULE_AND ? kCodesAnd
+              : aln->rule == HD_RULE_SPARSE ? kCodesSparse : kCodesSparseX;
+  code_table(table, t.v);
+  const uint64_t bytes = aln->n_rows * aln->words * 16;
+  aln->plane_buf[0] = DevBuf(bytes ? bytes : 16, ctx->stream);
+  if (aln->groups > 1) aln->plane_buf[1] = DevBuf(bytes ? bytes : 16, ctx->stream);
+  if (!aln->n_rows) return;
+  uint64_t jobs = aln->n_rows * ((aln->words + 31) / 32);
+  unsigned grid = grid_for(jobs * 32, 256);
+  uint4 *g0 = aln->plane_buf[0].as<uint4>(), *g1 = aln->plane_buf[1].as<uint4>();
+  const uint64_t *rs = rec.rec_start.as<uint64_t>();
+  if (aln->planes == 4)
+    k_pack<4><<<grid, 256, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
+                                             aln->words, t, g0, g1);
+  else if (aln->planes == 5)
+    k_pack<5><<<grid, 256, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
+                                             aln->words, t, g0, g1);
+  else
+    k_pack<6><<<grid, 256, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
+                                             aln->words, t, g0, g1);
+  HD_LAUNCHED(ctx);
+}
+
+// ----------------------------------------------------- reference distances
+// Rule of src/hamming.cc:128-136: a site counts when the reference codes of
+// the two bytes share no bit, or when the bytes differ and neither is '-'.
+__global__ void k_refdist(const uint8_t *base, const uint64_t *rs, const uint64_t *rl, uint64_t R,
+                          const uint8_t *ref, Table256 lookup, uint32_t *out) {
+  __shared__ uint8_t lk[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lk[i] = lookup.v[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t r = wid; r < R; r += nwarps) {
+    const uint8_t *p = base + rs[r];
+    const uint64_t len = rl[r];
+    uint32_t cnt = 0;
+    for (uint64_t s = lane; s < len; s += 32) {
+      uint8_t a = p[s], b = ref[s];
+      uint8_t la = lk[a], lb = lk[b];
+      bool invalid = (la & lb) == 0;
+      bool count = invalid || (a != b && la != 0xff && lb != 0xff);
+      cnt += count ? 1u : 0u;
+    }
+    cnt = warp_sum(cnt);
+    if (lane == 0) out[r] = cnt;
+  }
+}
+
+void reference_distances_device(hd_ctx *ctx, const Records &rec, const uint8_t *d_ref,
+                                int include_x, uint32_t *d_out) {
+  if (!rec.n) return;
+  Table256 lk;
+  for (int c = 0; c < 256; ++c) lk.v[c] = 0;
+  lk.v['-'] = 0xff;
+  lk.v['A'] = 0x11;
+  lk.v['C'] = 0x22;
+  lk.v['G'] = 0x44;
+  lk.v['T'] = 0x88;
+  if (include_x) lk.v['X'] = 0x33;
+  k_refdist<<<grid_for(rec.n * 32, 256), 256, 0, ctx->stream>>>(
+      rec.base, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(), rec.n, d_ref, lk, d_out);
+  HD_LAUNCHED(ctx);
+}
+
+// Query row (packed with the alignment's AND codes) against every row.
+__global__ void k_query(const uint4 *g0, uint64_t words, uint64_t n_rows, const uint4 *q,
+                        uint32_t *out) {
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t u = wid; u < n_rows; u += nwarps) {
+    const uint4 *row = g0 + u * words;
+    uint32_t cnt = 0;
+    for (uint64_t w = lane; w < words; w += 32) {
+      uint4 a = row[w], b = q[w];
+      cnt += __popc(~((a.x & b.x) | (a.y & b.y) | (a.z & b.z) | (a.w & b.w)));
+    }
+    cnt = warp_sum(cnt);
+    if (lane == 0) out[u] = cnt;
+  }
+}
+
+void alignment_query_distances(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
+                               uint32_t *d_out_rows) {
+  // pack the query with the same codes as the alignment (one row)
+  hd_alignment q;
+  q.n_rows = 1;
+  q.length = aln->length;
+  q.words = aln->words;
+  q.rule = HD_RULE_AND;
+  q.groups = 1;
+  q.planes = 4;
+  Records r1;
+  r1.n = 1;
+  r1.base = d_query;
+  r1.len0 = aln->length;
+  r1.rec_start = DevBuf(8, ctx->stream);
+  HD_CUDA(cudaMemsetAsync(r1.rec_start.p, 0, 8, ctx->stream));
+  pack_rows(ctx, r1, nullptr, &q);
+  k_query<<<grid_for(aln->n_rows * 32, 256), 256, 0, ctx->stream>>>(
+      aln->plane_buf[0].as<uint4>(), aln->words, aln->n_rows, q.plane_buf[0].as<uint4>(),
+      d_out_rows);
+  HD_LAUNCHED(ctx);
+  HD_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+}  // namespace hd

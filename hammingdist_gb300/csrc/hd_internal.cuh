@@ -1,0 +1,333 @@
+// Internal declarations shared by the libhd translation units: the context and
+// alignment objects behind the C ABI, device buffers from the stream-ordered
+// pool, a device-wide exclusive scan, and the PTX helpers (mbarrier, TMA) used
+// by the pairwise kernel.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/hammingdist_gb300.h"
+
+namespace hd {
+
+// ---------------------------------------------------------------- errors
+struct Error {
+  int code;
+  std::string msg;
+};
+[[noreturn]] inline void fail(int code, std::string msg) { throw Error{code, std::move(msg)}; }
+inline void check_cuda(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) {
+    if (e == cudaErrorMemoryAllocation) fail(HD_ERR_OOM, cudaGetErrorString(e));
+    fail(HD_ERR_CUDA, std::string(cudaGetErrorString(e)) + " (" + what + ")");
+  }
+}
+#define HD_CUDA(x) ::hd::check_cuda((x), #x)
+#define HD_LAUNCHED(ctx)                                  \
+  do {                                                    \
+    ::hd::check_cuda(cudaGetLastError(), "kernel launch"); \
+    (ctx)->launches++;                                     \
+  } while (0)
+
+// Status codes written by kernels into the context's device status word.
+constexpr int kStatusOk = 0;
+constexpr int kStatusTmaTimeout = 1;
+
+inline uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+inline uint64_t round_up(uint64_t a, uint64_t b) { return ceil_div(a, b) * b; }
+
+// ------------------------------------------------------- device buffers
+// Stream-ordered allocations from the device's default pool; the pool keeps
+// freed memory (release threshold = max), so steady-state calls do not reach
+// the driver allocator.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  cudaStream_t s = nullptr;
+  DevBuf() = default;
+  DevBuf(size_t n, cudaStream_t stream) : bytes(n), s(stream) {
+    if (n) HD_CUDA(cudaMallocAsync(&p, n, stream));
+  }
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept { *this = std::move(o); }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      bytes = o.bytes;
+      s = o.s;
+      o.p = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+}  // namespace hd
+
+// -------------------------------------------------------------- objects
+struct hd_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;  // compute
+  cudaStream_t side = nullptr;    // copies that overlap compute
+  std::string err;
+  int *d_status = nullptr;        // kernel status word
+  uint64_t launches = 0;
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+  double last_pair_ms = 0.0;
+  uint64_t last_pair_tiles = 0;
+  PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
+  hd::DevBuf file;                // device copy of the last FASTA input
+};
+
+struct hd_alignment {
+  hd_ctx *ctx = nullptr;
+  uint64_t n_input = 0;   // records read
+  uint64_t n_rows = 0;    // rows after dedupe
+  uint64_t length = 0;    // sites per row
+  uint64_t words = 0;     // 32-site words per row, multiple of 8
+  int rule = HD_RULE_AND;
+  int groups = 1;         // plane groups of 4 planes (uint4 per word)
+  int planes = 4;         // planes in use
+  hd::DevBuf plane_buf[2];
+  std::vector<uint64_t> seqidx;  // host, n_input entries (empty = identity)
+  hd::DevBuf d_seqidx;           // device copy (serving / reference queries)
+};
+
+namespace hd {
+
+// --------------------------------------------------------- device scan
+// Exclusive scan of n values (uint32 or uint64 input) into uint64 output;
+// *d_total receives the sum. Three launches; any n.
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr uint64_t kScanTile = (uint64_t)kScanThreads * kScanItems;
+
+template <class T>
+__device__ inline T warp_incl_scan(T v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T u = __shfl_up_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) >= (unsigned)o) v += u;
+  }
+  return v;
+}
+
+template <class T>
+__device__ inline T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide exclusive scan (blockDim.x multiple of 32, <= 1024).
+template <class T>
+__device__ inline T block_excl_scan(T v, T *warp_tmp /*[33]*/, T &total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  T inc = warp_incl_scan(v);
+  if (lane == 31) warp_tmp[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < nw ? warp_tmp[lane] : T(0);
+    T wi = warp_incl_scan(w);
+    if (lane < nw) warp_tmp[lane] = wi - w;
+    if (lane == nw - 1) warp_tmp[32] = wi;
+  }
+  __syncthreads();
+  T res = warp_tmp[warp] + inc - v;
+  total = warp_tmp[32];
+  __syncthreads();
+  return res;
+}
+
+template <class In>
+__global__ void k_scan_reduce(const In *in, uint64_t n, uint64_t *block_sums) {
+  __shared__ uint64_t tmp[33];
+  uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+  uint64_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k)
+    if (base + k < n) s += (uint64_t)in[base + k];
+  uint64_t tot;
+  block_excl_scan<uint64_t>(s, tmp, tot);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+// One block scans the block sums in place (exclusive) and writes the total.
+template <class Dummy = void>
+__global__ void k_scan_top(uint64_t *sums, uint64_t nb, uint64_t *d_total) {
+  __shared__ uint64_t tmp[33];
+  uint64_t carry = 0;
+  for (uint64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+    uint64_t i = b0 + threadIdx.x;
+    uint64_t v = i < nb ? sums[i] : 0;
+    uint64_t tot;
+    uint64_t ex = block_excl_scan<uint64_t>(v, tmp, tot);
+    if (i < nb) sums[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0 && d_total) *d_total = carry;
+}
+
+template <class In>
+__global__ void k_scan_down(const In *in, uint64_t *out, uint64_t n, const uint64_t *block_off) {
+  __shared__ uint64_t tmp[33];
+  uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+  uint64_t v[kScanItems];
+  uint64_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = base + k < n ? (uint64_t)in[base + k] : 0;
+    s += v[k];
+  }
+  uint64_t tot;
+  uint64_t off = block_excl_scan<uint64_t>(s, tmp, tot) + block_off[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < n) out[base + k] = off;
+    off += v[k];
+  }
+}
+
+template <class In>
+void scan_exclusive(hd_ctx *ctx, const In *in, uint64_t *out, uint64_t n, uint64_t *d_total) {
+  uint64_t nb = ceil_div(n ? n : 1, kScanTile);
+  DevBuf sums(nb * sizeof(uint64_t), ctx->stream);
+  k_scan_reduce<In><<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(in, n, sums.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+  k_scan_top<void><<<1, 1024, 0, ctx->stream>>>(sums.as<uint64_t>(), nb, d_total);
+  HD_LAUNCHED(ctx);
+  k_scan_down<In><<<(unsigned)nb, kScanThreads, 0, ctx->stream>>>(in, out, n, sums.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+}
+
+// ------------------------------------------------------- PTX helpers
+__device__ inline uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ inline void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ inline void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ inline void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ inline bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ inline uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for the barrier phase with a wall-clock limit; false = gave up.
+__device__ inline bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+}
+// 2-D tiled TMA load (global -> shared), completion counted on `bar`.
+__device__ inline void tma_load_2d(void *smem_dst, const CUtensorMap *map, int32_t x, int32_t y,
+                                   uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(smem_dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ inline void prefetch_tmap(const CUtensorMap *map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// ------------------------------------------------- parsed FASTA records
+// Records on the device: record r is rec_len[r] bytes at base + rec_start[r].
+struct Records {
+  uint64_t n = 0;          // records kept (after the n limit)
+  uint64_t len0 = 0;       // length of record 0
+  uint64_t max_len = 0;
+  bool all_equal = true;
+  const uint8_t *base = nullptr;
+  DevBuf rec_start, rec_len;  // uint64 [n]
+  DevBuf gathered;            // concatenation when records span several lines
+};
+
+// Character codes of the rules (bit p = bit plane p); '-' is all ones.
+enum CodeTable { kCodesAnd = 0, kCodesSparse = 1, kCodesSparseX = 2, kNumCodeTables = 3 };
+void code_table(int table, uint8_t out[256]);
+inline int planes_of(int rule) { return rule == HD_RULE_AND ? 4 : rule == HD_RULE_SPARSE ? 5 : 6; }
+
+// ----------------------------------------------------- stage launchers
+// ingest.cu
+Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_t n_limit);
+Records records_from_offsets(hd_ctx *ctx, const uint8_t *d_bytes, const uint64_t *h_offsets,
+                             uint64_t n);
+// Deduplicates: returns the unique records (first-occurrence order) as a list
+// of record indices on the device and fills seqidx (host, n entries).
+DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<uint64_t> &seqidx);
+// Sum over sites of the most frequent of A/C/G/T among the given rows.
+uint64_t consensus_matches(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows,
+                           uint64_t n_rows);
+// Packs rows (record ids d_rows, or identity if null) into bit planes.
+void pack_rows(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, hd_alignment *aln);
+void reference_distances_device(hd_ctx *ctx, const Records &rec, const uint8_t *d_ref,
+                                int include_x, uint32_t *d_out);
+void alignment_query_distances(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
+                               uint32_t *d_out_rows);
+
+// pairwise.cu: tiles of rows [tile_lo*128, tile_hi*128) x all earlier columns
+// into out (lt index out_base maps to out[0]).
+void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
+                    void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi);
+constexpr uint32_t kTile = 128;
+
+// format.cu: text of rows [i_lo, i_hi) of a lower triangle held on the
+// device (lt index lt_base at d_lt[0]). Returns bytes written to d_text
+// (capacity checked by the caller via the *_bound functions).
+uint64_t lt_text_bound(uint64_t i_lo, uint64_t i_hi, int dtype_bytes);
+uint64_t format_lt_rows(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint64_t lt_base,
+                        uint64_t i_lo, uint64_t i_hi, char *d_text);
+// Sparse lines of rows [i_lo, i_hi): counts text bytes per row into
+// d_row_bytes (uint64 [i_hi-i_lo]) and lines into *n_lines.
+void sparse_row_sizes(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint64_t lt_base,
+                      uint64_t i_lo, uint64_t i_hi, int64_t threshold, uint64_t *d_row_bytes,
+                      uint64_t *d_row_lines);
+uint64_t format_sparse_rows(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint64_t lt_base,
+                            uint64_t i_lo, uint64_t i_hi, int64_t threshold,
+                            const uint64_t *d_row_bytes, char *d_text);
+
+// peak.cu
+void measure_int_peaks(hd_ctx *ctx, double *lop3, double *popc, double *mix);
+
+}  // namespace hd

@@ -1,0 +1,421 @@
+// The Python module: the reference's pybind11 API (python/hammingdist.cc:28-133)
+// re-implemented over the libhd C ABI (include/hammingdist_gb300.h). Names,
+// keyword arguments, defaults, return dtypes and error messages follow the
+// reference; every distance is computed on the GPU.
+//
+// use_gpu keeps the reference's meaning for the RESULT: True gives the
+// reference GPU's values (dense AND rule; include_x rejected), False gives
+// the reference CPU's values (sparse rule when include_x or when fewer than
+// 0.5% of sites differ from the consensus, else the dense rule). Both run on
+// the GPU here.
+#include <fcntl.h>
+#include <pybind11/numpy.h>
+#include <pybind11/pybind11.h>
+#include <pybind11/stl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/hammingdist_gb300.h"
+
+namespace py = pybind11;
+
+namespace {
+
+std::mutex g_mu;         // one context per process; calls are serialised
+hd_ctx *g_ctx = nullptr;
+void *g_pin = nullptr;   // pinned staging for FASTA bytes, grows
+size_t g_pin_cap = 0;
+
+hd_ctx *ctx() {
+  if (!g_ctx) {
+    int dev = 0;
+    if (const char *e = std::getenv("HAMMINGDIST_DEVICE")) dev = std::atoi(e);
+    int rc = hd_ctx_create(dev, &g_ctx);
+    if (rc == HD_ERR_NO_DEVICE)
+      throw std::runtime_error("hammingdist_gb300: no CUDA device available (this build has no CPU path)");
+    if (rc != HD_OK) throw std::runtime_error("hammingdist_gb300: could not create a CUDA context");
+  }
+  return g_ctx;
+}
+
+void check(int rc) {
+  if (rc != HD_OK) throw std::runtime_error(hd_last_error(g_ctx));
+}
+
+[[noreturn]] void open_failed(const std::string &f) {
+  throw std::runtime_error("Error: Failed to open file '" + f + "'");
+}
+
+// Reads a whole file into the pinned staging buffer (parallel preads).
+std::pair<const char *, uint64_t> read_pinned(const std::string &path) {
+  int fd = ::open(path.c_str(), O_RDONLY);
+  if (fd < 0) open_failed(path);
+  struct stat sb;
+  if (fstat(fd, &sb) != 0 || !S_ISREG(sb.st_mode)) {
+    ::close(fd);
+    open_failed(path);
+  }
+  const uint64_t n = (uint64_t)sb.st_size;
+  if (n + 1 > g_pin_cap) {
+    if (g_pin) hd_host_free(g_ctx, g_pin);
+    g_pin = nullptr;
+    g_pin_cap = 0;
+    size_t cap = (size_t)((n + 1) * 5 / 4 + (1 << 20));
+    if (hd_host_alloc(g_ctx, cap, &g_pin) != HD_OK) {
+      ::close(fd);
+      throw std::runtime_error(hd_last_error(g_ctx));
+    }
+    g_pin_cap = cap;
+  }
+  char *dst = static_cast<char *>(g_pin);
+  const uint64_t kPart = 64ull << 20;
+  const unsigned nthreads = n > kPart ? std::min<unsigned>(8, (unsigned)((n + kPart - 1) / kPart)) : 1;
+  std::vector<std::thread> th;
+  std::vector<int> ok(nthreads, 1);
+  const uint64_t per = (n + nthreads - 1) / nthreads;
+  for (unsigned t = 0; t < nthreads; ++t) {
+    th.emplace_back([&, t] {
+      uint64_t off = t * per, end = std::min(n, off + per);
+      while (off < end) {
+        ssize_t r = ::pread(fd, dst + off, (size_t)std::min<uint64_t>(end - off, 1ull << 30), (off_t)off);
+        if (r <= 0) {
+          ok[t] = 0;
+          return;
+        }
+        off += (uint64_t)r;
+      }
+    });
+  }
+  for (auto &x : th) x.join();
+  ::close(fd);
+  for (int v : ok)
+    if (!v) open_failed(path);
+  return {dst, n};
+}
+
+struct Aln {
+  hd_alignment *p = nullptr;
+  ~Aln() { hd_alignment_free(p); }
+};
+
+void say(const std::string &s) { std::cout << "# hammingdist :: " << s << std::endl; }
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ DataSet
+// include/hamming/hamming.hh:22-143: owns the lower triangle
+// lt[i(i-1)/2 + j], i > j, and the sequence indices.
+template <typename T>
+struct DataSet {
+  uint64_t nsamples = 0;
+  std::vector<T> result;
+  std::vector<uint64_t> sequence_indices;
+
+  int at(const std::array<size_t, 2> &ij) const {
+    size_t i = ij[0], j = ij[1];
+    if (i < j) std::swap(i, j);
+    if (i == j) return 0;
+    return result.at(i * (i - 1) / 2 + j);
+  }
+
+  // hamming.hh:63-73 (full matrix, ", " separators): host formatting, not on
+  // the device path
+  void dump(const std::string &filename) const {
+    std::ofstream s(filename);
+    for (uint64_t i = 0; i < nsamples; ++i) {
+      for (uint64_t j = 0; j < nsamples; ++j) {
+        s << at({i, j});
+        if (j != nsamples - 1) s << ", ";
+      }
+      s << std::endl;
+    }
+  }
+
+  void dump_lower_triangular(const std::string &filename) const {
+    std::lock_guard<std::mutex> lk(g_mu);
+    hd_ctx *c = ctx();
+    py::gil_scoped_release nogil;
+    check(hd_write_lower_triangular(c, result.data(), nsamples, sizeof(T), filename.c_str()));
+  }
+
+  void dump_sparse(const std::string &filename, int threshold) const {
+    std::lock_guard<std::mutex> lk(g_mu);
+    hd_ctx *c = ctx();
+    py::gil_scoped_release nogil;
+    check(hd_write_sparse(c, result.data(), nsamples, sizeof(T), threshold, filename.c_str(), nullptr));
+  }
+
+  // hamming.hh:116-127
+  void dump_sequence_indices(const std::string &filename) const {
+    std::ofstream s(filename);
+    if (sequence_indices.empty()) {
+      for (uint64_t i = 0; i < nsamples; ++i) s << i << "\n";
+      return;
+    }
+    for (auto v : sequence_indices) s << v << "\n";
+  }
+};
+
+namespace {
+
+// infer n from n(n-1)/2 entries (hamming.hh:57-61)
+uint64_t n_from_entries(uint64_t e) {
+  uint64_t n = (uint64_t)std::llround((std::sqrt(8.0 * (double)e + 1.0) + 1.0) / 2.0);
+  while (n > 1 && n * (n - 1) / 2 > e) --n;
+  while (n * (n - 1) / 2 < e) ++n;
+  return n;
+}
+
+template <typename T>
+DataSet<T> compute(hd_alignment *aln, int64_t max_distance, bool announce, const char *what,
+                   std::chrono::steady_clock::time_point t0) {
+  DataSet<T> ds;
+  uint64_t n_rows = 0, L = 0, n_in = 0;
+  int rule = 0;
+  check(hd_alignment_info(aln, &n_rows, &L, &n_in, &rule));
+  ds.nsamples = n_rows;
+  ds.result.resize(n_rows < 2 ? 0 : n_rows * (n_rows - 1) / 2);
+  if (announce) {
+    say(std::string("Using GPU (") + what +
+        (rule == HD_RULE_AND ? ", dense distance rule)..." : ", sparse distance rule)..."));
+    say("...pre-processing completed in " + std::to_string((long long)ms_since(t0)) + " ms...");
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  if (!ds.result.empty())
+    check(hd_pairwise_lt(g_ctx, aln, sizeof(T), max_distance, ds.result.data(), 0));
+  if (announce)
+    say("...distance calculation completed in " + std::to_string((long long)ms_since(t1)) + " ms.");
+  return ds;
+}
+
+template <typename T>
+DataSet<T> from_fasta(const std::string &filename, bool include_x, bool remove_duplicates,
+                      size_t n, bool use_gpu, int max_distance) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
+  auto t0 = std::chrono::steady_clock::now();
+  auto [bytes, nbytes] = read_pinned(filename);
+  py::gil_scoped_release nogil;
+  Aln a;
+  check(hd_alignment_from_fasta(c, bytes, nbytes, 0, remove_duplicates, n, include_x,
+                                use_gpu ? HD_SEM_GPU : HD_SEM_CPU, &a.p));
+  DataSet<T> ds = compute<T>(a.p, max_distance, true, use_gpu ? "use_gpu=True" : "use_gpu=False", t0);
+  if (remove_duplicates) {
+    uint64_t n_in = 0;
+    check(hd_alignment_info(a.p, nullptr, nullptr, &n_in, nullptr));
+    ds.sequence_indices.resize(n_in);
+    check(hd_alignment_sequence_indices(a.p, ds.sequence_indices.data()));
+  }
+  return ds;
+}
+
+DataSet<uint8_t> from_stringlist(const std::vector<std::string> &data, bool include_x, bool use_gpu,
+                                 int max_distance) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
+  std::string cat;
+  std::vector<uint64_t> offsets(data.size() + 1, 0);
+  for (size_t k = 0; k < data.size(); ++k) {
+    cat += data[k];
+    offsets[k + 1] = cat.size();
+  }
+  py::gil_scoped_release nogil;
+  Aln a;
+  check(hd_alignment_from_sequences(c, cat.data(), offsets.data(), data.size(), include_x,
+                                    use_gpu ? HD_SEM_GPU : HD_SEM_CPU, &a.p));
+  return compute<uint8_t>(a.p, max_distance, false, "", std::chrono::steady_clock::now());
+}
+
+void from_fasta_to_lower_triangular(const std::string &in, const std::string &out,
+                                    bool remove_duplicates, size_t n, bool use_gpu,
+                                    int max_distance) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
+  auto t0 = std::chrono::steady_clock::now();
+  if (use_gpu) say("Using GPU...");
+  auto [bytes, nbytes] = read_pinned(in);
+  py::gil_scoped_release nogil;
+  Aln a;
+  check(hd_alignment_from_fasta(c, bytes, nbytes, 0, remove_duplicates, n, 0, HD_SEM_GPU, &a.p));
+  say("...pre-processing completed in " + std::to_string((long long)ms_since(t0)) + " ms...");
+  // src/hamming.cc:47-52: the reference computes this on the GPU only
+  if (!use_gpu) throw std::runtime_error("from_fasta_to_lower_triangular is currently only available on GPU");
+  auto t1 = std::chrono::steady_clock::now();
+  check(hd_pairwise_lt_to_file(c, a.p, max_distance, out.c_str()));
+  say("...distance calculation completed in " + std::to_string((long long)ms_since(t1)) + " ms.");
+}
+
+uint32_t distance(const std::string &s0, const std::string &s1, bool include_x) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
+  uint32_t d = 0;
+  check(hd_distance(c, s0.data(), s0.size(), s1.data(), s1.size(), include_x, &d));
+  return d;
+}
+
+template <typename T>
+py::array_t<T> owned_array(T *p, uint64_t n) {
+  py::capsule cap(p, [](void *q) { hd_free(q); });
+  return py::array_t<T>({(py::ssize_t)n}, {(py::ssize_t)sizeof(T)}, p, cap);
+}
+
+py::array_t<uint32_t> fasta_reference_distances(const std::string &ref, const std::string &fasta,
+                                                bool include_x) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
+  auto [bytes, nbytes] = read_pinned(fasta);
+  uint32_t *out = nullptr;
+  uint64_t n = 0;
+  {
+    py::gil_scoped_release nogil;
+    check(hd_reference_distances(c, ref.data(), ref.size(), bytes, nbytes, include_x, &out, &n));
+  }
+  return owned_array<uint32_t>(out, n);
+}
+
+py::array_t<uint64_t> fasta_sequence_indices(const std::string &fasta, size_t nlim) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
+  auto [bytes, nbytes] = read_pinned(fasta);
+  uint64_t *out = nullptr;
+  uint64_t n = 0;
+  {
+    py::gil_scoped_release nogil;
+    check(hd_fasta_sequence_indices(c, bytes, nbytes, nlim, &out, &n));
+  }
+  return owned_array<uint64_t>(out, n);
+}
+
+// Readers (hamming.hh:34-55, :152-166): host parsing of result files.
+template <typename T>
+DataSet<T> from_lower_triangular(const std::string &filename) {
+  std::ifstream s(filename);
+  DataSet<T> ds;
+  std::string line, d;
+  while (std::getline(s, line)) {
+    std::istringstream ls(line);
+    while (ls.good()) {
+      std::getline(ls, d, ',');
+      int v = std::stoi(d);
+      ds.result.push_back(v > (int)std::numeric_limits<T>::max() ? std::numeric_limits<T>::max()
+                                                                  : (T)v);
+    }
+  }
+  ds.nsamples = n_from_entries(ds.result.size());
+  return ds;
+}
+
+DataSet<uint8_t> from_csv(const std::string &filename) {
+  std::ifstream s(filename);
+  DataSet<uint8_t> ds;
+  std::string line;
+  uint64_t n = 0;
+  {
+    std::ifstream c(filename);
+    n = std::count(std::istreambuf_iterator<char>(c), std::istreambuf_iterator<char>(), '\n');
+  }
+  ds.nsamples = n;
+  ds.result.resize(n * (n + 1) / 2);
+  uint64_t i = 0, row = 0;
+  while (std::getline(s, line)) {
+    std::istringstream ls(line);
+    std::string d;
+    for (uint64_t j = 0; j < row; ++j) {
+      std::getline(ls, d, ',');
+      ds.result[i++] = (uint8_t)std::stoi(d);
+    }
+    ++row;
+  }
+  return ds;
+}
+
+template <typename T>
+void bind_dataset(py::module_ &m, const char *name, int default_threshold) {
+  py::class_<DataSet<T>>(m, name)
+      .def("dump", &DataSet<T>::dump, "Dump distances matrix in csv format")
+      .def("dump_lower_triangular", &DataSet<T>::dump_lower_triangular,
+           "Dump distances matrix in lower triangular format (comma-delimited, row-major)")
+      .def("dump_sparse", &DataSet<T>::dump_sparse, py::arg("filename"),
+           py::arg("threshold") = default_threshold,
+           "Dump distances matrix in sparse format excluding any distances above threshold")
+      .def("dump_sequence_indices", &DataSet<T>::dump_sequence_indices,
+           "Dump row index in distances matrix for each input sequence")
+      .def("__getitem__", &DataSet<T>::at)
+      .def_readonly("_distances", &DataSet<T>::result)
+      .def_property_readonly("lt_array", [](const DataSet<T> &self) {
+        // a fresh copy on every access, as the reference's py::array(size, ptr)
+        return py::array_t<T>((py::ssize_t)self.result.size(), self.result.data());
+      });
+}
+
+}  // namespace
+
+PYBIND11_MODULE(_C, m) {
+  m.doc() = "GB300 implementation of hammingdist's pairwise Hamming distances";
+  bind_dataset<uint8_t>(m, "DataSet", 255);
+  bind_dataset<uint16_t>(m, "DataSetLarge", 65535);
+  m.def("from_stringlist", &from_stringlist, py::arg("data"), py::arg("include_x") = false,
+        py::arg("use_gpu") = false, py::arg("max_distance") = std::numeric_limits<int>::max(),
+        "Creates a dataset from a list of strings");
+  m.def("from_csv", &from_csv,
+        "Creates a dataset by reading already computed distances from csv (full matrix expected)");
+  m.def("from_fasta", &from_fasta<uint8_t>, py::arg("filename"), py::arg("include_x") = false,
+        py::arg("remove_duplicates") = false, py::arg("n") = 0, py::arg("use_gpu") = false,
+        py::arg("max_distance") = 255,
+        "Creates a dataset by reading from a fasta file (assuming all sequences have equal "
+        "length). Maximum value of an element in the distances matrix: max_distance or 255, "
+        "whichever is lower.");
+  m.def("from_fasta_large", &from_fasta<uint16_t>, py::arg("filename"),
+        py::arg("include_x") = false, py::arg("remove_duplicates") = false, py::arg("n") = 0,
+        py::arg("use_gpu") = false, py::arg("max_distance") = 65535,
+        "Creates a dataset by reading from a fasta file (assuming all sequences have equal "
+        "length). Maximum value of an element in the distances matrix: max_distance or 65535, "
+        "whichever is lower");
+  m.def("from_fasta_to_lower_triangular", &from_fasta_to_lower_triangular,
+        py::arg("fasta_filename"), py::arg("output_filename"), py::arg("remove_duplicates") = false,
+        py::arg("n") = 0, py::arg("use_gpu") = true, py::arg("max_distance") = 65535,
+        "Construct lower triangular distances matrix output file from the fasta file. Maximum "
+        "value of an element in the distances matrix: max_distance or 65535, whichever is lower");
+  m.def("from_lower_triangular", &from_lower_triangular<uint8_t>,
+        "Creates a dataset by reading already computed distances from lower triangular format. "
+        "Maximum value of an element in the distances matrix: 255.");
+  m.def("from_lower_triangular_large", &from_lower_triangular<uint16_t>,
+        "Creates a dataset by reading already computed distances from lower triangular format. "
+        "Maximum value of an element in the distances matrix: 65535.");
+  m.def("distance", &distance, py::arg("seq0"), py::arg("seq1"), py::arg("include_x") = false,
+        "Calculate the distance between seq0 and seq1");
+  m.def("fasta_reference_distances", &fasta_reference_distances, py::arg("reference_sequence"),
+        py::arg("fasta_file"), py::arg("include_x") = false,
+        "Calculates the distance of each sequence in the fasta file from the supplied reference "
+        "sequence");
+  m.def("fasta_sequence_indices", &fasta_sequence_indices, py::arg("fasta_file"), py::arg("n") = 0,
+        "For each genome in the input fasta file the index of the corresponding row in the "
+        "distances matrix which excludes duplicates");
+  m.def("cuda_gpu_available", []() { return hd_device_available() != 0; },
+        "True if a GPU that supports CUDA is available");
+  m.def("_kernel_launches", []() -> uint64_t {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return g_ctx ? hd_ctx_kernel_launches(g_ctx) : 0;
+  });
+}

@@ -1,0 +1,189 @@
+/*
+ * hammingdist_gb300.h — C ABI of the GB300 (sm_103a) implementation of
+ * hammingdist's pairwise Hamming-distance path (libhd).
+ *
+ * Plain C types only: host/device pointers, sizes and status codes. No C++
+ * exception crosses this boundary; every entry point returns HD_OK (0) or a
+ * negative HD_ERR_* code, and hd_last_error() holds the message (the exact
+ * message text of the reference where it has one).
+ *
+ * Each declaration names the reference interface (ssciwr/hammingdist 1.4.0,
+ * file:line) that it replaces. The reference's pybind11 module
+ * (python/hammingdist.cc) is mirrored on top of this ABI by
+ * hammingdist_gb300/csrc/hd_module.cpp.
+ *
+ * Every computation runs on the GPU. There is no CPU fallback: without a
+ * usable CUDA device the calls fail with HD_ERR_NO_DEVICE.
+ */
+#ifndef HAMMINGDIST_GB300_H
+#define HAMMINGDIST_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define HD_OK 0
+#define HD_ERR_EMPTY -1          /* "Error: Empty sequence" */
+#define HD_ERR_LENGTH -2         /* "Error: Sequences do not all have the same length" */
+#define HD_ERR_CUDA -3           /* CUDA runtime error; message = cudaGetErrorString */
+#define HD_ERR_ARG -4            /* invalid argument */
+#define HD_ERR_IO -5             /* "Error: Failed to open file '<f>'" and write errors */
+#define HD_ERR_INCLUDE_X_GPU -6  /* "use_gpu=True cannot be used if include_x=True, ..." */
+#define HD_ERR_TIMEOUT -7        /* a bounded device-side wait ran out */
+#define HD_ERR_NO_DEVICE -8      /* no usable CUDA device */
+#define HD_ERR_REF_LENGTH -9     /* a record is longer than the reference sequence */
+#define HD_ERR_OOM -10           /* device or pinned host allocation failed */
+#define HD_ERR_STATE -11         /* object in the wrong state (e.g. released) */
+
+/* ---- semantics of a pairwise matrix ------------------------------------- */
+/* HD_SEM_GPU: the reference's use_gpu=True semantics — the dense AND rule of
+ *   src/distance_cuda.cu:57-65 on the 4-bit codes of src/hamming_impl.cc:31-44;
+ *   include_x is rejected (include/hamming/hamming_impl.hh:99-102).
+ * HD_SEM_CPU: the reference's use_gpu=False semantics — include_x or a
+ *   consensus difference fraction below 0.005 selects the sparse rule
+ *   (include/hamming/hamming_impl.hh:104-118, src/hamming_impl.cc:93-129),
+ *   else the dense AND rule. Computed on the GPU all the same.            */
+#define HD_SEM_GPU 0
+#define HD_SEM_CPU 1
+
+/* Rule actually used by an alignment (hd_alignment_info). */
+#define HD_RULE_AND 0       /* dense AND rule, 4 bit-planes */
+#define HD_RULE_SPARSE 1    /* sparse rule, X invalid (5 planes) */
+#define HD_RULE_SPARSE_X 2  /* sparse rule, X a fifth symbol (6 planes) */
+
+typedef struct hd_ctx hd_ctx;             /* one per device: streams, pools, status */
+typedef struct hd_alignment hd_alignment; /* packed alignment resident in HBM */
+
+/* Replaces distance_cuda_have_device (src/distance_cuda.cu:232-238) and
+ * cuda_gpu_available (include/hamming/hamming_impl.hh:23-29): 1 if a CUDA
+ * device is usable, else 0. */
+int hd_device_available(void);
+
+/* Context on `device` (ordinal). New; the reference has none (it uses the
+ * default stream and cudaMalloc per call). */
+int hd_ctx_create(int device, hd_ctx **out);
+void hd_ctx_destroy(hd_ctx *ctx);
+const char *hd_last_error(const hd_ctx *ctx);
+/* Number of kernels this context has launched so far (evidence for tests and
+ * benchmarks that the device path ran). */
+uint64_t hd_ctx_kernel_launches(const hd_ctx *ctx);
+/* Pinned host memory, reused for FASTA bytes and results. */
+int hd_host_alloc(hd_ctx *ctx, size_t bytes, void **out);
+void hd_host_free(hd_ctx *ctx, void *p);
+/* Frees a host array returned by hd_reference_distances /
+ * hd_fasta_sequence_indices. */
+void hd_free(void *p);
+/* Waits for all work on the context's streams. */
+int hd_ctx_synchronize(hd_ctx *ctx);
+/* The cudaStream_t (as void*) the context launches its kernels on, so a
+ * caller can time them with CUDA events on that stream. */
+void *hd_ctx_stream(const hd_ctx *ctx);
+
+/* ---- ingest ------------------------------------------------------------- */
+/* Replaces read_fasta + validate_data + to_dense_data
+ * (src/hamming_impl.cc:200-242, :80-91, :190-198, :244-267) and, with
+ * HD_SEM_CPU, the consensus/heuristic of include/hamming/hamming_impl.hh:
+ * 95-118. `fasta` holds the raw FASTA bytes, in host memory
+ * (fasta_on_device = 0; pinned memory from hd_host_alloc is fastest) or
+ * device memory (1). The bytes are parsed, deduplicated (remove_duplicates:
+ * unique rows in first-occurrence order) and packed into bit planes on the
+ * GPU. n_limit = 0 reads every record. Errors: HD_ERR_EMPTY, HD_ERR_LENGTH,
+ * HD_ERR_INCLUDE_X_GPU (semantics HD_SEM_GPU with include_x). */
+int hd_alignment_from_fasta(hd_ctx *ctx, const char *fasta, uint64_t nbytes,
+                            int fasta_on_device, int remove_duplicates,
+                            uint64_t n_limit, int include_x, int semantics,
+                            hd_alignment **out);
+/* Same from n sequences held back to back in `bytes` with offsets[0..n]
+ * (host memory). Replaces the DataSet(std::vector<std::string>&) path of
+ * from_stringlist (src/hamming.cc:16-21). */
+int hd_alignment_from_sequences(hd_ctx *ctx, const char *bytes,
+                                const uint64_t *offsets, uint64_t n,
+                                int include_x, int semantics,
+                                hd_alignment **out);
+/* Rows (after dedupe), sites per row, records read, rule in use. */
+int hd_alignment_info(const hd_alignment *aln, uint64_t *n_rows,
+                      uint64_t *length, uint64_t *n_input, int *rule);
+/* sequence_indices of read_fasta (src/hamming_impl.cc:228): n_input entries,
+ * the unique row of each input record; identity without dedupe. */
+int hd_alignment_sequence_indices(const hd_alignment *aln, uint64_t *out);
+void hd_alignment_free(hd_alignment *aln);
+
+/* ---- pairwise lower triangle ------------------------------------------- */
+/* Replaces distances_cuda_8bit / distances_cuda_16bit
+ * (src/distance_cuda.cu:204-214; header include/hamming/distance_cuda.hh:
+ * 19-25) and the dense/sparse CPU loops of include/hamming/hamming_impl.hh:
+ * 120-175. Writes lt[i(i-1)/2 + j] = min(count(i, j), max_dist) for i > j,
+ * n_rows(n_rows-1)/2 entries of dtype_bytes (1 = uint8, 2 = uint16,
+ * 4 = uint32). max_distance is clamped like safe_int_cast
+ * (include/hamming/hamming_impl.hh:37-45): above the dtype maximum it
+ * saturates, negative values wrap. `out` is host memory (out_on_device = 0)
+ * or device memory (1). */
+int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes,
+                   int64_t max_distance, void *out, int out_on_device);
+
+/* Replaces distances_cuda_to_lower_triangular (src/distance_cuda.cu:
+ * 216-223) with the streamed writer of partial_write_lower_triangular
+ * (include/hamming/hamming_utils.hh:64-104): uint16 distances, the text is
+ * formatted on the GPU and written to `path` while later rows compute.
+ * With fewer than 2 rows the file is left untouched, as in the reference. */
+int hd_pairwise_lt_to_file(hd_ctx *ctx, const hd_alignment *aln,
+                           int64_t max_distance, const char *path);
+
+/* ---- writers over a lower triangle held by the caller ------------------- */
+/* Replaces write_lower_triangular (include/hamming/hamming_utils.hh:106-110)
+ * as used by DataSet::dump_lower_triangular (include/hamming/hamming.hh:
+ * 75-77). `lt` is host memory with nsamples(nsamples-1)/2 entries. */
+int hd_write_lower_triangular(hd_ctx *ctx, const void *lt, uint64_t nsamples,
+                              int dtype_bytes, const char *path);
+/* Replaces DataSet::dump_sparse (include/hamming/hamming.hh:79-114): lines
+ * "i j d\n" for i > j and d <= threshold, in ascending row order (one of the
+ * orders the reference's OpenMP build can produce). *n_lines gets the count
+ * (may be NULL). */
+int hd_write_sparse(hd_ctx *ctx, const void *lt, uint64_t nsamples,
+                    int dtype_bytes, int64_t threshold, const char *path,
+                    uint64_t *n_lines);
+
+/* ---- reference distances / indices / single pair ------------------------ */
+/* Replaces fasta_reference_distances (src/hamming.cc:104-141): one uint32
+ * distance per FASTA record against `ref` under the rule of src/hamming.cc:
+ * 128-136. *out is allocated here (free with hd_free), *n_out entries.
+ * A record longer than `ref` fails with HD_ERR_REF_LENGTH (the reference
+ * reads past its buffer there). */
+int hd_reference_distances(hd_ctx *ctx, const char *ref, uint64_t ref_len,
+                           const char *fasta, uint64_t nbytes, int include_x,
+                           uint32_t **out, uint64_t *n_out);
+/* Same against a resident alignment: one distance per INPUT record (rows
+ * expanded through the sequence indices). ref_len must equal the alignment's
+ * length. Used by the serving loop. */
+int hd_alignment_reference_distances(hd_ctx *ctx, const hd_alignment *aln,
+                                     const char *ref, uint64_t ref_len,
+                                     int include_x, uint32_t *out);
+/* Replaces fasta_sequence_indices (src/hamming.cc:76-102). *out allocated
+ * here (free with hd_free), *n_out entries. */
+int hd_fasta_sequence_indices(hd_ctx *ctx, const char *fasta, uint64_t nbytes,
+                              uint64_t n_limit, uint64_t **out,
+                              uint64_t *n_out);
+/* Replaces distance (src/hamming.cc:54-74) and distance_cuda
+ * (src/distance_cuda.cu:225-230): one pair under the reference-distance rule.
+ * Unequal lengths fail with HD_ERR_LENGTH. */
+int hd_distance(hd_ctx *ctx, const char *s0, uint64_t l0, const char *s1,
+                uint64_t l1, int include_x, uint32_t *out);
+
+/* ---- measurement --------------------------------------------------------- */
+/* Integer-pipe peaks of this device, measured by timing dependent LOP3 and
+ * POPC chains (lane operations per second) and the pairwise inner loop's
+ * instruction mix (pair-sites per second). No reference counterpart. */
+int hd_measure_int_peaks(hd_ctx *ctx, double *lop3_per_s, double *popc_per_s,
+                         double *mix_pair_sites_per_s);
+/* Device time of the last pairwise kernel launch sequence (ms, CUDA events on
+ * the launching stream) and the number of tiles it processed. */
+int hd_last_pairwise_timing(const hd_ctx *ctx, double *ms, uint64_t *tiles);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HAMMINGDIST_GB300_H */

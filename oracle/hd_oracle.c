@@ -231,33 +231,39 @@ void hdo_pack_row(const char *seq, uint64_t L, uint8_t *out) {
   for (; k < nb; ++k) out[k] = 0xff;
 }
 
-/* Dense AND rule: distance_cpp, src/hamming_impl.cc:131-140 (and the SIMD
- * variants src/distance_avx512.cc:6-76, which add an early exit once the
- * running count reaches max_dist). A nibble counts when (a & b) == 0. Eight
- * bytes at a time: a zero nibble of c = a & b is found by folding its four
- * bits into the nibble's low bit.                                           */
+/* Dense AND rule: distance_cpp, src/hamming_impl.cc:131-140, in the form of
+ * the reference's SIMD kernels (src/distance_neon.cc:6-69; the SSE2/AVX2/
+ * AVX-512 files are the same algorithm at other widths): per 16-byte vector,
+ * c = a & b; each nibble of c that is zero adds 1 to a uint8 lane counter;
+ * lanes are summed after at most 127 vectors (16 when max_dist < 255) and the
+ * count returns early once it reaches max_dist. GCC generic vectors make this
+ * NEON on aarch64 and SSE2 on x86_64 without architecture intrinsics.      */
+typedef uint8_t hdo_v16u8 __attribute__((vector_size(16)));
+
 static int hdo_distance_dense(const uint8_t *a, const uint8_t *b, uint64_t nbytes,
                               int max_dist) {
-  const uint64_t lo = 0x1111111111111111ull;
+  const hdo_v16u8 zero = {0};
+  const hdo_v16u8 m0 = zero + 0x0f, m1 = zero + 0xf0;
   int r = 0;
-  uint64_t nw = nbytes / 8;
-  uint64_t w = 0;
-  while (w < nw) {
-    uint64_t end = w + 256 < nw ? w + 256 : nw; /* 4096 sites per block */
-    int blk = 0;
-    for (; w < end; ++w) {
-      uint64_t x, y;
-      memcpy(&x, a + 8 * w, 8);
-      memcpy(&y, b + 8 * w, 8);
-      uint64_t c = x & y;
-      c |= c >> 1;
-      c |= c >> 2;
-      blk += __builtin_popcountll(~c & lo);
+  const uint64_t n_iter = nbytes / 16;
+  const uint64_t n_inner = max_dist >= 255 ? 127 : 16;
+  for (uint64_t i0 = 0; i0 < n_iter; i0 += n_inner) {
+    const uint64_t i1 = i0 + n_inner < n_iter ? i0 + n_inner : n_iter;
+    hdo_v16u8 acc = zero;
+    for (uint64_t i = i0; i < i1; ++i) {
+      hdo_v16u8 x, y;
+      memcpy(&x, a + 16 * i, 16);
+      memcpy(&y, b + 16 * i, 16);
+      const hdo_v16u8 c = x & y;
+      acc -= (hdo_v16u8)((c & m0) == zero);  /* -1 per zero nibble */
+      acc -= (hdo_v16u8)((c & m1) == zero);
     }
+    int blk = 0;
+    for (int k = 0; k < 16; ++k) blk += acc[k];
     r += blk;
     if (r >= max_dist) return max_dist;
   }
-  for (uint64_t i = nw * 8; i < nbytes; ++i) {
+  for (uint64_t i = n_iter * 16; i < nbytes; ++i) {
     uint8_t c = a[i] & b[i];
     r += ((c & 0x0f) == 0) + ((c & 0xf0) == 0);
   }
