@@ -11,6 +11,7 @@ only when newer than their outputs.
 from __future__ import annotations
 
 import os
+import platform
 import subprocess
 import sys
 import sysconfig
@@ -62,8 +63,22 @@ def _run_all(cmds: list[list[str]], verbose: bool) -> None:
         raise RuntimeError("native build failed:\n" + msg)
 
 
+def _arch_stamp_ok() -> bool:
+    """Outputs built on another machine architecture are rebuilt."""
+    stamp = os.path.join(BUILD, "ARCH")
+    ok = os.path.exists(stamp) and open(stamp).read().strip() == platform.machine()
+    if not ok:
+        for f in [LIBHD, EXT] + [os.path.join(BUILD, x) for x in os.listdir(BUILD)]:
+            if os.path.isfile(f):
+                os.remove(f)
+        with open(stamp, "w") as fh:
+            fh.write(platform.machine())
+    return ok
+
+
 def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
+    _arch_stamp_ok()
     nvcc = _nvcc()
     hdrs = _headers()
     objs, cmds = [], []

@@ -34,13 +34,20 @@ ERRORS = {
 
 def build(force: bool = False) -> str:
     """Compile hd_oracle.c into oracle/_build/libhd_oracle.so (gcc, OpenMP)."""
-    if force or not os.path.exists(_OUT) or os.path.getmtime(_OUT) < os.path.getmtime(_SRC):
+    import platform
+
+    stamp = _OUT + ".arch"
+    same_arch = os.path.exists(stamp) and open(stamp).read() == platform.machine()
+    if force or not same_arch or not os.path.exists(_OUT) or \
+            os.path.getmtime(_OUT) < os.path.getmtime(_SRC):
         os.makedirs(os.path.dirname(_OUT), exist_ok=True)
         tmp = _OUT + f".tmp{os.getpid()}"
         subprocess.check_call(
             ["gcc", "-O3", "-std=c11", "-fopenmp", "-shared", "-fPIC", _SRC, "-o", tmp]
         )
         os.replace(tmp, _OUT)
+        with open(stamp, "w") as f:
+            f.write(platform.machine())
     return _OUT
 
 
