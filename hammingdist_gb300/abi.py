@@ -38,6 +38,7 @@ SIGNATURES = {
     "hd_pairwise_lt_to_file": (ci, [vp, vp, i64, cp]),
     "hd_write_lower_triangular": (ci, [vp, vp, u64, ci, cp]),
     "hd_write_sparse": (ci, [vp, vp, u64, ci, i64, cp, P(u64)]),
+    "hd_lower_triangular_text_noalloc": (ci, [vp, vp, u64, ci, vp, u64, P(u64)]),
     "hd_reference_distances": (ci, [vp, vp, u64, vp, u64, ci, P(vp), P(u64)]),
     "hd_alignment_reference_distances": (ci, [vp, vp, vp, u64, ci, vp]),
     "hd_fasta_sequence_indices": (ci, [vp, vp, u64, u64, P(vp), P(u64)]),
@@ -187,6 +188,16 @@ class Context:
         self._check(lib().hd_write_sparse(self.h, lt.ctypes.data, nsamples, lt.dtype.itemsize,
                                           threshold, path.encode(), ctypes.byref(nl)))
         return nl.value
+
+    def lower_triangular_text_noalloc(self, d_lt: int, nsamples: int, dtype, d_text: int,
+                                      capacity: int) -> int:
+        """Formats a device lower triangle into a device text buffer without
+        allocating device memory; returns the number of text bytes."""
+        nb = u64()
+        self._check(lib().hd_lower_triangular_text_noalloc(
+            self.h, _ptr(d_lt), nsamples, np.dtype(dtype).itemsize, _ptr(d_text), capacity,
+            ctypes.byref(nb)))
+        return nb.value
 
     def reference_distances(self, ref, data: bytes, include_x=False) -> np.ndarray:
         ref = ref.encode() if isinstance(ref, str) else bytes(ref)

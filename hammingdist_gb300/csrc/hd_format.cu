@@ -7,6 +7,8 @@
 // per 32 entries each lane computes its text length, a warp prefix sum places
 // it, and the lane writes its digits. Row starts come from a device scan of
 // per-row text lengths.
+#include <mutex>
+
 #include "hd_internal.cuh"
 
 namespace hd {
@@ -216,3 +218,109 @@ uint64_t format_sparse_rows(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint
 }
 
 }  // namespace hd
+
+// ===================================================== allocation-free text
+// A variant of the lower-triangular formatter above for callers that must not
+// allocate device memory: code that runs inside a host application whose
+// device memory is fully owned by its own allocator or capped by a fixed
+// budget, and latency-critical loops that cannot afford cudaMalloc/cudaFree
+// (cudaFree synchronises the whole device). Its scratch (per-row text
+// lengths, their offsets and the scan's block sums) lives in one file-scope
+// device array of fixed size instead of pool allocations.
+namespace {
+
+constexpr uint64_t kNoAllocMaxRows = 262144;  // rows of text (nsamples - 1)
+constexpr uint64_t kNoAllocMaxBlocks = (kNoAllocMaxRows + hd::kScanTile - 1) / hd::kScanTile;
+constexpr uint64_t kNoAllocWords = 2 * kNoAllocMaxRows + kNoAllocMaxBlocks + 8;  // ~4.2 MB
+
+// Held by every GPU that loads the library, until the process exits.
+static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocWords];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint64_t *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on `device`, looked up once per device
+// with that device current (in host code the array's name is only a host-side
+// stand-in, not a device address).
+uint64_t *noalloc_scratch(int device) {
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    hd::fail(HD_ERR_ARG, "device ordinal out of range for the allocation-free formatter");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      hd::fail(HD_ERR_CUDA, std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+    g_noalloc_ptr[device] = static_cast<uint64_t *>(p);
+  }
+  return g_noalloc_ptr[device];
+}
+
+template <typename T>
+uint64_t noalloc_text(hd_ctx *ctx, const T *d_lt, uint64_t nsamples, char *d_text,
+                      uint64_t capacity, uint64_t *scratch) {
+  using namespace hd;
+  const uint64_t rows = nsamples - 1;  // text rows i = 1 .. nsamples-1
+  uint64_t *row_len = scratch;
+  uint64_t *row_off = scratch + kNoAllocMaxRows;
+  uint64_t *sums = scratch + 2 * kNoAllocMaxRows;
+  uint64_t *total = sums + kNoAllocMaxBlocks;
+  const uint64_t nb = ceil_div(rows, kScanTile);
+  const unsigned g = warp_grid(ctx, rows);
+  cudaStream_t st = ctx->stream;
+  // every scratch word read below is written earlier in this call, so nothing
+  // has to be cleared between calls
+  k_lt_len<T><<<g, 256, 0, st>>>(d_lt, 0, 1, rows, row_len);
+  HD_LAUNCHED(ctx);
+  k_scan_reduce<uint64_t><<<(unsigned)nb, kScanThreads, 0, st>>>(row_len, rows, sums);
+  HD_LAUNCHED(ctx);
+  k_scan_top<void><<<1, 1024, 0, st>>>(sums, nb, total);
+  HD_LAUNCHED(ctx);
+  k_scan_down<uint64_t><<<(unsigned)nb, kScanThreads, 0, st>>>(row_len, row_off, rows, sums);
+  HD_LAUNCHED(ctx);
+  uint64_t bytes = 0;
+  HD_CUDA(cudaMemcpyAsync(&bytes, total, sizeof(bytes), cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  if (bytes > capacity) return bytes;  // the caller reports the shortfall
+  k_lt_write<T><<<g, 256, 0, st>>>(d_lt, 0, 1, rows, row_off, d_text);
+  HD_LAUNCHED(ctx);
+  HD_CUDA(cudaStreamSynchronize(st));
+  return bytes;
+}
+
+}  // namespace
+
+extern "C" int hd_lower_triangular_text_noalloc(hd_ctx *ctx, const void *d_lt, uint64_t nsamples,
+                                                int dtype_bytes, char *d_text,
+                                                uint64_t text_capacity, uint64_t *text_bytes) {
+  if (!ctx || !text_bytes) return HD_ERR_ARG;
+  *text_bytes = 0;
+  try {
+    HD_CUDA(cudaSetDevice(ctx->device));
+    if (dtype_bytes != 1 && dtype_bytes != 2 && dtype_bytes != 4)
+      hd::fail(HD_ERR_ARG, "dtype_bytes must be 1, 2 or 4");
+    if (nsamples > kNoAllocMaxRows)
+      hd::fail(HD_ERR_ARG, "hd_lower_triangular_text_noalloc: nsamples " + std::to_string(nsamples) +
+                               " exceeds its fixed scratch limit of " +
+                               std::to_string(kNoAllocMaxRows) + " rows");
+    if (nsamples < 2) return HD_OK;  // no entries, no text
+    if (!d_lt || (!d_text && text_capacity)) hd::fail(HD_ERR_ARG, "null buffer");
+    uint64_t *scratch = noalloc_scratch(ctx->device);
+    uint64_t need;
+    if (dtype_bytes == 1)
+      need = noalloc_text(ctx, static_cast<const uint8_t *>(d_lt), nsamples, d_text, text_capacity, scratch);
+    else if (dtype_bytes == 2)
+      need = noalloc_text(ctx, static_cast<const uint16_t *>(d_lt), nsamples, d_text, text_capacity, scratch);
+    else
+      need = noalloc_text(ctx, static_cast<const uint32_t *>(d_lt), nsamples, d_text, text_capacity, scratch);
+    *text_bytes = need;
+    if (need > text_capacity)
+      hd::fail(HD_ERR_ARG, "text buffer too small: " + std::to_string(need) + " bytes needed");
+    return HD_OK;
+  } catch (const hd::Error &e) {
+    ctx->err = e.msg;
+    return e.code;
+  }
+}
+

@@ -147,6 +147,28 @@ int hd_write_sparse(hd_ctx *ctx, const void *lt, uint64_t nsamples,
                     int dtype_bytes, int64_t threshold, const char *path,
                     uint64_t *n_lines);
 
+/* Lower-triangular text of a lower triangle already in device memory, into a
+ * caller-provided device buffer, WITHOUT ANY DEVICE ALLOCATION. No
+ * counterpart in the reference. For callers that cannot allocate device
+ * memory: applications whose device memory is owned by their own allocator
+ * or held to a fixed budget, and loops that cannot pay for cudaMalloc /
+ * cudaFree (cudaFree synchronises the device). Same bytes as
+ * hd_write_lower_triangular writes to a file.
+ *  - Limit: nsamples <= 262144; larger inputs fail with HD_ERR_ARG before
+ *    any work. The scratch is a fixed ~4.2 MB device array in the library,
+ *    held on every GPU that loads it until the process exits.
+ *  - The first call on a device looks up that array's device address (once
+ *    per device); make that first call before any stream capture.
+ *  - *text_bytes receives the text size; if it exceeds text_capacity the
+ *    call fails with HD_ERR_ARG and writes no text.
+ *  - All calls share the one scratch array: calls that overlap on the GPU
+ *    (other threads, other contexts on the same device) race and must not
+ *    be issued. */
+int hd_lower_triangular_text_noalloc(hd_ctx *ctx, const void *d_lt,
+                                     uint64_t nsamples, int dtype_bytes,
+                                     char *d_text, uint64_t text_capacity,
+                                     uint64_t *text_bytes);
+
 /* ---- reference distances / indices / single pair ------------------------ */
 /* Replaces fasta_reference_distances (src/hamming.cc:104-141): one uint32
  * distance per FASTA record against `ref` under the rule of src/hamming.cc:
