@@ -367,6 +367,35 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_kernel_only(args):
+    """The pairwise kernel alone on n distinct rows (profiling harness):
+    one alignment resident in HBM, warmup + steps launches of hd_pairwise_lt
+    into a device buffer, CUDA-event time per launch."""
+    import torch
+
+    from hammingdist_gb300 import abi, synth
+
+    ctx = abi.Context(0)
+    rows, _, _ = synth.alignment(args.n, args.L, p=P_SUB, seed=SEED)
+    seqs = [r.tobytes() for r in rows]
+    aln = ctx.alignment_from_sequences(seqs)
+    n = aln.n_rows
+    pairs = n * (n - 1) // 2
+    dt = np.uint16 if args.dtype == "u16" else np.uint8
+    out = torch.empty(pairs * np.dtype(dt).itemsize, dtype=torch.uint8, device="cuda:0")
+    torch.cuda.synchronize()
+    ms = []
+    for k in range(args.warmup + args.steps):
+        ctx.pairwise_lt(aln, dtype=dt, max_distance=255, out=out.data_ptr(), out_on_device=True)
+        if k >= args.warmup:
+            ms.append(ctx.last_pairwise_timing()[0])
+    mean = sum(ms) / len(ms)
+    print(json.dumps({"mode": "kernel-only", "n": n, "L": args.L, "dtype": args.dtype,
+                      "kernel_ms": mean, "pair_sites_T": pairs * args.L / (mean / 1e3) / 1e12,
+                      "launches": ctx.kernel_launches}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -375,8 +404,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="profiling harness: the pairwise kernel alone on --n distinct rows")
+    ap.add_argument("--n", type=int, default=12000)
+    ap.add_argument("--L", type=int, default=L)
+    ap.add_argument("--dtype", default="u8", choices=["u8", "u16"])
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.kernel_only:
+        run_kernel_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
