@@ -36,11 +36,51 @@ struct PairCfg {
   static constexpr int min_blocks = G == 1 ? 2 : 1;
 };
 
+// acc + p * one, issued as IMAD on the FMA pipe: `one` is a kernel argument
+// (always 1) that the compiler cannot fold, which keeps the accumulation off
+// the ALU pipe that the LOP3s saturate.
+__device__ __forceinline__ uint32_t mad_acc(uint32_t acc, uint32_t p, uint32_t one) {
+  uint32_t d;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(p), "r"(one), "r"(acc));
+  return d;
+}
+
+constexpr uint32_t kBand = 16;  // tile rows per L2 band
+
+// Tile of this CTA. Tiles are numbered row-major over the launch's tile rows
+// [row_lo, row_hi); inside each band of kBand tile rows the order is
+// column-major over the band's rectangle (J < I_lo) and row-major over its
+// triangle, so the CTAs resident at one time share the band's A tiles and
+// each B tile in L2.
+__device__ inline void tile_of(uint64_t t, uint32_t row_lo, uint32_t row_hi, uint32_t &I,
+                               uint32_t &J) {
+  uint32_t Ir = (uint32_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while ((uint64_t)(Ir + 1) * (Ir + 2) / 2 <= t) ++Ir;
+  while ((uint64_t)Ir * (Ir + 1) / 2 > t) --Ir;
+  const uint32_t I_lo = row_lo + (Ir - row_lo) / kBand * kBand;
+  const uint32_t I_hi = min(I_lo + kBand, row_hi);
+  const uint32_t h = I_hi - I_lo;
+  const uint64_t u = t - (uint64_t)I_lo * (I_lo + 1) / 2;
+  const uint64_t rect = (uint64_t)h * I_lo;
+  if (u < rect) {
+    J = (uint32_t)(u / h);
+    I = I_lo + (uint32_t)(u % h);
+  } else {
+    const uint64_t v = u - rect;
+    uint32_t i = (uint32_t)((sqrt(8.0 * (double)v + 1.0) - 1.0) * 0.5);
+    while ((uint64_t)(i + 1) * (i + 2) / 2 <= v) ++i;
+    while ((uint64_t)i * (i + 1) / 2 > v) --i;
+    I = I_lo + i;
+    J = I_lo + (uint32_t)(v - (uint64_t)i * (i + 1) / 2);
+  }
+}
+
 template <int G, int P, typename OutT>
 __global__ void __launch_bounds__(kThreads, PairCfg<G>::min_blocks)
     k_pairwise(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
                uint32_t n, uint32_t nk, uint32_t max_dist, OutT *__restrict__ out,
-               uint64_t out_base, uint64_t tile0, int *status) {
+               uint64_t out_base, uint64_t tile0, uint32_t row_lo, uint32_t row_hi, uint32_t one,
+               int *status) {
   constexpr int S = PairCfg<G>::stages;
   constexpr uint32_t SB = PairCfg<G>::stage_bytes;
   extern __shared__ uint8_t smem_raw[];
@@ -49,12 +89,8 @@ __global__ void __launch_bounds__(kThreads, PairCfg<G>::min_blocks)
       reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
 
   const uint32_t tid = threadIdx.x;
-  // tile t -> (I, J) with t = I(I+1)/2 + J, 0 <= J <= I
-  const uint64_t t = tile0 + blockIdx.x;
-  uint32_t I = (uint32_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-  while ((uint64_t)(I + 1) * (I + 2) / 2 <= t) ++I;
-  while ((uint64_t)I * (I + 1) / 2 > t) --I;
-  const uint32_t J = (uint32_t)(t - (uint64_t)I * (I + 1) / 2);
+  uint32_t I, J;
+  tile_of(tile0 + blockIdx.x, row_lo, row_hi, I, J);
 
   if (tid == 0) {
     prefetch_tmap(&tm0);
@@ -130,7 +166,7 @@ __global__ void __launch_bounds__(kThreads, PairCfg<G>::min_blocks)
             m |= a4[r] & b4;
             if (P == 6) m |= a5[r] & b5;
           }
-          acc[r][c] += __popc(~m);
+          acc[r][c] = mad_acc(acc[r][c], __popc(~m), one);
         }
       }
     }
@@ -181,8 +217,10 @@ static void make_tmap(hd_ctx *ctx, CUtensorMap *tm, const void *base, uint64_t w
 
 template <int G, int P, typename OutT>
 static void launch(hd_ctx *ctx, const CUtensorMap &tm0, const CUtensorMap &tm1, uint32_t n,
-                   uint32_t nk, uint32_t max_dist, void *d_out, uint64_t out_base, uint64_t t0,
-                   uint64_t t1) {
+                   uint32_t nk, uint32_t max_dist, void *d_out, uint64_t out_base,
+                   uint32_t row_lo, uint32_t row_hi) {
+  const uint64_t t0 = (uint64_t)row_lo * (row_lo + 1) / 2;
+  const uint64_t t1 = (uint64_t)row_hi * (row_hi + 1) / 2;
   auto kern = k_pairwise<G, P, OutT>;
   static bool configured = false;  // per instantiation
   if (!configured) {
@@ -193,7 +231,8 @@ static void launch(hd_ctx *ctx, const CUtensorMap &tm0, const CUtensorMap &tm1, 
   for (uint64_t t = t0; t < t1;) {
     uint64_t cnt = t1 - t < 0x7fffffffull ? t1 - t : 0x7fffffffull;
     kern<<<(unsigned)cnt, kThreads, PairCfg<G>::smem_bytes, ctx->stream>>>(
-        tm0, tm1, n, nk, max_dist, static_cast<OutT *>(d_out), out_base, t, ctx->d_status);
+        tm0, tm1, n, nk, max_dist, static_cast<OutT *>(d_out), out_base, t, row_lo, row_hi, 1u,
+        ctx->d_status);
     HD_LAUNCHED(ctx);
     t += cnt;
   }
@@ -202,13 +241,13 @@ static void launch(hd_ctx *ctx, const CUtensorMap &tm0, const CUtensorMap &tm1, 
 template <int G, int P>
 static void launch_dtype(hd_ctx *ctx, int dtype_bytes, const CUtensorMap &tm0,
                          const CUtensorMap &tm1, uint32_t n, uint32_t nk, uint32_t max_dist,
-                         void *d_out, uint64_t out_base, uint64_t t0, uint64_t t1) {
+                         void *d_out, uint64_t out_base, uint32_t lo, uint32_t hi) {
   if (dtype_bytes == 1)
-    launch<G, P, uint8_t>(ctx, tm0, tm1, n, nk, max_dist, d_out, out_base, t0, t1);
+    launch<G, P, uint8_t>(ctx, tm0, tm1, n, nk, max_dist, d_out, out_base, lo, hi);
   else if (dtype_bytes == 2)
-    launch<G, P, uint16_t>(ctx, tm0, tm1, n, nk, max_dist, d_out, out_base, t0, t1);
+    launch<G, P, uint16_t>(ctx, tm0, tm1, n, nk, max_dist, d_out, out_base, lo, hi);
   else
-    launch<G, P, uint32_t>(ctx, tm0, tm1, n, nk, max_dist, d_out, out_base, t0, t1);
+    launch<G, P, uint32_t>(ctx, tm0, tm1, n, nk, max_dist, d_out, out_base, lo, hi);
 }
 
 void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
@@ -224,11 +263,11 @@ void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint3
   if (aln->groups == 2) make_tmap(ctx, &tm1, aln->plane_buf[1].p, aln->words, aln->n_rows);
   else tm1 = tm0;
   if (aln->planes == 4)
-    launch_dtype<1, 4>(ctx, dtype_bytes, tm0, tm1, n, nk, max_dist, d_out, out_base, t0, t1);
+    launch_dtype<1, 4>(ctx, dtype_bytes, tm0, tm1, n, nk, max_dist, d_out, out_base, tile_lo, tile_hi);
   else if (aln->planes == 5)
-    launch_dtype<2, 5>(ctx, dtype_bytes, tm0, tm1, n, nk, max_dist, d_out, out_base, t0, t1);
+    launch_dtype<2, 5>(ctx, dtype_bytes, tm0, tm1, n, nk, max_dist, d_out, out_base, tile_lo, tile_hi);
   else
-    launch_dtype<2, 6>(ctx, dtype_bytes, tm0, tm1, n, nk, max_dist, d_out, out_base, t0, t1);
+    launch_dtype<2, 6>(ctx, dtype_bytes, tm0, tm1, n, nk, max_dist, d_out, out_base, tile_lo, tile_hi);
   ctx->last_pair_tiles += t1 - t0;
 }
 
