@@ -14,8 +14,9 @@
 //    of the 128 A-rows and the 128 B-rows per stage into shared memory, three
 //    stages deep, completion tracked by mbarriers (bounded waits);
 //  * each of the 256 threads owns an 8 x 8 block of pairs and, per word,
-//    counts mismatches as popc(~((a0&b0)|(a1&b1)|(a2&b2)|(a3&b3))): four
-//    LOP3 and one POPC per 32 pair-sites;
+//    counts matching sites as popc((a0&b0)|(a1&b1)|(a2&b2)|(a3&b3)): four
+//    LOP3 and one POPC per 32 pair-sites (mismatches = sites - matches, as
+//    every padded site matches);
 //  * the epilogue saturates with min(count, max_dist) (safe_int_cast,
 //    include/hamming/hamming_impl.hh:37-45), stages the tile in shared memory
 //    and writes each row's contiguous lower-triangle span.
@@ -42,6 +43,13 @@ struct PairCfg {
 __device__ __forceinline__ uint32_t mad_acc(uint32_t acc, uint32_t p, uint32_t one) {
   uint32_t d;
   asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(p), "r"(one), "r"(acc));
+  return d;
+}
+
+// x | (y & z) as one LOP3 (truth table 0xF8).
+__device__ __forceinline__ uint32_t or_and(uint32_t x, uint32_t y, uint32_t z) {
+  uint32_t d;
+  asm("lop3.b32 %0, %1, %2, %3, 0xF8;" : "=r"(d) : "r"(x), "r"(y), "r"(z));
   return d;
 }
 
@@ -161,12 +169,16 @@ __global__ void __launch_bounds__(kThreads, PairCfg<G>::min_blocks)
         }
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-          uint32_t m = (a[r].x & b.x) | (a[r].y & b.y) | (a[r].z & b.z) | (a[r].w & b.w);
+          // match bits: four LOP3 per word (one more per extra plane)
+          uint32_t m = a[r].x & b.x;
+          m = or_and(m, a[r].y, b.y);
+          m = or_and(m, a[r].z, b.z);
+          m = or_and(m, a[r].w, b.w);
           if constexpr (G == 2) {
-            m |= a4[r] & b4;
-            if (P == 6) m |= a5[r] & b5;
+            m = or_and(m, a4[r], b4);
+            if (P == 6) m = or_and(m, a5[r], b5);
           }
-          acc[r][c] = mad_acc(acc[r][c], __popc(~m), one);
+          acc[r][c] = mad_acc(acc[r][c], __popc(m), one);
         }
       }
     }
@@ -181,13 +193,16 @@ __global__ void __launch_bounds__(kThreads, PairCfg<G>::min_blocks)
     }
   }
 
-  // epilogue: saturate, stage the tile, store each row's contiguous span
+  // epilogue: mismatches = sites - matches; saturate, stage the tile, store
+  // each row's contiguous span
+  const uint32_t sites = nk * kKW * 32;
   OutT *tile = reinterpret_cast<OutT *>(smem);
 #pragma unroll
   for (int r = 0; r < 8; ++r)
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-      const uint32_t v = acc[r][c] < max_dist ? acc[r][c] : max_dist;
+      const uint32_t mism = sites - acc[r][c];  // every padded site matches
+      const uint32_t v = mism < max_dist ? mism : max_dist;
       tile[(ty + 16 * r) * kTile + tx + 16 * c] = (OutT)v;
     }
   __syncthreads();
