@@ -21,17 +21,20 @@ if not _os.path.exists(_EXT) or not _os.path.exists(_os.path.join(_PKG, "libhd.s
 from ._C import (  # noqa: E402,F401
     DataSet,
     DataSetLarge,
+    autotune,
     cuda_gpu_available,
     distance,
     fasta_reference_distances,
     fasta_sequence_indices,
     from_csv,
     from_fasta,
+    from_fasta_batch,
     from_fasta_large,
     from_fasta_to_lower_triangular,
     from_lower_triangular,
     from_lower_triangular_large,
     from_stringlist,
+    load_tuning,
     _kernel_launches,
 )
 

@@ -43,6 +43,16 @@ SIGNATURES = {
     "hd_alignment_reference_distances": (ci, [vp, vp, vp, u64, ci, vp]),
     "hd_fasta_sequence_indices": (ci, [vp, vp, u64, u64, P(vp), P(u64)]),
     "hd_distance": (ci, [vp, vp, u64, vp, u64, ci, P(ctypes.c_uint32)]),
+    "hd_batch_create": (ci, [vp, P(vp)]),
+    "hd_batch_add": (ci, [vp, vp, ci, i64, vp, ci]),
+    "hd_batch_run": (ci, [vp]),
+    "hd_batch_timing": (ci, [vp, P(ctypes.c_double), P(u64), P(u64)]),
+    "hd_batch_free": (None, [vp]),
+    "hd_alignments_from_fasta_many": (ci, [vp, u64, P(vp), P(u64), ci, u64, ci, ci, P(vp)]),
+    "hd_autotune": (ci, [vp, u64]),
+    "hd_tune_lookup": (ci, [vp, u64, u64, ci, P(ci), P(ci)]),
+    "hd_tune_save": (ci, [vp, cp]),
+    "hd_tune_load": (ci, [vp, cp]),
     "hd_measure_int_peaks": (ci, [vp, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
     "hd_last_pairwise_timing": (ci, [vp, P(ctypes.c_double), P(u64)]),
 }
@@ -228,6 +238,36 @@ class Context:
                                       int(include_x), ctypes.byref(d)))
         return int(d.value)
 
+    def alignments_from_fasta_many(self, datas, remove_duplicates=False, n=0, include_x=False,
+                                   semantics=SEM_GPU):
+        """Several alignments ingested concurrently (one per FASTA buffer)."""
+        k = len(datas)
+        bufs = (vp * k)(*[ctypes.cast(ctypes.c_char_p(d), vp) for d in datas])
+        sizes = (u64 * k)(*[len(d) for d in datas])
+        outs = (vp * k)()
+        self._check(lib().hd_alignments_from_fasta_many(self.h, k, bufs, sizes,
+                                                        int(remove_duplicates), n, int(include_x),
+                                                        semantics, outs))
+        return [Alignment(self, vp(outs[i])) for i in range(k)]
+
+    def batch(self) -> "Batch":
+        return Batch(self)
+
+    def autotune(self, max_n_bucket=6):
+        self._check(lib().hd_autotune(self.h, max_n_bucket))
+
+    def tune_lookup(self, n_rows, length, dtype):
+        t, s = ci(), ci()
+        self._check(lib().hd_tune_lookup(self.h, n_rows, length, np.dtype(dtype).itemsize,
+                                         ctypes.byref(t), ctypes.byref(s)))
+        return t.value, s.value
+
+    def tune_save(self, path):
+        self._check(lib().hd_tune_save(self.h, path.encode()))
+
+    def tune_load(self, path):
+        self._check(lib().hd_tune_load(self.h, path.encode()))
+
     def measure_int_peaks(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         self._check(lib().hd_measure_int_peaks(self.h, ctypes.byref(a), ctypes.byref(b),
@@ -238,6 +278,53 @@ class Context:
         ms, tiles = ctypes.c_double(), u64()
         self._check(lib().hd_last_pairwise_timing(self.h, ctypes.byref(ms), ctypes.byref(tiles)))
         return ms.value, tiles.value
+
+
+class Batch:
+    """Independent matrices computed together by the persistent engine; the
+    launches are captured in a CUDA graph on the first run and replayed."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = vp()
+        ctx._check(lib().hd_batch_create(ctx.h, ctypes.byref(h)))
+        self.h = h
+        self.outputs = []
+
+    def add(self, aln: Alignment, dtype=np.uint8, max_distance=255, out=None, out_on_device=False):
+        dt = np.dtype(dtype)
+        if out is None:
+            n = aln.n_rows
+            out = np.zeros(max(n * (n - 1) // 2, 1), dtype=dt)
+            self.outputs.append((out, n * (n - 1) // 2))
+            ptr = out.ctypes.data
+        else:
+            self.outputs.append((None, 0))
+            ptr = _ptr(out)
+        self.ctx._check(lib().hd_batch_add(self.h, aln.h, dt.itemsize, int(max_distance), ptr,
+                                           int(out_on_device)))
+        return len(self.outputs) - 1
+
+    def run(self):
+        self.ctx._check(lib().hd_batch_run(self.h))
+        return [o[: n] if o is not None else None for o, n in self.outputs]
+
+    def timing(self):
+        ms, launches, tiles = ctypes.c_double(), u64(), u64()
+        self.ctx._check(lib().hd_batch_timing(self.h, ctypes.byref(ms), ctypes.byref(launches),
+                                              ctypes.byref(tiles)))
+        return ms.value, launches.value, tiles.value
+
+    def free(self):
+        if self.h:
+            lib().hd_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def _take(ptr: ctypes.c_void_p, n: int, dtype) -> np.ndarray:

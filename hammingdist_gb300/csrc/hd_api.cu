@@ -4,9 +4,12 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <cstdio>
 #include <cstdlib>
 #include <limits>
+#include <thread>
 
 #include "hd_internal.cuh"
 
@@ -290,6 +293,8 @@ int hd_ctx_create(int device, hd_ctx **out) {
 
 void hd_ctx_destroy(hd_ctx *ctx) {
   if (!ctx) return;
+  for (hd_ctx *w : ctx->workers) hd_ctx_destroy(w);
+  ctx->workers.clear();
   cudaSetDevice(ctx->device);
   ctx->file.release();
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -591,6 +596,181 @@ int hd_last_pairwise_timing(const hd_ctx *ctx, double *ms, uint64_t *tiles) {
   if (ms) *ms = ctx->last_pair_ms;
   if (tiles) *tiles = ctx->last_pair_tiles;
   return HD_OK;
+}
+
+// ------------------------------------------------------------------ batches
+}  // extern "C"
+
+struct hd_batch {
+  hd_ctx *ctx = nullptr;
+  struct Job {
+    const hd_alignment *aln;
+    int dtype;
+    uint32_t max_dist;
+    void *out;
+    int out_on_device;
+  };
+  std::vector<Job> jobs;
+  bool built = false;
+  std::vector<DevBuf> staging;  // device outputs of host-output jobs
+  hd::PairLaunchPlan plan;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double last_ms = 0;
+  uint64_t tiles = 0;
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    plan = hd::PairLaunchPlan();
+    staging.clear();
+    built = false;
+  }
+  ~hd_batch() {
+    if (ctx) cudaSetDevice(ctx->device);
+    reset();
+  }
+};
+
+extern "C" {
+
+int hd_batch_create(hd_ctx *ctx, hd_batch **out) {
+  if (!ctx || !out) return HD_ERR_ARG;
+  *out = new hd_batch();
+  (*out)->ctx = ctx;
+  return HD_OK;
+}
+
+int hd_batch_add(hd_batch *b, const hd_alignment *aln, int dtype_bytes, int64_t max_distance,
+                 void *out, int out_on_device) {
+  if (!b || !aln) return HD_ERR_ARG;
+  return guard(b->ctx, [&] {
+    check_dtype(dtype_bytes);
+    if (!out && aln->n_rows >= 2) fail(HD_ERR_ARG, "null output");
+    b->jobs.push_back({aln, dtype_bytes, clamp_max(max_distance, dtype_bytes), out, out_on_device});
+    b->reset();  // the graph is rebuilt on the next run
+  });
+}
+
+int hd_batch_run(hd_batch *b) {
+  if (!b) return HD_ERR_ARG;
+  hd_ctx *ctx = b->ctx;
+  return guard(ctx, [&] {
+    cudaStream_t st = ctx->stream;
+    if (!b->built) {
+      std::vector<hd::PairJobSpec> specs;
+      b->staging.clear();
+      b->tiles = 0;
+      for (auto &j : b->jobs) {
+        const uint64_t n = j.aln->n_rows;
+        if (n < 2) continue;
+        hd::PairJobSpec s;
+        s.aln = j.aln;
+        s.dtype = j.dtype;
+        s.max_dist = j.max_dist;
+        if (j.out_on_device) {
+          s.d_out = j.out;
+        } else {
+          b->staging.emplace_back(tri(n) * j.dtype, st);
+          s.d_out = b->staging.back().p;
+        }
+        s.cfg = hd::tile_config_for(ctx, n, j.aln->length, j.dtype);
+        s.tile_lo = 0;
+        s.tile_hi = (uint32_t)hd::ceil_div(n, s.cfg.tile);
+        specs.push_back(s);
+      }
+      b->plan = hd::PairLaunchPlan();
+      hd::prepare_pairwise_jobs(ctx, specs, st, &b->plan);
+      HD_CUDA(cudaStreamSynchronize(st));
+      for (auto &L : b->plan.launches) b->tiles += L.tiles;
+      // capture the counter resets + persistent launches once
+      const uint64_t launches0 = ctx->launches;
+      HD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      hd::launch_pairwise_plan(ctx, b->plan, st);
+      HD_CUDA(cudaStreamEndCapture(st, &b->graph));
+      ctx->launches = launches0;  // counted when the graph runs
+      HD_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+      b->built = true;
+    }
+    HD_CUDA(cudaEventRecord(ctx->ev_start, st));
+    HD_CUDA(cudaGraphLaunch(b->exec, st));
+    ctx->launches += b->plan.launches.size();
+    size_t k = 0;
+    for (auto &j : b->jobs) {
+      if (j.aln->n_rows < 2 || j.out_on_device) continue;
+      HD_CUDA(cudaMemcpyAsync(j.out, b->staging[k].p, tri(j.aln->n_rows) * j.dtype,
+                              cudaMemcpyDeviceToHost, st));
+      ++k;
+    }
+    HD_CUDA(cudaEventRecord(ctx->ev_stop, st));
+    HD_CUDA(cudaStreamSynchronize(st));
+    float ms = 0;
+    HD_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+    b->last_ms = ms;
+    check_status(ctx);
+  });
+}
+
+int hd_batch_timing(const hd_batch *b, double *ms, uint64_t *launches, uint64_t *tiles) {
+  if (!b) return HD_ERR_ARG;
+  if (ms) *ms = b->last_ms;
+  if (launches) *launches = b->plan.launches.size();
+  if (tiles) *tiles = b->tiles;
+  return HD_OK;
+}
+
+void hd_batch_free(hd_batch *b) { delete b; }
+
+int hd_alignments_from_fasta_many(hd_ctx *ctx, uint64_t count, const char *const *fasta,
+                                  const uint64_t *nbytes, int remove_duplicates,
+                                  uint64_t n_limit, int include_x, int semantics,
+                                  hd_alignment **out) {
+  if (!ctx || !out || (count && (!fasta || !nbytes))) return HD_ERR_ARG;
+  for (uint64_t i = 0; i < count; ++i) out[i] = nullptr;
+  return guard(ctx, [&] {
+    const size_t nw = (size_t)std::min<uint64_t>(count, 8);
+    while (ctx->workers.size() < nw) {
+      hd_ctx *w = nullptr;
+      int rc = hd_ctx_create(ctx->device, &w);
+      if (rc != HD_OK) fail(rc, "could not create a worker context");
+      w->tune = ctx->tune;
+      ctx->workers.push_back(w);
+    }
+    std::vector<uint64_t> launches0;
+    for (hd_ctx *w : ctx->workers) launches0.push_back(w->launches);
+    std::atomic<uint64_t> next{0};
+    std::atomic<int> first_rc{HD_OK};
+    std::string first_msg;
+    std::mutex mu;
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nw; ++t) {
+      th.emplace_back([&, t] {
+        hd_ctx *w = ctx->workers[t];
+        for (uint64_t i = next++; i < count && first_rc.load() == HD_OK; i = next++) {
+          int rc = hd_alignment_from_fasta(w, fasta[i], nbytes[i], 0, remove_duplicates, n_limit,
+                                           include_x, semantics, &out[i]);
+          if (rc != HD_OK) {
+            std::lock_guard<std::mutex> lk(mu);
+            if (first_rc.load() == HD_OK) {
+              first_rc = rc;
+              first_msg = std::string(hd_last_error(w)) + " (input " + std::to_string(i) + ")";
+            }
+          }
+        }
+      });
+    }
+    for (auto &x : th) x.join();
+    for (size_t t = 0; t < ctx->workers.size(); ++t)
+      ctx->launches += ctx->workers[t]->launches - launches0[t];
+    if (first_rc.load() != HD_OK) {
+      for (uint64_t i = 0; i < count; ++i) {
+        hd_alignment_free(out[i]);
+        out[i] = nullptr;
+      }
+      fail(first_rc.load(), first_msg);
+    }
+  });
 }
 
 }  // extern "C"

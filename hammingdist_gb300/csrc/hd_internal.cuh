@@ -95,6 +95,10 @@ struct hd_ctx {
   uint64_t last_pair_tiles = 0;
   PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
   hd::DevBuf file;                // device copy of the last FASTA input
+  // autotuned kernel configurations: key = (n bucket, L bucket, dtype)
+  std::vector<std::pair<uint32_t, std::pair<int, int>>> tune;
+  // child contexts (own streams) for concurrent ingest of many inputs
+  std::vector<hd_ctx *> workers;
 };
 
 struct hd_alignment {
@@ -311,6 +315,46 @@ void alignment_query_distances(hd_ctx *ctx, const hd_alignment *aln, const uint8
 void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
                     void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi);
 constexpr uint32_t kTile = 128;
+
+// Kernel configuration of one job: tile edge (64 or 128 rows; 4 or 8 rows
+// per thread) and TMA staging depth.
+struct TileConfig {
+  int tile = 128;
+  int stages = 3;
+};
+// One matrix (or a range of its tile rows, in units of cfg.tile) for the
+// persistent engine.
+struct PairJobSpec {
+  const hd_alignment *aln = nullptr;
+  int dtype = 1;
+  uint32_t max_dist = 255;
+  void *d_out = nullptr;
+  uint64_t out_base = 0;
+  uint32_t tile_lo = 0, tile_hi = 0;
+  TileConfig cfg;
+};
+struct PairLaunchPlan {
+  struct Launch {
+    const void *fn = nullptr;  // kernel
+    int smem = 0, tile = 0, stages = 0;
+    uint64_t grid = 0, tiles = 0, jobs = 0;
+    const void *d_jobs = nullptr;
+    unsigned long long *d_counter = nullptr;
+  };
+  std::vector<Launch> launches;
+  std::vector<DevBuf> blocks;  // job tables + tensor maps + tile counters
+};
+void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStream_t stream,
+                           PairLaunchPlan *plan);
+void launch_pairwise_plan(hd_ctx *ctx, PairLaunchPlan &plan, cudaStream_t stream);
+void run_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStream_t stream,
+                       PairLaunchPlan *keep);
+void make_tmap(hd_ctx *ctx, CUtensorMap *tm, const void *base, uint64_t words, uint64_t rows,
+               uint32_t tile);
+TileConfig default_tile_config(uint64_t n_rows, uint64_t length, int dtype_bytes);
+bool tile_config_valid(int tile, int stages);
+// tune.cu: the autotuned table (or the default) for (n, L, dtype)
+TileConfig tile_config_for(hd_ctx *ctx, uint64_t n_rows, uint64_t length, int dtype_bytes);
 
 // format.cu: text of rows [i_lo, i_hi) of a lower triangle held on the
 // device (lt index lt_base at d_lt[0]). Returns bytes written to d_text

@@ -266,6 +266,92 @@ void from_fasta_to_lower_triangular(const std::string &in, const std::string &ou
   say("...distance calculation completed in " + std::to_string((long long)ms_since(t1)) + " ms.");
 }
 
+// Many FASTA files: concurrent ingest, then all matrices in one batch run
+// (persistent kernel over every job's tiles, launches replayed from a CUDA
+// graph). `large` / `max_distance` are one value or one per file; a large
+// entry gives a DataSetLarge (uint16) like from_fasta_large. No reference
+// counterpart: the reference computes one matrix per call.
+py::list from_fasta_batch(const std::vector<std::string> &files, bool include_x,
+                          bool remove_duplicates, size_t n, bool use_gpu, py::object max_distance,
+                          py::object large) {
+  const size_t k = files.size();
+  std::vector<int> big(k, 0);
+  std::vector<int64_t> md(k, 0);
+  for (size_t i = 0; i < k; ++i) {
+    big[i] = py::isinstance<py::sequence>(large) ? py::cast<bool>(large[py::int_(i)])
+                                                 : py::cast<bool>(large);
+    if (max_distance.is_none()) md[i] = big[i] ? 65535 : 255;
+    else if (py::isinstance<py::sequence>(max_distance)) md[i] = py::cast<int>(max_distance[py::int_(i)]);
+    else md[i] = py::cast<int>(max_distance);
+  }
+  std::vector<std::string> bytes(k);
+  for (size_t i = 0; i < k; ++i) {
+    std::ifstream f(files[i], std::ios::binary);
+    if (!f) open_failed(files[i]);
+    bytes[i].assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
+  std::vector<const char *> ptrs(k);
+  std::vector<uint64_t> sizes(k);
+  for (size_t i = 0; i < k; ++i) {
+    ptrs[i] = bytes[i].data();
+    sizes[i] = bytes[i].size();
+  }
+  std::vector<hd_alignment *> alns(k, nullptr);
+  std::vector<DataSet<uint8_t>> small(k);
+  std::vector<DataSet<uint16_t>> wide(k);
+  {
+    py::gil_scoped_release nogil;
+    check(hd_alignments_from_fasta_many(c, k, ptrs.data(), sizes.data(), remove_duplicates, n,
+                                        include_x, use_gpu ? HD_SEM_GPU : HD_SEM_CPU, alns.data()));
+    std::vector<Aln> own(k);
+    for (size_t i = 0; i < k; ++i) own[i].p = alns[i];
+    hd_batch *b = nullptr;
+    check(hd_batch_create(c, &b));
+    std::unique_ptr<hd_batch, void (*)(hd_batch *)> bguard(b, hd_batch_free);
+    for (size_t i = 0; i < k; ++i) {
+      uint64_t rows = 0, n_in = 0;
+      check(hd_alignment_info(alns[i], &rows, nullptr, &n_in, nullptr));
+      const uint64_t e = rows < 2 ? 0 : rows * (rows - 1) / 2;
+      if (big[i]) {
+        wide[i].nsamples = rows;
+        wide[i].result.resize(e);
+        check(hd_batch_add(b, alns[i], 2, md[i], wide[i].result.data(), 0));
+      } else {
+        small[i].nsamples = rows;
+        small[i].result.resize(e);
+        check(hd_batch_add(b, alns[i], 1, md[i], small[i].result.data(), 0));
+      }
+      if (remove_duplicates) {
+        auto &idx = big[i] ? wide[i].sequence_indices : small[i].sequence_indices;
+        idx.resize(n_in);
+        check(hd_alignment_sequence_indices(alns[i], idx.data()));
+      }
+    }
+    check(hd_batch_run(b));
+  }
+  py::list out;
+  for (size_t i = 0; i < k; ++i) {
+    if (big[i]) out.append(py::cast(std::move(wide[i])));
+    else out.append(py::cast(std::move(small[i])));
+  }
+  return out;
+}
+
+void autotune(const std::string &path) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
+  py::gil_scoped_release nogil;
+  check(hd_autotune(c, 6));
+  if (!path.empty()) check(hd_tune_save(c, path.c_str()));
+}
+
+void load_tuning(const std::string &path) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  check(hd_tune_load(ctx(), path.c_str()));
+}
+
 uint32_t distance(const std::string &s0, const std::string &s1, bool include_x) {
   std::lock_guard<std::mutex> lk(g_mu);
   hd_ctx *c = ctx();
@@ -414,6 +500,16 @@ PYBIND11_MODULE(_C, m) {
         "distances matrix which excludes duplicates");
   m.def("cuda_gpu_available", []() { return hd_device_available() != 0; },
         "True if a GPU that supports CUDA is available");
+  m.def("from_fasta_batch", &from_fasta_batch, py::arg("filenames"), py::arg("include_x") = false,
+        py::arg("remove_duplicates") = false, py::arg("n") = 0, py::arg("use_gpu") = true,
+        py::arg("max_distance") = py::none(), py::arg("large") = false,
+        "Distance matrices of several fasta files computed together on the GPU (one batch: "
+        "concurrent ingest, one persistent kernel, launches replayed from a CUDA graph). "
+        "Returns a list of DataSet (or DataSetLarge where `large`).");
+  m.def("autotune", &autotune, py::arg("path") = std::string(),
+        "Times the pairwise kernel configurations on this GPU, keeps the fastest per "
+        "(n, L, dtype) bucket and optionally saves the table as JSON");
+  m.def("load_tuning", &load_tuning, py::arg("path"), "Loads a table saved by autotune");
   m.def("_kernel_launches", []() -> uint64_t {
     std::lock_guard<std::mutex> lk(g_mu);
     return g_ctx ? hd_ctx_kernel_launches(g_ctx) : 0;

@@ -195,6 +195,47 @@ int hd_fasta_sequence_indices(hd_ctx *ctx, const char *fasta, uint64_t nbytes,
 int hd_distance(hd_ctx *ctx, const char *s0, uint64_t l0, const char *s1,
                 uint64_t l1, int include_x, uint32_t *out);
 
+/* ---- batches of independent matrices ------------------------------------ */
+/* No reference counterpart: the reference computes one matrix per call. A
+ * batch holds jobs (alignment, dtype, max_distance, output); hd_batch_run
+ * computes all of them with one persistent kernel per kernel configuration,
+ * whose CTAs draw triangle tiles of every job from a device counter, biggest
+ * jobs first. The launches are captured in a CUDA graph on the first run and
+ * replayed on later runs of the same batch. Outputs in host memory are
+ * staged on the device and copied back after the graph. */
+typedef struct hd_batch hd_batch;
+int hd_batch_create(hd_ctx *ctx, hd_batch **out);
+int hd_batch_add(hd_batch *b, const hd_alignment *aln, int dtype_bytes,
+                 int64_t max_distance, void *out, int out_on_device);
+int hd_batch_run(hd_batch *b);
+/* Device time of the last hd_batch_run (graph launch + copies, ms), the
+ * number of persistent launches in its graph and the tiles they process. */
+int hd_batch_timing(const hd_batch *b, double *ms, uint64_t *launches,
+                    uint64_t *tiles);
+void hd_batch_free(hd_batch *b);
+/* Builds `count` alignments from `count` FASTA buffers (host memory) in
+ * parallel on worker contexts with their own streams; same semantics per
+ * buffer as hd_alignment_from_fasta. On error nothing is returned and the
+ * message names the failing input. */
+int hd_alignments_from_fasta_many(hd_ctx *ctx, uint64_t count,
+                                  const char *const *fasta,
+                                  const uint64_t *nbytes,
+                                  int remove_duplicates, uint64_t n_limit,
+                                  int include_x, int semantics,
+                                  hd_alignment **out);
+
+/* ---- autotuning ------------------------------------------------------------ */
+/* Times every kernel configuration (tile edge 64/128 = 4/8 rows per thread,
+ * TMA staging depth 2-4) for each (n bucket <= max_n_bucket, L bucket,
+ * dtype) with the GPU filled, and keeps the fastest per bucket in the
+ * context. Without a table (or with HAMMINGDIST_TILE=<tile>x<stages>) a
+ * built-in choice applies. No reference counterpart. */
+int hd_autotune(hd_ctx *ctx, uint64_t max_n_bucket);
+int hd_tune_lookup(hd_ctx *ctx, uint64_t n_rows, uint64_t length,
+                   int dtype_bytes, int *tile, int *stages);
+int hd_tune_save(hd_ctx *ctx, const char *path);
+int hd_tune_load(hd_ctx *ctx, const char *path);
+
 /* ---- measurement --------------------------------------------------------- */
 /* Integer-pipe peaks of this device, measured by timing dependent LOP3 and
  * POPC chains (lane operations per second) and the pairwise inner loop's

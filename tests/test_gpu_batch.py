@@ -1,0 +1,146 @@
+"""The persistent engine on batches of independent matrices, its CUDA-graph
+replay, every kernel configuration the autotuner can pick, and
+from_fasta_batch against per-file from_fasta. All checks are bit-exact
+against the oracle or the single-matrix path."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gpu_util import seqidx_of, write
+from hammingdist_gb300 import synth
+from oracle import hd_oracle as o
+
+pytestmark = pytest.mark.gpu
+hd = pytest.importorskip("hammingdist_gb300")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from hammingdist_gb300 import abi
+
+    c = abi.Context(0)
+    yield c
+    c.close()
+
+
+def _mixed_inputs():
+    shapes = [(1, 40), (2, 17), (50, 1000), (129, 257), (300, 5000), (700, 333), (64, 65),
+              (1000, 2999)]
+    out = []
+    for k, (n, L) in enumerate(shapes):
+        seqs = synth.random_strings(n, L, b"ACGT-N", seed=500 + k)
+        out.append(seqs)
+    return out
+
+
+def test_batch_matches_single_and_oracle(ctx):
+    import torch
+
+    inputs = _mixed_inputs()
+    alns = [ctx.alignment_from_sequences(s) for s in inputs]
+    b = ctx.batch()
+    specs = []
+    for k, (a, seqs) in enumerate(zip(alns, inputs)):
+        dt = np.uint16 if k % 2 else np.uint8
+        md = [255, 65535, 3, 89, 0, 497, 255, 65535][k]
+        specs.append((dt, md))
+        b.add(a, dtype=dt, max_distance=md)
+    # one job with a device output
+    n_dev = alns[5].n_rows
+    d_out = torch.zeros(n_dev * (n_dev - 1) // 2 * 2, dtype=torch.uint8, device="cuda:0")
+    torch.cuda.synchronize()
+    b.add(alns[5], dtype=np.uint16, max_distance=777, out=d_out.data_ptr(), out_on_device=True)
+    for rep in range(2):  # second run replays the captured graph
+        outs = b.run()
+        for k, seqs in enumerate(inputs):
+            dt, md = specs[k]
+            want = o.lt_dense(seqs, max_distance=md, dtype=dt) if len(seqs) > 1 else np.zeros(0, dt)
+            np.testing.assert_array_equal(outs[k], want, err_msg=f"job {k} rep {rep}")
+            np.testing.assert_array_equal(ctx.pairwise_lt(alns[k], dtype=dt, max_distance=md), want)
+        got = d_out.cpu().numpy().view(np.uint16)
+        np.testing.assert_array_equal(got, o.lt_dense(inputs[5], max_distance=777, dtype=np.uint16))
+    ms, launches, tiles = b.timing()
+    assert ms > 0 and launches >= 1 and tiles > 0
+    b.free()
+
+
+def test_batch_sparse_rule_jobs(ctx):
+    from hammingdist_gb300 import abi
+
+    rows, _, _ = synth.alignment(150, 3000, p=1e-4, seed=61, dash_max=5)
+    rows[::9, ::17] = ord("X")
+    seqs = [r.tobytes() for r in rows]
+    b = ctx.batch()
+    a_x = ctx.alignment_from_sequences(seqs, include_x=True, semantics=abi.SEM_CPU)
+    a_s = ctx.alignment_from_sequences(seqs, include_x=False, semantics=abi.SEM_CPU)
+    assert a_x.rule == "sparse_x" and a_s.rule == "sparse"
+    b.add(a_x, dtype=np.uint8, max_distance=255)
+    b.add(a_s, dtype=np.uint16, max_distance=65535)
+    outs = b.run()
+    np.testing.assert_array_equal(outs[0], o.lt_cpu(seqs, include_x=True, max_distance=255)[0])
+    np.testing.assert_array_equal(outs[1], o.lt_cpu(seqs, include_x=False, max_distance=65535,
+                                                    dtype=np.uint16)[0])
+
+
+@pytest.mark.parametrize("tile,stages", [(128, 3), (128, 2), (128, 4), (64, 3), (64, 4)])
+def test_every_kernel_configuration(ctx, tmp_path, tile, stages):
+    """A tuning table that maps every bucket to one configuration: results are
+    the same bit for bit."""
+    entries = [{"n_bucket": nb, "L_bucket": lb, "dtype": dt, "tile": tile, "stages": stages}
+               for nb in range(7) for lb in range(4) for dt in (1, 2)]
+    path = str(tmp_path / "tune.json")
+    with open(path, "w") as f:
+        json.dump({"device": "test", "entries": entries}, f)
+    ctx.tune_load(path)
+    try:
+        assert ctx.tune_lookup(300, 1000, np.uint8) == (tile, stages)
+        for k, (n, L) in enumerate([(2, 5), (65, 300), (200, 4097), (513, 64)]):
+            seqs = synth.random_strings(n, L, b"ACGT-NX", seed=900 + k)
+            aln = ctx.alignment_from_sequences(seqs)
+            for dt, md in ((np.uint8, 255), (np.uint16, 40)):
+                np.testing.assert_array_equal(ctx.pairwise_lt(aln, dtype=dt, max_distance=md),
+                                              o.lt_dense(seqs, max_distance=md, dtype=dt))
+    finally:
+        with open(path, "w") as f:
+            json.dump({"entries": []}, f)
+        ctx.tune_load(path)  # back to the built-in choice
+
+
+def test_autotune_small_buckets(ctx, tmp_path):
+    ctx.autotune(max_n_bucket=1)
+    path = str(tmp_path / "t.json")
+    ctx.tune_save(path)
+    table = json.load(open(path))
+    assert len(table["entries"]) == 2 * 4 * 2
+    for e in table["entries"]:
+        assert (e["tile"], e["stages"]) in {(128, 3), (128, 2), (128, 4), (64, 3), (64, 4)}
+    ctx.tune_load(path)
+    seqs = synth.random_strings(150, 1500, b"ACGT-", seed=3)
+    aln = ctx.alignment_from_sequences(seqs)
+    np.testing.assert_array_equal(ctx.pairwise_lt(aln), o.lt_dense(seqs))
+
+
+def test_from_fasta_batch_matches_per_file_calls(tmp_path):
+    rng = np.random.default_rng(8)
+    files, large = [], []
+    for k in range(12):
+        n = int(np.exp(rng.uniform(np.log(20), np.log(600))))
+        L = int(rng.choice([100, 1000, 2999]))
+        rows, _, _ = synth.alignment(n, L, p=float(rng.uniform(1e-4, 1e-2)), seed=100 + k,
+                                     dup_frac=0.2)
+        files.append(write(tmp_path, f"f{k}.fasta", synth.to_fasta(rows)))
+        large.append(bool(k % 3 == 0))
+    for dedup in (False, True):
+        got = hd.from_fasta_batch(files, remove_duplicates=dedup, large=large)
+        assert len(got) == len(files)
+        for f, big, ds in zip(files, large, got):
+            ref = (hd.from_fasta_large if big else hd.from_fasta)(f, remove_duplicates=dedup,
+                                                                  use_gpu=True)
+            assert type(ds) is type(ref)
+            np.testing.assert_array_equal(np.asarray(ds.lt_array), np.asarray(ref.lt_array))
+            np.testing.assert_array_equal(seqidx_of(ds, tmp_path), seqidx_of(ref, tmp_path))
+    bad = write(tmp_path, "bad.fasta", b">a\nACGT\n>b\nAC\n")
+    with pytest.raises(RuntimeError, match="same length"):
+        hd.from_fasta_batch(files[:2] + [bad])
