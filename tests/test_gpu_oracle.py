@@ -152,7 +152,9 @@ def test_launches_and_device_output(ctx):
     assert ctx.kernel_launches > before
     np.testing.assert_array_equal(out.cpu().numpy(), o.lt_dense(seqs))
     ms, tiles = ctx.last_pairwise_timing()
-    assert ms > 0 and tiles == 2 * 3 // 2  # nb = 2 tiles per side -> 3 tiles
+    tile, _ = ctx.tune_lookup(n, 300, np.uint8)
+    nb = -(-n // tile)
+    assert ms > 0 and tiles == nb * (nb + 1) // 2
 
 
 def test_errors(ctx, tmp_path):
