@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -63,50 +64,58 @@ void check(int rc) {
   throw std::runtime_error("Error: Failed to open file '" + f + "'");
 }
 
-// Reads a whole file into the pinned staging buffer (parallel preads).
-std::pair<const char *, uint64_t> read_pinned(const std::string &path) {
-  int fd = ::open(path.c_str(), O_RDONLY);
-  if (fd < 0) open_failed(path);
-  struct stat sb;
-  if (fstat(fd, &sb) != 0 || !S_ISREG(sb.st_mode)) {
-    ::close(fd);
-    open_failed(path);
-  }
-  const uint64_t n = (uint64_t)sb.st_size;
-  if (n + 1 > g_pin_cap) {
+// Pinned staging buffer of at least n bytes (grows, never shrinks).
+char *pinned(uint64_t n) {
+  if (n > g_pin_cap) {
     if (g_pin) hd_host_free(g_ctx, g_pin);
     g_pin = nullptr;
     g_pin_cap = 0;
-    size_t cap = (size_t)((n + 1) * 5 / 4 + (1 << 20));
-    if (hd_host_alloc(g_ctx, cap, &g_pin) != HD_OK) {
-      ::close(fd);
-      throw std::runtime_error(hd_last_error(g_ctx));
-    }
+    size_t cap = (size_t)(n * 5 / 4 + (1 << 20));
+    if (hd_host_alloc(g_ctx, cap, &g_pin) != HD_OK) throw std::runtime_error(hd_last_error(g_ctx));
     g_pin_cap = cap;
   }
-  char *dst = static_cast<char *>(g_pin);
+  return static_cast<char *>(g_pin);
+}
+
+// Reads n bytes of `path` into dst with parallel preads (64 MB pieces).
+bool read_into(const std::string &path, char *dst, uint64_t n) {
+  int fd = ::open(path.c_str(), O_RDONLY);
+  if (fd < 0) return false;
   const uint64_t kPart = 64ull << 20;
   const unsigned nthreads = n > kPart ? std::min<unsigned>(8, (unsigned)((n + kPart - 1) / kPart)) : 1;
-  std::vector<std::thread> th;
   std::vector<int> ok(nthreads, 1);
   const uint64_t per = (n + nthreads - 1) / nthreads;
-  for (unsigned t = 0; t < nthreads; ++t) {
-    th.emplace_back([&, t] {
-      uint64_t off = t * per, end = std::min(n, off + per);
-      while (off < end) {
-        ssize_t r = ::pread(fd, dst + off, (size_t)std::min<uint64_t>(end - off, 1ull << 30), (off_t)off);
-        if (r <= 0) {
-          ok[t] = 0;
-          return;
-        }
-        off += (uint64_t)r;
+  auto work = [&](unsigned t) {
+    uint64_t off = t * per, end = std::min(n, off + per);
+    while (off < end) {
+      ssize_t r = ::pread(fd, dst + off, (size_t)std::min<uint64_t>(end - off, 1ull << 30), (off_t)off);
+      if (r <= 0) {
+        ok[t] = 0;
+        return;
       }
-    });
+      off += (uint64_t)r;
+    }
+  };
+  if (nthreads == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nthreads; ++t) th.emplace_back(work, t);
+    for (auto &x : th) x.join();
   }
-  for (auto &x : th) x.join();
   ::close(fd);
   for (int v : ok)
-    if (!v) open_failed(path);
+    if (!v) return false;
+  return true;
+}
+
+// Reads a whole file into the pinned staging buffer.
+std::pair<const char *, uint64_t> read_pinned(const std::string &path) {
+  struct stat sb;
+  if (::stat(path.c_str(), &sb) != 0 || !S_ISREG(sb.st_mode)) open_failed(path);
+  const uint64_t n = (uint64_t)sb.st_size;
+  char *dst = pinned(n + 1);
+  if (!read_into(path, dst, n)) open_failed(path);
   return {dst, n};
 }
 
@@ -284,19 +293,32 @@ py::list from_fasta_batch(const std::vector<std::string> &files, bool include_x,
     else if (py::isinstance<py::sequence>(max_distance)) md[i] = py::cast<int>(max_distance[py::int_(i)]);
     else md[i] = py::cast<int>(max_distance);
   }
-  std::vector<std::string> bytes(k);
-  for (size_t i = 0; i < k; ++i) {
-    std::ifstream f(files[i], std::ios::binary);
-    if (!f) open_failed(files[i]);
-    bytes[i].assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
-  }
   std::lock_guard<std::mutex> lk(g_mu);
   hd_ctx *c = ctx();
-  std::vector<const char *> ptrs(k);
-  std::vector<uint64_t> sizes(k);
+  // all files into one pinned buffer, read in parallel
+  std::vector<uint64_t> sizes(k), offs(k + 1, 0);
   for (size_t i = 0; i < k; ++i) {
-    ptrs[i] = bytes[i].data();
-    sizes[i] = bytes[i].size();
+    struct stat sb;
+    if (::stat(files[i].c_str(), &sb) != 0 || !S_ISREG(sb.st_mode)) open_failed(files[i]);
+    sizes[i] = (uint64_t)sb.st_size;
+    offs[i + 1] = offs[i] + sizes[i] + 16;
+  }
+  char *buf = pinned(offs[k] + 1);
+  std::vector<const char *> ptrs(k);
+  for (size_t i = 0; i < k; ++i) ptrs[i] = buf + offs[i];
+  {
+    py::gil_scoped_release nogil;
+    std::atomic<size_t> next{0};
+    std::atomic<long> bad{-1};
+    std::vector<std::thread> th;
+    const unsigned nt = std::min<unsigned>(16, (unsigned)std::max<size_t>(k, 1));
+    for (unsigned t = 0; t < nt; ++t)
+      th.emplace_back([&] {
+        for (size_t i = next++; i < k; i = next++)
+          if (!read_into(files[i], buf + offs[i], sizes[i])) bad = (long)i;
+      });
+    for (auto &x : th) x.join();
+    if (bad.load() >= 0) open_failed(files[bad.load()]);
   }
   std::vector<hd_alignment *> alns(k, nullptr);
   std::vector<DataSet<uint8_t>> small(k);
