@@ -18,6 +18,9 @@ if not _os.path.exists(_EXT) or not _os.path.exists(_os.path.join(_PKG, "libhd.s
         "hammingdist_gb300: native extension not built (libhd.so / _C). "
         "Run `python hammingdist_gb300/build.py` first; there is no CPU fallback.")
 
+# measured kernel configurations for GB300 (applied only on a matching device)
+_os.environ.setdefault("HAMMINGDIST_TUNING", _os.path.join(_PKG, "tuning", "gb300.json"))
+
 from ._C import (  # noqa: E402,F401
     DataSet,
     DataSetLarge,

@@ -49,6 +49,7 @@ SIGNATURES = {
     "hd_batch_timing": (ci, [vp, P(ctypes.c_double), P(u64), P(u64)]),
     "hd_batch_free": (None, [vp]),
     "hd_alignments_from_fasta_many": (ci, [vp, u64, P(vp), P(u64), ci, u64, ci, ci, P(vp)]),
+    "hd_alignments_from_fasta_files": (ci, [vp, u64, P(cp), ci, u64, ci, ci, P(vp)]),
     "hd_autotune": (ci, [vp, u64]),
     "hd_tune_lookup": (ci, [vp, u64, u64, ci, P(ci), P(ci)]),
     "hd_tune_save": (ci, [vp, cp]),
@@ -248,6 +249,16 @@ class Context:
         self._check(lib().hd_alignments_from_fasta_many(self.h, k, bufs, sizes,
                                                         int(remove_duplicates), n, int(include_x),
                                                         semantics, outs))
+        return [Alignment(self, vp(outs[i])) for i in range(k)]
+
+    def alignments_from_fasta_files(self, paths, remove_duplicates=False, n=0, include_x=False,
+                                    semantics=SEM_GPU):
+        """Several alignments from FASTA files: reads overlap device ingest."""
+        k = len(paths)
+        arr = (cp * k)(*[p.encode() for p in paths])
+        outs = (vp * k)()
+        self._check(lib().hd_alignments_from_fasta_files(self.h, k, arr, int(remove_duplicates), n,
+                                                         int(include_x), semantics, outs))
         return [Alignment(self, vp(outs[i])) for i in range(k)]
 
     def batch(self) -> "Batch":

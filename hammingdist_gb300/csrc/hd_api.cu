@@ -1,6 +1,7 @@
 // The C ABI (include/hammingdist_gb300.h): argument checks, error mapping,
 // host<->device movement and the orchestration of the device stages.
 #include <fcntl.h>
+#include <sys/stat.h>
 #include <unistd.h>
 
 #include <algorithm>
@@ -282,6 +283,21 @@ int hd_ctx_create(int device, hd_ctx **out) {
                                              cudaEnableDefault, &q));
     if (!fn || q != cudaDriverEntryPointSuccess) fail(HD_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     ctx->encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    // default autotuner table: HAMMINGDIST_TUNING names a file saved by
+    // hd_tune_save; it applies only if it was measured on this device kind
+    if (const char *path = std::getenv("HAMMINGDIST_TUNING")) {
+      cudaDeviceProp prop;
+      HD_CUDA(cudaGetDeviceProperties(&prop, device));
+      FILE *f = std::fopen(path, "rb");
+      if (f) {
+        char head[256] = {0};
+        size_t got = std::fread(head, 1, sizeof(head) - 1, f);
+        std::fclose(f);
+        head[got] = 0;
+        const std::string want = std::string("\"device\": \"") + prop.name + "\"";
+        if (std::string(head).find(want) != std::string::npos) hd_tune_load(ctx, path);
+      }
+    }
   });
   if (rc != HD_OK) {
     hd_ctx_destroy(ctx);
@@ -297,6 +313,7 @@ void hd_ctx_destroy(hd_ctx *ctx) {
   ctx->workers.clear();
   cudaSetDevice(ctx->device);
   ctx->file.release();
+  if (ctx->pin) cudaFreeHost(ctx->pin);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
@@ -722,55 +739,137 @@ int hd_batch_timing(const hd_batch *b, double *ms, uint64_t *launches, uint64_t 
 
 void hd_batch_free(hd_batch *b) { delete b; }
 
+}  // extern "C"
+
+namespace {
+
+// Runs job(worker ctx, i) for i in [0, count) on up to max_workers worker
+// contexts in parallel; stops at the first error and reports it (with the
+// input index) as the context's error. Worker kernel launches are added to
+// the parent's count.
+template <class Job>
+void run_on_workers(hd_ctx *ctx, uint64_t count, size_t max_workers, Job &&job) {
+  const size_t nw = (size_t)std::min<uint64_t>(count, max_workers);
+  while (ctx->workers.size() < nw) {
+    hd_ctx *w = nullptr;
+    int rc = hd_ctx_create(ctx->device, &w);
+    if (rc != HD_OK) fail(rc, "could not create a worker context");
+    ctx->workers.push_back(w);
+  }
+  std::vector<uint64_t> launches0;
+  for (hd_ctx *w : ctx->workers) {
+    w->tune = ctx->tune;
+    launches0.push_back(w->launches);
+  }
+  std::atomic<uint64_t> next{0};
+  std::atomic<int> first_rc{HD_OK};
+  std::string first_msg;
+  std::mutex mu;
+  std::vector<std::thread> th;
+  for (size_t t = 0; t < nw; ++t) {
+    th.emplace_back([&, t] {
+      hd_ctx *w = ctx->workers[t];
+      for (uint64_t i = next++; i < count && first_rc.load() == HD_OK; i = next++) {
+        int rc = job(w, i);
+        if (rc != HD_OK) {
+          std::lock_guard<std::mutex> lk(mu);
+          if (first_rc.load() == HD_OK) {
+            first_rc = rc;
+            first_msg = std::string(hd_last_error(w)) + " (input " + std::to_string(i) + ")";
+          }
+        }
+      }
+    });
+  }
+  for (auto &x : th) x.join();
+  for (size_t t = 0; t < ctx->workers.size() && t < launches0.size(); ++t)
+    ctx->launches += ctx->workers[t]->launches - launches0[t];
+  if (first_rc.load() != HD_OK) fail(first_rc.load(), first_msg);
+}
+
+// Reads `path` into the context's pinned buffer (grown as needed).
+int read_file_pinned(hd_ctx *w, const char *path, const char **data, uint64_t *size) {
+  return guard(w, [&] {
+    int fd = ::open(path, O_RDONLY);
+    struct stat sb;
+    if (fd < 0 || fstat(fd, &sb) != 0 || !S_ISREG(sb.st_mode)) {
+      if (fd >= 0) ::close(fd);
+      fail(HD_ERR_IO, std::string("Error: Failed to open file '") + path + "'");
+    }
+    const uint64_t n = (uint64_t)sb.st_size;
+    if (n + 1 > w->pin_cap) {
+      if (w->pin) cudaFreeHost(w->pin);
+      w->pin = nullptr;
+      w->pin_cap = 0;
+      const size_t cap = (size_t)((n + 1) * 3 / 2 + (1 << 20));
+      cudaError_t e = cudaHostAlloc(&w->pin, cap, cudaHostAllocDefault);
+      if (e != cudaSuccess) {
+        ::close(fd);
+        HD_CUDA(e);
+      }
+      w->pin_cap = cap;
+    }
+    char *dst = static_cast<char *>(w->pin);
+    uint64_t off = 0;
+    while (off < n) {
+      ssize_t r = ::pread(fd, dst + off, (size_t)std::min<uint64_t>(n - off, 1ull << 30), (off_t)off);
+      if (r <= 0) {
+        ::close(fd);
+        fail(HD_ERR_IO, std::string("Error: Failed to open file '") + path + "'");
+      }
+      off += (uint64_t)r;
+    }
+    ::close(fd);
+    *data = dst;
+    *size = n;
+  });
+}
+
+}  // namespace
+
+extern "C" {
+
 int hd_alignments_from_fasta_many(hd_ctx *ctx, uint64_t count, const char *const *fasta,
                                   const uint64_t *nbytes, int remove_duplicates,
                                   uint64_t n_limit, int include_x, int semantics,
                                   hd_alignment **out) {
   if (!ctx || !out || (count && (!fasta || !nbytes))) return HD_ERR_ARG;
   for (uint64_t i = 0; i < count; ++i) out[i] = nullptr;
-  return guard(ctx, [&] {
-    const size_t nw = (size_t)std::min<uint64_t>(count, 8);
-    while (ctx->workers.size() < nw) {
-      hd_ctx *w = nullptr;
-      int rc = hd_ctx_create(ctx->device, &w);
-      if (rc != HD_OK) fail(rc, "could not create a worker context");
-      w->tune = ctx->tune;
-      ctx->workers.push_back(w);
-    }
-    std::vector<uint64_t> launches0;
-    for (hd_ctx *w : ctx->workers) launches0.push_back(w->launches);
-    std::atomic<uint64_t> next{0};
-    std::atomic<int> first_rc{HD_OK};
-    std::string first_msg;
-    std::mutex mu;
-    std::vector<std::thread> th;
-    for (size_t t = 0; t < nw; ++t) {
-      th.emplace_back([&, t] {
-        hd_ctx *w = ctx->workers[t];
-        for (uint64_t i = next++; i < count && first_rc.load() == HD_OK; i = next++) {
-          int rc = hd_alignment_from_fasta(w, fasta[i], nbytes[i], 0, remove_duplicates, n_limit,
-                                           include_x, semantics, &out[i]);
-          if (rc != HD_OK) {
-            std::lock_guard<std::mutex> lk(mu);
-            if (first_rc.load() == HD_OK) {
-              first_rc = rc;
-              first_msg = std::string(hd_last_error(w)) + " (input " + std::to_string(i) + ")";
-            }
-          }
-        }
-      });
-    }
-    for (auto &x : th) x.join();
-    for (size_t t = 0; t < ctx->workers.size(); ++t)
-      ctx->launches += ctx->workers[t]->launches - launches0[t];
-    if (first_rc.load() != HD_OK) {
-      for (uint64_t i = 0; i < count; ++i) {
-        hd_alignment_free(out[i]);
-        out[i] = nullptr;
-      }
-      fail(first_rc.load(), first_msg);
-    }
+  int rc = guard(ctx, [&] {
+    run_on_workers(ctx, count, 8, [&](hd_ctx *w, uint64_t i) {
+      return hd_alignment_from_fasta(w, fasta[i], nbytes[i], 0, remove_duplicates, n_limit,
+                                     include_x, semantics, &out[i]);
+    });
   });
+  if (rc != HD_OK)
+    for (uint64_t i = 0; i < count; ++i) {
+      hd_alignment_free(out[i]);
+      out[i] = nullptr;
+    }
+  return rc;
+}
+
+int hd_alignments_from_fasta_files(hd_ctx *ctx, uint64_t count, const char *const *paths,
+                                   int remove_duplicates, uint64_t n_limit, int include_x,
+                                   int semantics, hd_alignment **out) {
+  if (!ctx || !out || (count && !paths)) return HD_ERR_ARG;
+  for (uint64_t i = 0; i < count; ++i) out[i] = nullptr;
+  int rc = guard(ctx, [&] {
+    run_on_workers(ctx, count, 12, [&](hd_ctx *w, uint64_t i) {
+      const char *data = nullptr;
+      uint64_t size = 0;
+      int r = read_file_pinned(w, paths[i], &data, &size);
+      if (r != HD_OK) return r;
+      return hd_alignment_from_fasta(w, data, size, 0, remove_duplicates, n_limit, include_x,
+                                     semantics, &out[i]);
+    });
+  });
+  if (rc != HD_OK)
+    for (uint64_t i = 0; i < count; ++i) {
+      hd_alignment_free(out[i]);
+      out[i] = nullptr;
+    }
+  return rc;
 }
 
 }  // extern "C"

@@ -99,6 +99,9 @@ struct hd_ctx {
   std::vector<std::pair<uint32_t, std::pair<int, int>>> tune;
   // child contexts (own streams) for concurrent ingest of many inputs
   std::vector<hd_ctx *> workers;
+  // pinned staging for file reads by this context (grows)
+  void *pin = nullptr;
+  size_t pin_cap = 0;
 };
 
 struct hd_alignment {

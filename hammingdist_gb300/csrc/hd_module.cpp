@@ -295,38 +295,17 @@ py::list from_fasta_batch(const std::vector<std::string> &files, bool include_x,
   }
   std::lock_guard<std::mutex> lk(g_mu);
   hd_ctx *c = ctx();
-  // all files into one pinned buffer, read in parallel
-  std::vector<uint64_t> sizes(k), offs(k + 1, 0);
-  for (size_t i = 0; i < k; ++i) {
-    struct stat sb;
-    if (::stat(files[i].c_str(), &sb) != 0 || !S_ISREG(sb.st_mode)) open_failed(files[i]);
-    sizes[i] = (uint64_t)sb.st_size;
-    offs[i + 1] = offs[i] + sizes[i] + 16;
-  }
-  char *buf = pinned(offs[k] + 1);
-  std::vector<const char *> ptrs(k);
-  for (size_t i = 0; i < k; ++i) ptrs[i] = buf + offs[i];
-  {
-    py::gil_scoped_release nogil;
-    std::atomic<size_t> next{0};
-    std::atomic<long> bad{-1};
-    std::vector<std::thread> th;
-    const unsigned nt = std::min<unsigned>(16, (unsigned)std::max<size_t>(k, 1));
-    for (unsigned t = 0; t < nt; ++t)
-      th.emplace_back([&] {
-        for (size_t i = next++; i < k; i = next++)
-          if (!read_into(files[i], buf + offs[i], sizes[i])) bad = (long)i;
-      });
-    for (auto &x : th) x.join();
-    if (bad.load() >= 0) open_failed(files[bad.load()]);
-  }
+  std::vector<const char *> paths(k);
+  for (size_t i = 0; i < k; ++i) paths[i] = files[i].c_str();
   std::vector<hd_alignment *> alns(k, nullptr);
   std::vector<DataSet<uint8_t>> small(k);
   std::vector<DataSet<uint16_t>> wide(k);
   {
     py::gil_scoped_release nogil;
-    check(hd_alignments_from_fasta_many(c, k, ptrs.data(), sizes.data(), remove_duplicates, n,
-                                        include_x, use_gpu ? HD_SEM_GPU : HD_SEM_CPU, alns.data()));
+    auto t1 = std::chrono::steady_clock::now();
+    check(hd_alignments_from_fasta_files(c, k, paths.data(), remove_duplicates, n, include_x,
+                                         use_gpu ? HD_SEM_GPU : HD_SEM_CPU, alns.data()));
+    const double t_ingest = ms_since(t1);
     std::vector<Aln> own(k);
     for (size_t i = 0; i < k; ++i) own[i].p = alns[i];
     hd_batch *b = nullptr;
@@ -351,7 +330,16 @@ py::list from_fasta_batch(const std::vector<std::string> &files, bool include_x,
         check(hd_alignment_sequence_indices(alns[i], idx.data()));
       }
     }
+    auto t2 = std::chrono::steady_clock::now();
     check(hd_batch_run(b));
+    double graph_ms = 0;
+    uint64_t launches = 0, tiles = 0;
+    hd_batch_timing(b, &graph_ms, &launches, &tiles);
+    say("batch of " + std::to_string(k) + " alignments: read + ingest " +
+        std::to_string(t_ingest) + " ms, distances " +
+        std::to_string(ms_since(t2)) + " ms (" + std::to_string(launches) +
+        " persistent launches, " + std::to_string(tiles) + " tiles, device " +
+        std::to_string(graph_ms) + " ms).");
   }
   py::list out;
   for (size_t i = 0; i < k; ++i) {

@@ -224,6 +224,16 @@ int hd_alignments_from_fasta_many(hd_ctx *ctx, uint64_t count,
                                   int include_x, int semantics,
                                   hd_alignment **out);
 
+/* Same from FASTA files: worker contexts each read the next file into their
+ * own pinned buffer and ingest it at once, so reading one file overlaps the
+ * device ingest of others. An unreadable file fails with HD_ERR_IO
+ * ("Error: Failed to open file '<f>'"). */
+int hd_alignments_from_fasta_files(hd_ctx *ctx, uint64_t count,
+                                   const char *const *paths,
+                                   int remove_duplicates, uint64_t n_limit,
+                                   int include_x, int semantics,
+                                   hd_alignment **out);
+
 /* ---- autotuning ------------------------------------------------------------ */
 /* Times every kernel configuration (tile edge 64/128 = 4/8 rows per thread,
  * TMA staging depth 2-4) for each (n bucket <= max_n_bucket, L bucket,
