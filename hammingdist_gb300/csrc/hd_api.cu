@@ -787,29 +787,11 @@ void run_on_workers(hd_ctx *ctx, uint64_t count, size_t max_workers, Job &&job) 
   if (first_rc.load() != HD_OK) fail(first_rc.load(), first_msg);
 }
 
-// Reads `path` into the context's pinned buffer (grown as needed).
-int read_file_pinned(hd_ctx *w, const char *path, const char **data, uint64_t *size) {
+// Reads `path` (n bytes) into dst.
+int read_file_into(hd_ctx *w, const char *path, char *dst, uint64_t n) {
   return guard(w, [&] {
     int fd = ::open(path, O_RDONLY);
-    struct stat sb;
-    if (fd < 0 || fstat(fd, &sb) != 0 || !S_ISREG(sb.st_mode)) {
-      if (fd >= 0) ::close(fd);
-      fail(HD_ERR_IO, std::string("Error: Failed to open file '") + path + "'");
-    }
-    const uint64_t n = (uint64_t)sb.st_size;
-    if (n + 1 > w->pin_cap) {
-      if (w->pin) cudaFreeHost(w->pin);
-      w->pin = nullptr;
-      w->pin_cap = 0;
-      const size_t cap = (size_t)((n + 1) * 3 / 2 + (1 << 20));
-      cudaError_t e = cudaHostAlloc(&w->pin, cap, cudaHostAllocDefault);
-      if (e != cudaSuccess) {
-        ::close(fd);
-        HD_CUDA(e);
-      }
-      w->pin_cap = cap;
-    }
-    char *dst = static_cast<char *>(w->pin);
+    if (fd < 0) fail(HD_ERR_IO, std::string("Error: Failed to open file '") + path + "'");
     uint64_t off = 0;
     while (off < n) {
       ssize_t r = ::pread(fd, dst + off, (size_t)std::min<uint64_t>(n - off, 1ull << 30), (off_t)off);
@@ -820,8 +802,6 @@ int read_file_pinned(hd_ctx *w, const char *path, const char **data, uint64_t *s
       off += (uint64_t)r;
     }
     ::close(fd);
-    *data = dst;
-    *size = n;
   });
 }
 
@@ -855,13 +835,29 @@ int hd_alignments_from_fasta_files(hd_ctx *ctx, uint64_t count, const char *cons
   if (!ctx || !out || (count && !paths)) return HD_ERR_ARG;
   for (uint64_t i = 0; i < count; ++i) out[i] = nullptr;
   int rc = guard(ctx, [&] {
+    // every file gets a slice of one pinned arena (grown once, then reused)
+    std::vector<uint64_t> size(count), off(count + 1, 0);
+    for (uint64_t i = 0; i < count; ++i) {
+      struct stat sb;
+      if (::stat(paths[i], &sb) != 0 || !S_ISREG(sb.st_mode))
+        fail(HD_ERR_IO, std::string("Error: Failed to open file '") + paths[i] + "'");
+      size[i] = (uint64_t)sb.st_size;
+      off[i + 1] = off[i] + hd::round_up(size[i] + 1, 256);
+    }
+    if (off[count] > ctx->pin_cap) {
+      if (ctx->pin) cudaFreeHost(ctx->pin);
+      ctx->pin = nullptr;
+      ctx->pin_cap = 0;
+      const size_t cap = (size_t)(off[count] * 5 / 4 + (1 << 20));
+      HD_CUDA(cudaHostAlloc(&ctx->pin, cap, cudaHostAllocDefault));
+      ctx->pin_cap = cap;
+    }
+    char *arena = static_cast<char *>(ctx->pin);
     run_on_workers(ctx, count, 12, [&](hd_ctx *w, uint64_t i) {
-      const char *data = nullptr;
-      uint64_t size = 0;
-      int r = read_file_pinned(w, paths[i], &data, &size);
+      int r = read_file_into(w, paths[i], arena + off[i], size[i]);
       if (r != HD_OK) return r;
-      return hd_alignment_from_fasta(w, data, size, 0, remove_duplicates, n_limit, include_x,
-                                     semantics, &out[i]);
+      return hd_alignment_from_fasta(w, arena + off[i], size[i], 0, remove_duplicates, n_limit,
+                                     include_x, semantics, &out[i]);
     });
   });
   if (rc != HD_OK)

@@ -203,20 +203,28 @@ extern "C" int hd_tune_load(hd_ctx *ctx, const char *path) {
     ss << f.rdbuf();
     const std::string s = ss.str();
     std::vector<std::pair<uint32_t, std::pair<int, int>>> table;
-    size_t pos = 0;
-    auto field = [&](const char *name, size_t from, int &v) {
-      size_t p = s.find(std::string("\"") + name + "\":", from);
-      if (p == std::string::npos) return false;
-      v = std::atoi(s.c_str() + p + std::strlen(name) + 3);
+    // one entry per object holding "n_bucket"; whitespace between tokens is free
+    auto field = [&](const char *name, size_t from, size_t to, int &v) {
+      const std::string key = std::string("\"") + name + "\"";
+      size_t p = s.find(key, from);
+      if (p == std::string::npos || p >= to) return false;
+      p = s.find(':', p + key.size());
+      if (p == std::string::npos || p >= to) return false;
+      v = std::atoi(s.c_str() + p + 1);
       return true;
     };
-    while ((pos = s.find("{\"n_bucket\"", pos)) != std::string::npos) {
+    size_t pos = 0;
+    while ((pos = s.find("\"n_bucket\"", pos)) != std::string::npos) {
+      const size_t begin = s.rfind('{', pos);
+      const size_t end = s.find('}', pos);
       int nb, lb, dt, tile, st;
-      if (!field("n_bucket", pos, nb) || !field("L_bucket", pos, lb) || !field("dtype", pos, dt) ||
-          !field("tile", pos, tile) || !field("stages", pos, st) || !hd::tile_config_valid(tile, st))
+      if (begin == std::string::npos || end == std::string::npos || !field("n_bucket", begin, end, nb) ||
+          !field("L_bucket", begin, end, lb) || !field("dtype", begin, end, dt) ||
+          !field("tile", begin, end, tile) || !field("stages", begin, end, st) ||
+          !hd::tile_config_valid(tile, st))
         hd::fail(HD_ERR_ARG, std::string("malformed tuning file '") + path + "'");
       table.push_back({hd::key_of(nb, lb, dt), {tile, st}});
-      ++pos;
+      pos = end;
     }
     ctx->tune = table;
   });
