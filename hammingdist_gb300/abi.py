@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -98,6 +99,7 @@ def _ptr(x):
 class Alignment:
     def __init__(self, ctx: "Context", handle):
         self.ctx, self.h = ctx, handle
+        ctx._owned.add(self)
         n_rows, length, n_in, rule = u64(), u64(), u64(), ci()
         ctx._check(lib().hd_alignment_info(handle, ctypes.byref(n_rows), ctypes.byref(length),
                                            ctypes.byref(n_in), ctypes.byref(rule)))
@@ -128,9 +130,12 @@ class Context:
         if rc != 0:
             raise HDError(rc, f"hd_ctx_create failed ({rc})")
         self.h = h
+        self._owned = weakref.WeakSet()  # alignments and batches made here
 
     def close(self):
         if self.h:
+            for obj in list(self._owned):  # batches reference the context's streams
+                obj.free()
             lib().hd_ctx_destroy(self.h)
             self.h = None
 
@@ -301,6 +306,7 @@ class Batch:
         ctx._check(lib().hd_batch_create(ctx.h, ctypes.byref(h)))
         self.h = h
         self.outputs = []
+        ctx._owned.add(self)
 
     def add(self, aln: Alignment, dtype=np.uint8, max_distance=255, out=None, out_on_device=False):
         dt = np.dtype(dtype)

@@ -96,6 +96,7 @@ hd_alignment *build_alignment(hd_ctx *ctx, hd::Records &rec, int remove_duplicat
   auto *aln = new hd_alignment();
   try {
     aln->ctx = ctx;
+    aln->device = ctx->device;
     aln->n_input = rec.n;
     aln->length = rec.len0;
     aln->words = words_for(rec.len0);
@@ -391,11 +392,7 @@ int hd_alignment_sequence_indices(const hd_alignment *aln, uint64_t *out) {
   return HD_OK;
 }
 
-void hd_alignment_free(hd_alignment *aln) {
-  if (!aln) return;
-  if (aln->ctx) cudaSetDevice(aln->ctx->device);
-  delete aln;
-}
+void hd_alignment_free(hd_alignment *aln) { delete aln; }
 
 int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, int64_t max_distance,
                    void *out, int out_on_device) {

@@ -685,6 +685,7 @@ void alignment_query_distances(hd_ctx *ctx, const hd_alignment *aln, const uint8
                                uint32_t *d_out_rows) {
   // pack the query with the same codes as the alignment (one row)
   hd_alignment q;
+  q.device = ctx->device;
   q.n_rows = 1;
   q.length = aln->length;
   q.words = aln->words;

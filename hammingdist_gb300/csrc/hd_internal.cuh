@@ -105,7 +105,8 @@ struct hd_ctx {
 };
 
 struct hd_alignment {
-  hd_ctx *ctx = nullptr;
+  hd_ctx *ctx = nullptr;  // creating context; may be destroyed before the alignment
+  int device = 0;
   uint64_t n_input = 0;   // records read
   uint64_t n_rows = 0;    // rows after dedupe
   uint64_t length = 0;    // sites per row
@@ -116,6 +117,16 @@ struct hd_alignment {
   hd::DevBuf plane_buf[2];
   std::vector<uint64_t> seqidx;  // host, n_input entries (empty = identity)
   hd::DevBuf d_seqidx;           // device copy (serving / reference queries)
+  // Freed on the null stream: every API call has synchronised its own stream
+  // before returning, so no queued work still reads these buffers, and the
+  // creating context (and its streams) may already be gone.
+  ~hd_alignment() {
+    cudaSetDevice(device);
+    for (auto *b : {&plane_buf[0], &plane_buf[1], &d_seqidx}) {
+      b->s = nullptr;
+      b->release();
+    }
+  }
 };
 
 namespace hd {

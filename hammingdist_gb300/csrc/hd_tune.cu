@@ -133,6 +133,7 @@ extern "C" int hd_autotune(hd_ctx *ctx, uint64_t max_n_bucket) {
       for (int lb = 0; lb < 4; ++lb) {
         hd_alignment a;
         a.ctx = ctx;
+        a.device = ctx->device;
         a.n_rows = hd::kNRep[nb];
         a.length = hd::kLRep[lb];
         a.words = hd::round_up(hd::ceil_div(a.length, 32), 8);
