@@ -77,7 +77,7 @@ static double time_kernel(hd_ctx *ctx, void (*kern)(uint32_t, uint32_t *), uint3
 void measure_int_peaks(hd_ctx *ctx, double *lop3, double *popc, double *mix) {
   DevBuf sink(64, ctx->stream);
   const unsigned blocks = (unsigned)ctx->sm_count * 8;  // 64 warps per SM
-  const uint32_t iters = 32;  // ~70 ms per kernel at 64 LOP3 lanes/clk/SM
+  const uint32_t iters = 256;  // ~0.5 ms per kernel at 64 LOP3 lanes/clk/SM
   const double ops = (double)blocks * kPeakThreads * iters * kPeakUnroll * 8;
   double t1 = time_kernel(ctx, k_peak_lop3, iters, sink.as<uint32_t>(), blocks);
   double t2 = time_kernel(ctx, k_peak_popc, iters / 4, sink.as<uint32_t>(), blocks);
