@@ -51,6 +51,20 @@ SIGNATURES = {
     "hd_batch_free": (None, [vp]),
     "hd_alignments_from_fasta_many": (ci, [vp, u64, P(vp), P(u64), ci, u64, ci, ci, P(vp)]),
     "hd_alignments_from_fasta_files": (ci, [vp, u64, P(cp), ci, u64, ci, ci, P(vp)]),
+    "hd_alignment_view": (ci, [vp, u64, u64, P(vp)]),
+    "hd_synthetic_fasta": (ci, [vp, u64, u64, ctypes.c_double, u64, ctypes.c_uint32,
+                                ctypes.c_double, vp, u64, P(u64)]),
+    "hd_server_create": (ci, [vp, u64, ci, P(vp)]),
+    "hd_server_add_alignment": (ci, [vp, vp, P(ctypes.c_uint32)]),
+    "hd_server_submit_reference": (ci, [vp, ctypes.c_uint32, vp, u64, P(u64)]),
+    "hd_server_submit_pairwise": (ci, [vp, ctypes.c_uint32, u64, u64, ci, i64, P(u64)]),
+    "hd_server_submit_sparse": (ci, [vp, ctypes.c_uint32, u64, u64, i64, P(u64)]),
+    "hd_server_wait": (ci, [vp, u64, ctypes.c_double]),
+    "hd_server_result": (ci, [vp, u64, P(vp), P(u64), P(u64), P(ctypes.c_double),
+                              P(ctypes.c_double)]),
+    "hd_server_release": (ci, [vp, u64]),
+    "hd_server_stats": (ci, [vp, P(u64), P(u64), P(u64), P(u64)]),
+    "hd_server_free": (None, [vp]),
     "hd_autotune": (ci, [vp, u64]),
     "hd_tune_lookup": (ci, [vp, u64, u64, ci, P(ci), P(ci)]),
     "hd_tune_save": (ci, [vp, cp]),
@@ -106,6 +120,14 @@ class Alignment:
         self.n_rows, self.length, self.n_input = n_rows.value, length.value, n_in.value
         self.rule = RULES[rule.value]
 
+    def view(self, row0: int, n_rows: int) -> "Alignment":
+        """Rows [row0, row0 + n_rows) (borrows this alignment's memory)."""
+        v = vp()
+        self.ctx._check(lib().hd_alignment_view(self.h, row0, n_rows, ctypes.byref(v)))
+        out = Alignment(self.ctx, v)
+        out._base = self  # keep the base alive while the view is
+        return out
+
     def sequence_indices(self) -> np.ndarray:
         out = np.zeros(max(self.n_input, 1), dtype=np.uint64)
         self.ctx._check(lib().hd_alignment_sequence_indices(self.h, out.ctypes.data))
@@ -134,7 +156,11 @@ class Context:
 
     def close(self):
         if self.h:
-            for obj in list(self._owned):  # batches reference the context's streams
+            # servers use resident alignments in flight; views borrow their bases
+            def order(o):
+                return (0 if isinstance(o, Server) else 1 if isinstance(o, Batch) else
+                        2 if getattr(o, "_base", None) is not None else 3)
+            for obj in sorted(list(self._owned), key=order):
                 obj.free()
             lib().hd_ctx_destroy(self.h)
             self.h = None
@@ -266,6 +292,19 @@ class Context:
                                                          int(include_x), semantics, outs))
         return [Alignment(self, vp(outs[i])) for i in range(k)]
 
+    def synthetic_fasta(self, n, L, p=1e-3, seed=0, dash_max=200, n_rate=1e-4, out=None):
+        """Seeded synthetic FASTA written on the device; returns the byte count
+        (and writes into the device pointer `out` when given)."""
+        nb = u64()
+        self._check(lib().hd_synthetic_fasta(self.h, n, L, p, seed, dash_max, n_rate,
+                                             _ptr(out) if out is not None else None,
+                                             (1 << 63) if out is not None else 0,
+                                             ctypes.byref(nb)))
+        return nb.value
+
+    def server(self, output_budget_bytes=8 << 30, max_waves=3) -> "Server":
+        return Server(self, output_budget_bytes, max_waves)
+
     def batch(self) -> "Batch":
         return Batch(self)
 
@@ -335,6 +374,87 @@ class Batch:
     def free(self):
         if self.h:
             lib().hd_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request loop over resident alignments with continuous batching
+    (hd_server_*). Results: uint32 array (reference), dtype array
+    (pairwise), bytes (sparse text)."""
+
+    KINDS = {}
+
+    def __init__(self, ctx: Context, budget: int, max_waves: int):
+        self.ctx = ctx
+        h = vp()
+        ctx._check(lib().hd_server_create(ctx.h, budget, max_waves, ctypes.byref(h)))
+        self.h = h
+        self._kind = {}
+        self._keep = []
+        ctx._owned.add(self)
+
+    def add(self, aln: Alignment) -> int:
+        i = ctypes.c_uint32()
+        self.ctx._check(lib().hd_server_add_alignment(self.h, aln.h, ctypes.byref(i)))
+        self._keep.append(aln)
+        return i.value
+
+    def reference(self, aln_id: int, query) -> int:
+        q = query.encode() if isinstance(query, str) else bytes(query)
+        t = u64()
+        self.ctx._check(lib().hd_server_submit_reference(self.h, aln_id, _ptr(q), len(q),
+                                                         ctypes.byref(t)))
+        self._kind[t.value] = ("ref", np.uint32)
+        return t.value
+
+    def pairwise(self, aln_id: int, row0: int, n_rows: int, dtype=np.uint8, max_distance=255):
+        t = u64()
+        dt = np.dtype(dtype)
+        self.ctx._check(lib().hd_server_submit_pairwise(self.h, aln_id, row0, n_rows, dt.itemsize,
+                                                        int(max_distance), ctypes.byref(t)))
+        self._kind[t.value] = ("pair", dt)
+        return t.value
+
+    def sparse(self, aln_id: int, row0: int, n_rows: int, threshold: int) -> int:
+        t = u64()
+        self.ctx._check(lib().hd_server_submit_sparse(self.h, aln_id, row0, n_rows, threshold,
+                                                      ctypes.byref(t)))
+        self._kind[t.value] = ("sparse", None)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = 60.0):
+        self.ctx._check(lib().hd_server_wait(self.h, ticket, timeout))
+
+    def result(self, ticket: int, release: bool = True):
+        """(value, count, latency_ms, queue_ms) of a finished request."""
+        data, nb, cnt = vp(), u64(), u64()
+        lat, q = ctypes.c_double(), ctypes.c_double()
+        self.ctx._check(lib().hd_server_result(self.h, ticket, ctypes.byref(data), ctypes.byref(nb),
+                                               ctypes.byref(cnt), ctypes.byref(lat),
+                                               ctypes.byref(q)))
+        raw = ctypes.string_at(data.value, nb.value) if nb.value else b""
+        kind, dt = self._kind.pop(ticket)
+        value = raw if kind == "sparse" else np.frombuffer(raw, dtype=dt).copy()
+        if release:
+            lib().hd_server_release(self.h, ticket)
+        return value, cnt.value, lat.value, q.value
+
+    def stats(self):
+        w, c, m, b = u64(), u64(), u64(), u64()
+        self.ctx._check(lib().hd_server_stats(self.h, ctypes.byref(w), ctypes.byref(c),
+                                              ctypes.byref(m), ctypes.byref(b)))
+        return {"waves": w.value, "completed": c.value, "max_inflight": m.value,
+                "bytes_in_use": b.value}
+
+    def free(self):
+        if self.h:
+            lib().hd_server_free(self.h)
             self.h = None
 
     def __del__(self):

@@ -22,7 +22,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 CU_SOURCES = ["hd_ingest.cu", "hd_pairwise.cu", "hd_format.cu", "hd_peak.cu", "hd_tune.cu",
-              "hd_api.cu"]
+              "hd_synth.cu", "hd_server.cu", "hd_api.cu"]
 GENCODE = "arch=compute_103a,code=sm_103a"
 LIBHD = os.path.join(PKG, "libhd.so")
 EXT = os.path.join(PKG, "_C" + sysconfig.get_config_var("EXT_SUFFIX"))

@@ -681,28 +681,28 @@ __global__ void k_query(const uint4 *g0, uint64_t words, uint64_t n_rows, const 
   }
 }
 
+void query_distances_async(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
+                           uint32_t *d_out_rows, DevBuf &q_planes) {
+  // pack the query with the alignment's AND codes (one row), then one warp per row
+  Table256 t;
+  code_table(kCodesAnd, t.v);
+  q_planes = DevBuf(aln->words * 16, ctx->stream);
+  DevBuf rs(8, ctx->stream);  // record start 0, freed after the kernels in stream order
+  HD_CUDA(cudaMemsetAsync(rs.p, 0, 8, ctx->stream));
+  k_pack<4><<<grid_for(((aln->words + 31) / 32) * 32, 256), 256, 0, ctx->stream>>>(
+      d_query, rs.as<uint64_t>(), nullptr, 1, aln->length, aln->words, t, q_planes.as<uint4>(),
+      nullptr);
+  HD_LAUNCHED(ctx);
+  k_query<<<grid_for(aln->n_rows * 32, 256), 256, 0, ctx->stream>>>(
+      static_cast<const uint4 *>(aln->planes_ptr(0)), aln->words, aln->n_rows,
+      q_planes.as<uint4>(), d_out_rows);
+  HD_LAUNCHED(ctx);
+}
+
 void alignment_query_distances(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
                                uint32_t *d_out_rows) {
-  // pack the query with the same codes as the alignment (one row)
-  hd_alignment q;
-  q.device = ctx->device;
-  q.n_rows = 1;
-  q.length = aln->length;
-  q.words = aln->words;
-  q.rule = HD_RULE_AND;
-  q.groups = 1;
-  q.planes = 4;
-  Records r1;
-  r1.n = 1;
-  r1.base = d_query;
-  r1.len0 = aln->length;
-  r1.rec_start = DevBuf(8, ctx->stream);
-  HD_CUDA(cudaMemsetAsync(r1.rec_start.p, 0, 8, ctx->stream));
-  pack_rows(ctx, r1, nullptr, &q);
-  k_query<<<grid_for(aln->n_rows * 32, 256), 256, 0, ctx->stream>>>(
-      aln->plane_buf[0].as<uint4>(), aln->words, aln->n_rows, q.plane_buf[0].as<uint4>(),
-      d_out_rows);
-  HD_LAUNCHED(ctx);
+  DevBuf q;
+  query_distances_async(ctx, aln, d_query, d_out_rows, q);
   HD_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 

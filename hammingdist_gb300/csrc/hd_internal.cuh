@@ -107,6 +107,9 @@ struct hd_ctx {
 struct hd_alignment {
   hd_ctx *ctx = nullptr;  // creating context; may be destroyed before the alignment
   int device = 0;
+  // a view (hd_alignment_view) borrows rows [row0, row0 + n_rows) of `base`
+  const hd_alignment *base = nullptr;
+  uint64_t row0 = 0;
   uint64_t n_input = 0;   // records read
   uint64_t n_rows = 0;    // rows after dedupe
   uint64_t length = 0;    // sites per row
@@ -120,6 +123,11 @@ struct hd_alignment {
   // Freed on the null stream: every API call has synchronised its own stream
   // before returning, so no queued work still reads these buffers, and the
   // creating context (and its streams) may already be gone.
+  // device address of plane group g of this alignment (or view)
+  const void *planes_ptr(int g) const {
+    const hd_alignment *o = base ? base : this;
+    return static_cast<const uint8_t *>(o->plane_buf[g].p) + row0 * words * 16;
+  }
   ~hd_alignment() {
     cudaSetDevice(device);
     for (auto *b : {&plane_buf[0], &plane_buf[1], &d_seqidx}) {
@@ -323,6 +331,9 @@ void reference_distances_device(hd_ctx *ctx, const Records &rec, const uint8_t *
                                 int include_x, uint32_t *d_out);
 void alignment_query_distances(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
                                uint32_t *d_out_rows);
+// same without synchronising: q_planes holds the packed query until the caller syncs
+void query_distances_async(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
+                           uint32_t *d_out_rows, DevBuf &q_planes);
 
 // pairwise.cu: tiles of rows [tile_lo*128, tile_hi*128) x all earlier columns
 // into out (lt index out_base maps to out[0]).

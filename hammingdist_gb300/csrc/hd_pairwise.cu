@@ -396,8 +396,8 @@ void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStr
     for (size_t q = 0; q < nj; ++q) {
       const PairJobSpec &s = specs[grp.idx[q]];
       const hd_alignment *a = s.aln;
-      make_tmap(ctx, &tms[2 * q], a->plane_buf[0].p, a->words, a->n_rows, v.tile);
-      if (a->groups == 2) make_tmap(ctx, &tms[2 * q + 1], a->plane_buf[1].p, a->words, a->n_rows, v.tile);
+      make_tmap(ctx, &tms[2 * q], a->planes_ptr(0), a->words, a->n_rows, v.tile);
+      if (a->groups == 2) make_tmap(ctx, &tms[2 * q + 1], a->planes_ptr(1), a->words, a->n_rows, v.tile);
       else tms[2 * q + 1] = tms[2 * q];
       PairJob &j = pj[q];
       j.tmap0 = d_tms + 2 * q;

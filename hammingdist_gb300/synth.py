@@ -87,3 +87,37 @@ def random_strings(n: int, L: int, chars: bytes, seed: int) -> list[bytes]:
     pool = np.frombuffer(chars, dtype=np.uint8)
     m = pool[rng.integers(0, len(pool), size=(n, L))]
     return [m[i].tobytes() for i in range(n)]
+
+
+# ---------------------------------------------------------------------------
+# Host mirror of the device generator (hd_synthetic_fasta, csrc/hd_synth.cu):
+# every byte is a function of (seed, record, site), so a host caller can
+# rebuild a root or a record of a resident set generated on the device.
+_M = (1 << 64) - 1
+
+
+def _mix(x):
+    x = np.asarray(x, dtype=np.uint64)
+    x = x ^ (x >> np.uint64(30))
+    x = x * np.uint64(0xBF58476D1CE4E5B9)
+    x = x ^ (x >> np.uint64(27))
+    x = x * np.uint64(0x94D049BB133111EB)
+    return x ^ (x >> np.uint64(31))
+
+
+def _hash(seed, a, b):
+    with np.errstate(over="ignore"):
+        a = np.asarray(a, dtype=np.uint64)
+        b = np.asarray(b, dtype=np.uint64)
+        return _mix(np.uint64(seed & _M) + a * np.uint64(0x9E3779B97F4A7C15)
+                    + b * np.uint64(0xD1B54A32D192ED03))
+
+
+def device_root(seed: int, L: int) -> np.ndarray:
+    """Root sequence of hd_synthetic_fasta(seed, ..., L)."""
+    s = np.arange(L, dtype=np.uint64)
+    return _ACGT[(_hash(seed, 0xFFFFFFFF, s) & np.uint64(3)).astype(np.intp)]
+
+
+def device_fasta_bytes(n: int, L: int) -> int:
+    return n * (L + 13)

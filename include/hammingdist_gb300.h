@@ -234,6 +234,61 @@ int hd_alignments_from_fasta_files(hd_ctx *ctx, uint64_t count,
                                    int include_x, int semantics,
                                    hd_alignment **out);
 
+/* A view of rows [row0, row0 + n_rows) of an alignment, usable wherever an
+ * alignment is (pairwise, batches, serving). It borrows the base's device
+ * memory: free the view before the base. No reference counterpart. */
+int hd_alignment_view(const hd_alignment *base, uint64_t row0, uint64_t n_rows,
+                      hd_alignment **out);
+
+/* ---- synthetic input (benchmarks and tests) -------------------------------- */
+/* Writes n seeded synthetic FASTA records of L sites into device memory
+ * (d_out, capacity bytes; d_out = NULL only reports *nbytes): a root uniform
+ * over ACGT, substitution probability p, N runs (about n_rate per site, 1-50
+ * long), '-' runs of 0..dash_max at both ends; records ">s%09d\n" + sites +
+ * "\n". Every byte is a function of (seed, record, site). No reference
+ * counterpart. */
+int hd_synthetic_fasta(hd_ctx *ctx, uint64_t n, uint64_t L, double p,
+                       uint64_t seed, uint32_t dash_max, double n_rate,
+                       void *d_out, uint64_t capacity, uint64_t *nbytes);
+
+/* ---- serving --------------------------------------------------------------- */
+/* A request loop over resident alignments with continuous batching. No
+ * reference counterpart. Requests are admitted in arrival order while the
+ * device output bytes they need fit in output_budget_bytes (a request larger
+ * than the budget runs alone); every admitted request is folded into one
+ * wave (one persistent pairwise kernel over all matrices' tiles, plus the
+ * query kernels) launched on a free worker stream, with up to max_waves
+ * waves on the device at once. Results stay in the server until released.
+ *  - reference: distances of `query` (length = the alignment's length) to
+ *    every input record, uint32 (the fasta_reference_distances rule);
+ *  - pairwise: lower triangle of rows [row0, row0 + n_rows), dtype 1 or 2;
+ *  - sparse: "i j d\n" text (window-relative i > j, d <= threshold < 255)
+ *    in ascending rows, as DataSet::dump_sparse writes it. */
+typedef struct hd_server hd_server;
+int hd_server_create(hd_ctx *ctx, uint64_t output_budget_bytes, int max_waves,
+                     hd_server **out);
+int hd_server_add_alignment(hd_server *s, const hd_alignment *aln, uint32_t *id);
+int hd_server_submit_reference(hd_server *s, uint32_t aln_id, const char *query,
+                               uint64_t len, uint64_t *ticket);
+int hd_server_submit_pairwise(hd_server *s, uint32_t aln_id, uint64_t row0,
+                              uint64_t n_rows, int dtype_bytes,
+                              int64_t max_distance, uint64_t *ticket);
+int hd_server_submit_sparse(hd_server *s, uint32_t aln_id, uint64_t row0,
+                            uint64_t n_rows, int64_t threshold,
+                            uint64_t *ticket);
+/* Waits up to timeout_s for the request; returns its status. */
+int hd_server_wait(hd_server *s, uint64_t ticket, double timeout_s);
+/* Result of a finished request: bytes, element/line count, latency from
+ * submission to completion and the part of it spent waiting for admission. */
+int hd_server_result(hd_server *s, uint64_t ticket, const void **data,
+                     uint64_t *bytes, uint64_t *count, double *latency_ms,
+                     double *queue_ms);
+int hd_server_release(hd_server *s, uint64_t ticket);
+int hd_server_stats(hd_server *s, uint64_t *waves, uint64_t *completed,
+                    uint64_t *max_inflight, uint64_t *bytes_in_use);
+/* Stops admitting, fails queued requests, drains the waves on the device. */
+void hd_server_free(hd_server *s);
+
 /* ---- autotuning ------------------------------------------------------------ */
 /* Times every kernel configuration (tile edge 64/128 = 4/8 rows per thread,
  * TMA staging depth 2-4) for each (n bucket <= max_n_bucket, L bucket,
