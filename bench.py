@@ -491,6 +491,139 @@ def run_batched(args):
             "tuning": args.tuning or "built-in"}), flush=True)
 
 
+def run_serve(args):
+    """Serving: 8 alignments resident in HBM (n = 200k, 100k, 50k, 50k, 20k,
+    20k, 10k, 10k at --serve-scale 1; L=29,903; generated on the device), a
+    Poisson request stream (--serve-rate per s for --serve-seconds): 60%
+    reference-distance queries (a new seeded query against a resident set),
+    30% pairwise matrices of a window of n rows (n log-uniform 100-10,000,
+    uint8/uint16), 10% sparse dumps of such a window (threshold 1-5).
+    Reports p50/p99 latency at that load, the throughput of the same requests
+    submitted at once (server saturated) and of serial plain calls."""
+    import threading as th
+
+    import torch
+
+    from hammingdist_gb300 import abi, synth
+
+    ctx = abi.Context(0)
+    L_ = 29903
+    sizes = [int(x * args.serve_scale) for x in (200000, 100000, 50000, 50000, 20000, 20000,
+                                                  10000, 10000)]
+    alns, t0 = [], time.perf_counter()
+    for k, n in enumerate(sizes):
+        nb = ctx.synthetic_fasta(n, L_, p=1e-3, seed=900 + k)
+        buf = torch.empty(nb, dtype=torch.uint8, device="cuda:0")
+        torch.cuda.synchronize()
+        ctx.synthetic_fasta(n, L_, p=1e-3, seed=900 + k, out=buf.data_ptr())
+        alns.append(ctx.alignment_from_fasta(buf.data_ptr(), nb, on_device=True))
+        del buf
+    torch.cuda.empty_cache()
+    load_s = time.perf_counter() - t0
+    roots = [synth.device_root(900 + k, L_) for k in range(len(sizes))]
+
+    rng = np.random.default_rng(31337)
+    n_req = int(args.serve_rate * args.serve_seconds)
+    gaps = rng.exponential(1.0 / args.serve_rate, n_req)
+    arrivals = np.cumsum(gaps)
+    reqs = []
+    for _ in range(n_req):
+        u = rng.random()
+        a = int(rng.integers(0, len(sizes)))
+        if u < 0.6:
+            q = roots[a].copy()
+            m = rng.random(L_) < 1e-3
+            q[m] = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, int(m.sum()))]
+            reqs.append(("ref", a, q.tobytes()))
+        else:
+            n = int(round(np.exp(rng.uniform(np.log(100), np.log(10000)))))
+            cand = [i for i, s_ in enumerate(sizes) if s_ >= n]
+            a = int(rng.choice(cand))
+            r0 = int(rng.integers(0, sizes[a] - n + 1))
+            if u < 0.9:
+                reqs.append(("pair", a, r0, n, np.uint16 if rng.random() < 0.5 else np.uint8))
+            else:
+                reqs.append(("sparse", a, r0, n, int(rng.integers(1, 6))))
+
+    def submit(srv, ids, r):
+        if r[0] == "ref":
+            return srv.reference(ids[r[1]], r[2])
+        if r[0] == "pair":
+            return srv.pairwise(ids[r[1]], r[2], r[3], dtype=r[4], max_distance=65535)
+        return srv.sparse(ids[r[1]], r[2], r[3], r[4])
+
+    def run_stream(paced):
+        srv = ctx.server(output_budget_bytes=args.serve_budget_gb << 30, max_waves=3)
+        ids = [srv.add(a) for a in alns]
+        tickets = [None] * len(reqs)
+        start = time.perf_counter()
+
+        def producer():
+            for i, r in enumerate(reqs):
+                if paced:
+                    delay = start + arrivals[i] - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                tickets[i] = submit(srv, ids, r)
+
+        thr = th.Thread(target=producer)
+        thr.start()
+        lat, queue, kinds = [], [], []
+        for i in range(len(reqs)):
+            while tickets[i] is None:
+                time.sleep(0.0005)
+            srv.wait(tickets[i], 600)
+            _, _, l, q = srv.result(tickets[i])
+            lat.append(l)
+            queue.append(q)
+            kinds.append(reqs[i][0])
+        thr.join()
+        wall = time.perf_counter() - start
+        stats = srv.stats()
+        srv.free()
+        lat = np.array(lat)
+        per_kind = {k: {"p50_ms": float(np.percentile(lat[np.array(kinds) == k], 50)),
+                        "p99_ms": float(np.percentile(lat[np.array(kinds) == k], 99)),
+                        "count": int(np.sum(np.array(kinds) == k))}
+                    for k in ("ref", "pair", "sparse") if np.any(np.array(kinds) == k)}
+        return {"req_per_s": len(reqs) / wall, "wall_s": wall,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(lat.mean()), "queue_p99_ms": float(np.percentile(queue, 99)),
+                "per_kind": per_kind, "waves": stats["waves"],
+                "max_waves_in_flight": stats["max_inflight"]}
+
+    paced = run_stream(True)
+    saturated = run_stream(False)
+    # serial plain calls over the same requests (a bounded sample, timed)
+    n_serial = min(len(reqs), args.serve_serial)
+    t = time.perf_counter()
+    with tempfile.TemporaryDirectory() as d:
+        sp = os.path.join(d, "sparse.txt")
+        for r in reqs[:n_serial]:
+            a = alns[r[1]]
+            if r[0] == "ref":
+                ctx.alignment_reference_distances(a, r[2])
+            else:
+                v = a.view(r[2], r[3])
+                if r[0] == "pair":
+                    ctx.pairwise_lt(v, dtype=r[4], max_distance=65535)
+                else:
+                    lt = ctx.pairwise_lt(v, dtype=np.uint8, max_distance=255)
+                    ctx.write_sparse(lt, r[3], r[4], sp)
+                v.free()
+    serial = n_serial / (time.perf_counter() - t)
+    print(json.dumps({
+        "mode": "serve", "metric": "p50/p99 ms and req/s (8 resident alignments)",
+        "resident_rows": sizes, "L": L_, "requests": len(reqs), "rate_per_s": args.serve_rate,
+        "seconds": args.serve_seconds, "load_s": load_s, "paced": paced,
+        "saturated": saturated, "serial_plain_req_per_s": serial,
+        "saturated_vs_serial": saturated["req_per_s"] / serial,
+        "budget_gb": args.serve_budget_gb}), flush=True)
+    for a in alns:
+        a.free()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -508,8 +641,16 @@ def main():
                     help="batched workload: matrices/s of from_fasta_batch vs a plain loop")
     ap.add_argument("--batch-size", type=int, default=64)
     ap.add_argument("--tuning", default="", help="autotuner table (JSON) to load first")
+    ap.add_argument("--serve", action="store_true", help="serving workload (Poisson stream)")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-scale", type=float, default=1.0)
+    ap.add_argument("--serve-budget-gb", type=int, default=8)
+    ap.add_argument("--serve-serial", type=int, default=600)
     args = ap.parse_args()
-    if args.batched:
+    if args.serve:
+        run_serve(args)
+    elif args.batched:
         run_batched(args)
     elif args.kernel_only:
         run_kernel_only(args)
