@@ -44,14 +44,16 @@ struct Req {
   uint64_t id = 0;
   int kind = kRef;
   uint32_t aln = 0;
+  const hd_alignment *a = nullptr;  // resolved under the lock at submission
   uint64_t r0 = 0, n = 0;
   int dtype = 1;
   uint32_t max_dist = 255;
   int64_t thr = 0;
   std::string query;
   Clock::time_point t_submit, t_admit, t_done;
-  int status = 1;  // 1 pending, 0 done, < 0 error code
+  int status = 1;  // 1 pending, 0 done, < 0 error code; written under the lock only
   std::string err;
+  int outcome = 1;  // status computed by the completion thread, published under the lock
   std::vector<uint8_t> result;
   uint64_t count = 0;
   uint64_t out_bytes = 0;  // device bytes reserved at admission
@@ -134,7 +136,7 @@ void hd_server::launch_wave(Wave &wv) {
     if (!wv.done) HD_CUDA(cudaEventCreateWithFlags(&wv.done, cudaEventDisableTiming));
     std::vector<hd::PairJobSpec> specs;
     for (Req *r : wv.reqs) {
-      const hd_alignment *a = resident[r->aln];
+      const hd_alignment *a = r->a;
       if (r->kind == kRef) {
         r->d_query = DevBuf(r->query.size() + 16, w->stream);
         HD_CUDA(cudaMemcpyAsync(r->d_query.p, r->query.data(), r->query.size(),
@@ -195,14 +197,15 @@ void hd_server::finalize_wave(Wave &wv) {
     wv.launch_rc = HD_ERR_CUDA;
     wv.launch_err = cudaGetErrorString(ce);
   }
+  // results go to fields no waiter reads before `status` is published
   for (Req *r : wv.reqs) {
     if (wv.launch_rc != HD_OK) {
-      r->status = wv.launch_rc;
+      r->outcome = wv.launch_rc;
       r->err = wv.launch_err;
       continue;
     }
     try {
-      const hd_alignment *a = resident[r->aln];
+      const hd_alignment *a = r->a;
       if (r->kind == kRef) {
         std::vector<uint32_t> rows(a->n_rows);
         HD_CUDA(cudaMemcpy(rows.data(), r->d_out.p, a->n_rows * 4, cudaMemcpyDeviceToHost));
@@ -243,9 +246,9 @@ void hd_server::finalize_wave(Wave &wv) {
           r->count = lines;
         }
       }
-      r->status = 0;
+      r->outcome = 0;
     } catch (const hd::Error &e) {
-      r->status = e.code;
+      r->outcome = e.code;
       r->err = e.msg;
     }
   }
@@ -269,8 +272,9 @@ void hd_server::complete_loop() {
     finalize_wave(*wv);
     lk.lock();
     const auto now = Clock::now();
-    for (Req *r : wv->reqs) {
+    for (Req *r : wv->reqs) {  // publish: waiters may now read and release r
       r->t_done = now;
+      r->status = r->outcome;
       ++completed;
     }
     in_use -= wv->reserved;
@@ -361,6 +365,7 @@ int hd_server_submit_reference(hd_server *s, uint32_t aln_id, const char *query,
     auto r = std::make_unique<Req>();
     r->kind = kRef;
     r->aln = aln_id;
+    r->a = a;
     r->query.assign(query, len);
     r->out_bytes = a->n_rows * 4;
     *ticket = submit(s, std::move(r));
@@ -378,6 +383,7 @@ int hd_server_submit_pairwise(hd_server *s, uint32_t aln_id, uint64_t row0, uint
     auto r = std::make_unique<Req>();
     r->kind = kPair;
     r->aln = aln_id;
+    r->a = a;
     r->r0 = row0;
     r->n = n_rows;
     r->dtype = dtype_bytes;
@@ -397,6 +403,7 @@ int hd_server_submit_sparse(hd_server *s, uint32_t aln_id, uint64_t row0, uint64
     auto r = std::make_unique<Req>();
     r->kind = kSparse;
     r->aln = aln_id;
+    r->a = a;
     r->r0 = row0;
     r->n = n_rows;
     r->thr = threshold;
