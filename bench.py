@@ -491,6 +491,97 @@ def run_batched(args):
             "tuning": args.tuning or "built-in"}), flush=True)
 
 
+def _device_fasta_file(ctx, path, n, L_, p, seed):
+    """Seeded synthetic FASTA generated on the device, written to `path`."""
+    import torch
+
+    nb = ctx.synthetic_fasta(n, L_, p=p, seed=seed)
+    buf = torch.empty(nb, dtype=torch.uint8, device="cuda:0")
+    torch.cuda.synchronize()
+    ctx.synthetic_fasta(n, L_, p=p, seed=seed, out=buf.data_ptr())
+    host = buf.cpu().numpy()
+    del buf
+    with open(path, "wb") as f:
+        f.write(memoryview(host))
+    return nb
+
+
+def run_streaming(args):
+    """Wide distances and streamed outputs at full size (L=29,903):
+    from_fasta_large on n=50,000 (p=2e-2, uint16, max_distance=65535);
+    from_fasta_to_lower_triangular on n=100,000 (p=5e-5, max_distance=2, the
+    text streamed to disk while later rows compute); dump_sparse(threshold=3)
+    of the n=100,000 set built with max_distance=255. Checks: output sizes,
+    the first rows against the oracle, every sparse line recomputed by the
+    oracle."""
+    import hammingdist_gb300 as hd
+    from hammingdist_gb300 import abi
+    from oracle import hd_oracle as o
+
+    ctx = abi.Context(0)
+    L_ = 29903
+    res = {"mode": "streaming", "L": L_}
+    with tempfile.TemporaryDirectory(dir=args.tmpdir or None) as d:
+        f50 = os.path.join(d, "n50k.fasta")
+        f100 = os.path.join(d, "n100k.fasta")
+        _device_fasta_file(ctx, f50, args.n_wide, L_, 2e-2, 501)
+        _device_fasta_file(ctx, f100, args.n_stream, L_, 5e-5, 502)
+        head50 = open(f50, "rb").read(200 * (L_ + 13))
+        head100 = open(f100, "rb").read(200 * (L_ + 13))
+        # wide distances
+        with quiet_stdout():
+            t = time.perf_counter()
+            ds = hd.from_fasta_large(f50, use_gpu=True)
+            lt = np.asarray(ds.lt_array)
+            dt = time.perf_counter() - t
+        n = args.n_wide
+        ref = o.from_fasta_dense(head50, dtype=np.uint16, max_distance=65535)[0]
+        res["from_fasta_large"] = {
+            "n": n, "seconds": dt, "Gpair_sites_per_s": n * (n - 1) / 2 * L_ / dt / 1e9,
+            "max_distance_seen": int(lt.max()), "above_255": int(np.count_nonzero(lt > 255)),
+            "first_200_rows_bit_exact": bool(np.array_equal(lt[: ref.size], ref))}
+        del ds, lt
+        # streamed lower-triangular text
+        out = os.path.join(d, "lt.txt")
+        with quiet_stdout():
+            t = time.perf_counter()
+            hd.from_fasta_to_lower_triangular(f100, out, max_distance=2)
+            dt = time.perf_counter() - t
+        n = args.n_stream
+        size = os.path.getsize(out)
+        with open(out, "rb") as f:
+            head_text = f.read(4 * 200 * 200)
+        want = o.format_lower_triangular(o.from_fasta_dense(head100, dtype=np.uint16,
+                                                            max_distance=2)[0])
+        res["from_fasta_to_lower_triangular"] = {
+            "n": n, "seconds": dt, "Gpair_sites_per_s": n * (n - 1) / 2 * L_ / dt / 1e9,
+            "bytes_written": size, "GB_per_s_text": size / dt / 1e9,
+            "size_is_2_bytes_per_entry": size == n * (n - 1),
+            "first_200_rows_bit_exact": head_text[: len(want)] == want}
+        os.remove(out)
+        # sparse dump of the max_distance=255 set
+        sp = os.path.join(d, "sparse.txt")
+        with quiet_stdout():
+            t = time.perf_counter()
+            ds = hd.from_fasta(f100, use_gpu=True, max_distance=255)
+            t1 = time.perf_counter()
+            ds.dump_sparse(sp, 3)
+            dt = time.perf_counter() - t
+        lines = open(sp, "rb").read().splitlines()
+        recs, _ = o.read_fasta(open(f100, "rb").read())
+        ok = True
+        for ln in lines[: args.sparse_check]:
+            i, j, dd = (int(x) for x in ln.split())
+            ok &= o.lt_dense([recs[i], recs[j]], max_distance=255)[0] == dd <= 3
+        res["dump_sparse"] = {
+            "n": n, "threshold": 3, "seconds_total": dt, "seconds_matrix": t1 - t,
+            "seconds_dump": dt - (t1 - t), "lines": len(lines),
+            "lines_checked_by_oracle": min(len(lines), args.sparse_check), "lines_ok": bool(ok)}
+        del ds
+    print(json.dumps(res), flush=True)
+    ctx.close()
+
+
 def run_serve(args):
     """Serving: 8 alignments resident in HBM (n = 200k, 100k, 50k, 50k, 20k,
     20k, 10k, 10k at --serve-scale 1; L=29,903; generated on the device), a
@@ -641,6 +732,12 @@ def main():
                     help="batched workload: matrices/s of from_fasta_batch vs a plain loop")
     ap.add_argument("--batch-size", type=int, default=64)
     ap.add_argument("--tuning", default="", help="autotuner table (JSON) to load first")
+    ap.add_argument("--streaming", action="store_true",
+                    help="wide-distance and streamed-output workloads at full size")
+    ap.add_argument("--n-wide", type=int, default=50000)
+    ap.add_argument("--n-stream", type=int, default=100000)
+    ap.add_argument("--sparse-check", type=int, default=2000)
+    ap.add_argument("--tmpdir", default="")
     ap.add_argument("--serve", action="store_true", help="serving workload (Poisson stream)")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
@@ -648,7 +745,9 @@ def main():
     ap.add_argument("--serve-budget-gb", type=int, default=8)
     ap.add_argument("--serve-serial", type=int, default=600)
     args = ap.parse_args()
-    if args.serve:
+    if args.streaming:
+        run_streaming(args)
+    elif args.serve:
         run_serve(args)
     elif args.batched:
         run_batched(args)
