@@ -15,7 +15,9 @@ One step = that whole pass. Metric = unique pairs x L / step time
           left in HBM. Timed with CUDA events on the library's stream.
   e2e   : the public API a user calls (hammingdist_gb300.from_fasta(file) +
           .lt_array + fasta_reference_distances(root, file)): file -> pinned
-          host buffer -> device -> host results, every step.
+          host buffer -> device -> host results, every step. The file is read
+          once per step (its mtime changes before each step); the second call
+          finds the same unchanged file already in pinned memory.
 Inputs are larger than L2 (598 MB of FASTA text, 209 MB of packed rows), so
 no L2 flush is needed between steps.
 
@@ -308,6 +310,10 @@ def run_ours(args):
         e2e_times = []
         h2d = d2h = 0
         for k in range(args.warmup + args.steps):
+            # a new modification time: from_fasta reads the file again every
+            # step; fasta_reference_distances then reuses the bytes it read
+            stamp = time.time_ns()
+            os.utime(path, ns=(stamp, stamp))
             torch.cuda.synchronize()
             with quiet_stdout():
                 t = time.perf_counter()
@@ -318,7 +324,7 @@ def run_ours(args):
                 dt = time.perf_counter() - t
             if k >= args.warmup:
                 e2e_times.append(dt)
-            h2d = 2 * nbytes  # the FASTA goes up for each of the two calls
+            h2d = 2 * nbytes  # the FASTA goes up for each of the two calls (read once)
             d2h = lt_arr.nbytes + 8 * N + rd2.nbytes
         parity = parity and bool(np.array_equal(np.asarray(lt_arr), lt_host)) and \
             bool(np.array_equal(rd2, rd_want))
