@@ -63,6 +63,8 @@ SIGNATURES = {
     "hd_server_result": (ci, [vp, u64, P(vp), P(u64), P(u64), P(ctypes.c_double),
                               P(ctypes.c_double)]),
     "hd_server_release": (ci, [vp, u64]),
+    "hd_server_cancel": (ci, [vp, u64]),
+    "hd_selftest_wait_timeout": (ci, [vp, u64, P(ci), P(ctypes.c_double)]),
     "hd_server_stats": (ci, [vp, P(u64), P(u64), P(u64), P(u64)]),
     "hd_server_free": (None, [vp]),
     "hd_autotune": (ci, [vp, u64]),
@@ -323,6 +325,13 @@ class Context:
     def tune_load(self, path):
         self._check(lib().hd_tune_load(self.h, path.encode()))
 
+    def selftest_wait_timeout(self, limit_ns=1_000_000):
+        """(status, waited_ms) of a bounded wait that is made to run out."""
+        st, ms = ci(), ctypes.c_double()
+        self._check(lib().hd_selftest_wait_timeout(self.h, limit_ns, ctypes.byref(st),
+                                                   ctypes.byref(ms)))
+        return st.value, ms.value
+
     def measure_int_peaks(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         self._check(lib().hd_measure_int_peaks(self.h, ctypes.byref(a), ctypes.byref(b),
@@ -444,6 +453,10 @@ class Server:
         if release:
             lib().hd_server_release(self.h, ticket)
         return value, cnt.value, lat.value, q.value
+
+    def cancel(self, ticket: int):
+        self.ctx._check(lib().hd_server_cancel(self.h, ticket))
+        self._kind.pop(ticket, None)
 
     def stats(self):
         w, c, m, b = u64(), u64(), u64(), u64()

@@ -87,4 +87,45 @@ void measure_int_peaks(hd_ctx *ctx, double *lop3, double *popc, double *mix) {
   if (mix) *mix = std::min(8.0 * (ops / t1), 32.0 * (ops / 4 / t2));
 }
 
+// Bounded-wait self-test: one thread initialises an mbarrier that nothing
+// will ever arrive on and waits for it with the same bounded wait the
+// pairwise kernel uses; when the limit runs out it records where it gave up
+// and returns. Shows on the device that a stuck wait ends with a status the
+// host can read and that the context stays usable. Nothing faults or hangs.
+__global__ void k_wait_selftest(uint64_t limit_ns, int *status, unsigned long long *waited_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  const uint64_t t0 = global_ns();
+  const bool ok = mbar_wait_bounded(&bar, 0, limit_ns);
+  *waited_ns = global_ns() - t0;
+  *status = ok ? 0 : kStatusTmaTimeout;
+}
+
 }  // namespace hd
+
+extern "C" int hd_selftest_wait_timeout(hd_ctx *ctx, uint64_t limit_ns, int *status,
+                                        double *waited_ms) {
+  if (!ctx || !status) return HD_ERR_ARG;
+  try {
+    HD_CUDA(cudaSetDevice(ctx->device));
+    if (limit_ns > 1000000000ull) hd::fail(HD_ERR_ARG, "self-test limit above 1 s");
+    hd::DevBuf out(16, ctx->stream);
+    HD_CUDA(cudaMemsetAsync(out.p, 0xff, 16, ctx->stream));
+    hd::k_wait_selftest<<<1, 32, 0, ctx->stream>>>(
+        limit_ns, out.as<int>(), reinterpret_cast<unsigned long long *>(out.as<uint8_t>() + 8));
+    HD_LAUNCHED(ctx);
+    int host[4];
+    HD_CUDA(cudaMemcpyAsync(host, out.p, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    HD_CUDA(cudaStreamSynchronize(ctx->stream));
+    *status = host[0];
+    unsigned long long ns;
+    std::memcpy(&ns, host + 2, 8);
+    if (waited_ms) *waited_ms = ns / 1e6;
+    return HD_OK;
+  } catch (const hd::Error &e) {
+    ctx->err = e.msg;
+    return e.code;
+  }
+}

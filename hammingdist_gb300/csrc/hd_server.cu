@@ -22,6 +22,7 @@
 // completion thread finalises waves in launch order (copies results back,
 // formats sparse text on the device), releases their bytes and wakes
 // waiters. All waits are host-side and bounded by the caller's timeout.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -451,6 +452,24 @@ int hd_server_result(hd_server *s, uint64_t ticket, const void **data, uint64_t 
     *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
   if (queue_ms)
     *queue_ms = std::chrono::duration<double, std::milli>(r->t_admit - r->t_submit).count();
+  return HD_OK;
+}
+
+int hd_server_cancel(hd_server *s, uint64_t ticket) {
+  if (!s) return HD_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return HD_ERR_ARG;
+  Req *r = it->second.get();
+  auto q = std::find(s->pending.begin(), s->pending.end(), r);
+  if (q == s->pending.end()) {
+    s->ctx->err = "request already admitted";
+    return HD_ERR_STATE;
+  }
+  s->pending.erase(q);
+  r->status = HD_ERR_STATE;
+  r->err = "request cancelled";
+  s->cv.notify_all();
   return HD_OK;
 }
 

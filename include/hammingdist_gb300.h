@@ -284,6 +284,10 @@ int hd_server_result(hd_server *s, uint64_t ticket, const void **data,
                      uint64_t *bytes, uint64_t *count, double *latency_ms,
                      double *queue_ms);
 int hd_server_release(hd_server *s, uint64_t ticket);
+/* Withdraws a request that is still queued (not yet admitted): it finishes
+ * with HD_ERR_STATE "request cancelled". Admitted requests cannot be
+ * cancelled (HD_ERR_STATE). */
+int hd_server_cancel(hd_server *s, uint64_t ticket);
 int hd_server_stats(hd_server *s, uint64_t *waves, uint64_t *completed,
                     uint64_t *max_inflight, uint64_t *bytes_in_use);
 /* Stops admitting, fails queued requests, drains the waves on the device. */
@@ -307,6 +311,13 @@ int hd_tune_load(hd_ctx *ctx, const char *path);
  * instruction mix (pair-sites per second). No reference counterpart. */
 int hd_measure_int_peaks(hd_ctx *ctx, double *lop3_per_s, double *popc_per_s,
                          double *mix_pair_sites_per_s);
+/* Failure-path self-test: a kernel waits, with the bounded wait of the
+ * pairwise kernel and a limit of limit_ns (<= 1 s), on an mbarrier that is
+ * never completed; *status receives the kernel's status word (1 = the wait
+ * ran out) and *waited_ms how long it waited. Nothing faults or hangs, and
+ * the context stays usable. No reference counterpart. */
+int hd_selftest_wait_timeout(hd_ctx *ctx, uint64_t limit_ns, int *status,
+                             double *waited_ms);
 /* Device time of the last pairwise kernel launch sequence (ms, CUDA events on
  * the launching stream) and the number of tiles it processed. */
 int hd_last_pairwise_timing(const hd_ctx *ctx, double *ms, uint64_t *tiles);
