@@ -574,11 +574,15 @@ def run_streaming(args):
             ds.dump_sparse(sp, 3)
             dt = time.perf_counter() - t
         lines = open(sp, "rb").read().splitlines()
-        recs, _ = o.read_fasta(open(f100, "rb").read())
         ok = True
-        for ln in lines[: args.sparse_check]:
-            i, j, dd = (int(x) for x in ln.split())
-            ok &= o.lt_dense([recs[i], recs[j]], max_distance=255)[0] == dd <= 3
+        rec_bytes = L_ + 13  # the generator writes fixed-width records
+        with open(f100, "rb") as fh:
+            def rec(i):
+                fh.seek(i * rec_bytes + 12)
+                return fh.read(L_)
+            for ln in lines[: args.sparse_check]:
+                i, j, dd = (int(x) for x in ln.split())
+                ok &= o.lt_dense([rec(i), rec(j)], max_distance=255)[0] == dd <= 3
         res["dump_sparse"] = {
             "n": n, "threshold": 3, "seconds_total": dt, "seconds_matrix": t1 - t,
             "seconds_dump": dt - (t1 - t), "lines": len(lines),

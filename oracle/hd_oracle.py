@@ -111,7 +111,8 @@ def read_fasta(data: bytes, remove_duplicates: bool = False, n: int = 0):
     total = int(offsets[-1]) if len(offsets) else 0
     raw = b""
     if seqs.value:
-        raw = ctypes.string_at(seqs.value, total) if total else b""
+        # (c_char * n) copies any size; ctypes.string_at takes a C int size
+        raw = bytes((ctypes.c_char * total).from_address(seqs.value)) if total else b""
         L.hdo_free(seqs.value)
     out = [raw[int(offsets[k]):int(offsets[k + 1])] for k in range(nrec.value)]
     indices = _take(idx.value, nin.value, np.uint64) if idx.value else np.zeros(0, np.uint64)
