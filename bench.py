@@ -16,8 +16,9 @@ One step = that whole pass. Metric = unique pairs x L / step time
   e2e   : the public API a user calls (hammingdist_gb300.from_fasta(file) +
           .lt_array + fasta_reference_distances(root, file)): file -> pinned
           host buffer -> device -> host results, every step. The file is read
-          once per step (its mtime changes before each step); the second call
-          finds the same unchanged file already in pinned memory.
+          and uploaded once per step (its mtime changes before each step; the
+          read and the upload overlap); the second call finds the same
+          unchanged file already on the device.
 Inputs are larger than L2 (598 MB of FASTA text, 209 MB of packed rows), so
 no L2 flush is needed between steps.
 
@@ -310,8 +311,9 @@ def run_ours(args):
         e2e_times = []
         h2d = d2h = 0
         for k in range(args.warmup + args.steps):
-            # a new modification time: from_fasta reads the file again every
-            # step; fasta_reference_distances then reuses the bytes it read
+            # a new modification time: from_fasta reads and uploads the file
+            # again every step; fasta_reference_distances then finds the same
+            # unchanged file already on the device
             stamp = time.time_ns()
             os.utime(path, ns=(stamp, stamp))
             torch.cuda.synchronize()
@@ -324,7 +326,7 @@ def run_ours(args):
                 dt = time.perf_counter() - t
             if k >= args.warmup:
                 e2e_times.append(dt)
-            h2d = 2 * nbytes  # the FASTA goes up for each of the two calls (read once)
+            h2d = nbytes  # the FASTA goes up once per step
             d2h = lt_arr.nbytes + 8 * N + rd2.nbytes
         parity = parity and bool(np.array_equal(np.asarray(lt_arr), lt_host)) and \
             bool(np.array_equal(rd2, rd_want))
@@ -357,7 +359,10 @@ def run_ours(args):
                              "peak_source": "in-run LOP3 microbenchmark (hd_measure_int_peaks); "
                                             "MEASURED_PEAKS.json has no integer-pipe figure",
                              "popc_peak_T": peaks["popc_per_s"] / 1e12,
-                             "pair_sites_bound_T": peaks["mix_pair_sites_per_s"] / 1e12,
+                             "pair_sites_bound_T": min(8 * peaks["lop3_per_s"],
+                                                       32 * peaks["popc_per_s"]) / 1e12,
+                             "mix_ceiling_T": peaks["mix_pair_sites_per_s"] / 1e12,
+                             "frac_of_mix_ceiling": pairs * L / kern_s / peaks["mix_pair_sites_per_s"],
                              "kernel_pair_sites_T": pairs * L / kern_s / 1e12,
                              "hbm_write_GBs": pairs / kern_s / 1e9},
                 "e2e": {"value": e2e_value, "unit": "Gpair-sites/s", "h2d_bytes_per_step": h2d,

@@ -31,6 +31,7 @@ SIGNATURES = {
     "hd_ctx_synchronize": (ci, [vp]),
     "hd_ctx_stream": (vp, [vp]),
     "hd_alignment_from_fasta": (ci, [vp, vp, u64, ci, ci, u64, ci, ci, P(vp)]),
+    "hd_alignment_from_fasta_file": (ci, [vp, cp, ci, u64, ci, ci, P(vp)]),
     "hd_alignment_from_sequences": (ci, [vp, vp, vp, u64, ci, ci, P(vp)]),
     "hd_alignment_info": (ci, [vp, P(u64), P(u64), P(u64), P(ci)]),
     "hd_alignment_sequence_indices": (ci, [vp, vp]),
@@ -41,8 +42,10 @@ SIGNATURES = {
     "hd_write_sparse": (ci, [vp, vp, u64, ci, i64, cp, P(u64)]),
     "hd_lower_triangular_text_noalloc": (ci, [vp, vp, u64, ci, vp, u64, P(u64)]),
     "hd_reference_distances": (ci, [vp, vp, u64, vp, u64, ci, P(vp), P(u64)]),
+    "hd_reference_distances_file": (ci, [vp, vp, u64, cp, ci, P(vp), P(u64)]),
     "hd_alignment_reference_distances": (ci, [vp, vp, vp, u64, ci, vp]),
     "hd_fasta_sequence_indices": (ci, [vp, vp, u64, u64, P(vp), P(u64)]),
+    "hd_fasta_sequence_indices_file": (ci, [vp, cp, u64, P(vp), P(u64)]),
     "hd_distance": (ci, [vp, vp, u64, vp, u64, ci, P(ctypes.c_uint32)]),
     "hd_batch_create": (ci, [vp, P(vp)]),
     "hd_batch_add": (ci, [vp, vp, ci, i64, vp, ci]),
@@ -71,6 +74,8 @@ SIGNATURES = {
     "hd_tune_lookup": (ci, [vp, u64, u64, ci, P(ci), P(ci)]),
     "hd_tune_save": (ci, [vp, cp]),
     "hd_tune_load": (ci, [vp, cp]),
+    "hd_trace_enable": (ci, [vp, ctypes.c_int]),
+    "hd_trace_last": (ctypes.c_char_p, [vp]),
     "hd_measure_int_peaks": (ci, [vp, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
     "hd_last_pairwise_timing": (ci, [vp, P(ctypes.c_double), P(u64)]),
 }
@@ -193,6 +198,15 @@ class Context:
                                                   semantics, ctypes.byref(a)))
         return Alignment(self, a)
 
+    def alignment_from_fasta_file(self, path, remove_duplicates=False, n=0, include_x=False,
+                                  semantics=SEM_GPU) -> Alignment:
+        a = vp()
+        self._check(lib().hd_alignment_from_fasta_file(self.h, os.fsencode(path),
+                                                       int(remove_duplicates), n,
+                                                       int(include_x), semantics,
+                                                       ctypes.byref(a)))
+        return Alignment(self, a)
+
     def alignment_from_sequences(self, seqs, include_x=False, semantics=SEM_GPU) -> Alignment:
         seqs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
         raw = b"".join(seqs)
@@ -251,6 +265,14 @@ class Context:
                                                  ctypes.byref(out), ctypes.byref(n)))
         return _take(out, n.value, np.uint32)
 
+    def reference_distances_file(self, ref, path, include_x=False) -> np.ndarray:
+        ref = ref.encode() if isinstance(ref, str) else bytes(ref)
+        out, n = vp(), u64()
+        self._check(lib().hd_reference_distances_file(self.h, _ptr(ref), len(ref),
+                                                      os.fsencode(path), int(include_x),
+                                                      ctypes.byref(out), ctypes.byref(n)))
+        return _take(out, n.value, np.uint32)
+
     def alignment_reference_distances(self, aln: Alignment, ref) -> np.ndarray:
         ref = ref.encode() if isinstance(ref, str) else bytes(ref)
         out = np.zeros(max(aln.n_input, 1), dtype=np.uint32)
@@ -262,6 +284,12 @@ class Context:
         out, cnt = vp(), u64()
         self._check(lib().hd_fasta_sequence_indices(self.h, _ptr(data), len(data), n,
                                                     ctypes.byref(out), ctypes.byref(cnt)))
+        return _take(out, cnt.value, np.uint64)
+
+    def fasta_sequence_indices_file(self, path, n=0) -> np.ndarray:
+        out, cnt = vp(), u64()
+        self._check(lib().hd_fasta_sequence_indices_file(self.h, os.fsencode(path), n,
+                                                         ctypes.byref(out), ctypes.byref(cnt)))
         return _take(out, cnt.value, np.uint64)
 
     def distance(self, s0, s1, include_x=False) -> int:
@@ -331,6 +359,14 @@ class Context:
         self._check(lib().hd_selftest_wait_timeout(self.h, limit_ns, ctypes.byref(st),
                                                    ctypes.byref(ms)))
         return st.value, ms.value
+
+    def trace(self, on=True):
+        """Turns per-phase tracing of this context's calls on or off."""
+        self._check(lib().hd_trace_enable(self.h, 1 if on else 0))
+
+    def trace_last(self):
+        """Text of the last traced call: phases with their stream times."""
+        return (lib().hd_trace_last(self.h) or b"").decode()
 
     def measure_int_peaks(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

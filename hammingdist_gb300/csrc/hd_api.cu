@@ -12,11 +12,69 @@
 #include <limits>
 #include <thread>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "hd_internal.cuh"
 
 using hd::DevBuf;
 using hd::Error;
 using hd::fail;
+
+namespace hd {
+
+namespace {
+cudaEvent_t trace_event(hd_ctx *ctx, size_t k) {
+  while (ctx->trace.pool.size() <= k) {
+    cudaEvent_t e;
+    HD_CUDA(cudaEventCreate(&e));
+    ctx->trace.pool.push_back(e);
+  }
+  return ctx->trace.pool[k];
+}
+}  // namespace
+
+void trace_begin(hd_ctx *ctx, const char *call) {
+  if (!ctx->trace.on) return;
+  if (ctx->trace.call) nvtxRangePop();  // an earlier call ended by an error
+  ctx->trace.call = call;
+  ctx->trace.names.assign(1, nullptr);
+  HD_CUDA(cudaEventRecord(trace_event(ctx, 0), ctx->stream));
+  nvtxRangePushA(call);
+}
+
+void trace_mark(hd_ctx *ctx, const char *phase) {
+  if (!ctx->trace.on || !ctx->trace.call) return;
+  const size_t k = ctx->trace.names.size();
+  HD_CUDA(cudaEventRecord(trace_event(ctx, k), ctx->stream));
+  ctx->trace.names.push_back(phase);
+  nvtxMarkA(phase);
+}
+
+void trace_end(hd_ctx *ctx) {
+  if (!ctx->trace.on || !ctx->trace.call) return;
+  nvtxRangePop();
+  Trace &t = ctx->trace;
+  std::string text = std::string(t.call) + ":";
+  if (t.names.size() > 1) {
+    HD_CUDA(cudaEventSynchronize(t.pool[t.names.size() - 1]));
+    float total = 0;
+    for (size_t k = 1; k < t.names.size(); ++k) {
+      float ms = 0;
+      HD_CUDA(cudaEventElapsedTime(&ms, t.pool[k - 1], t.pool[k]));
+      total += ms;
+      char buf[128];
+      std::snprintf(buf, sizeof buf, " %s %.3f ms,", t.names[k], ms);
+      text += buf;
+    }
+    char buf[64];
+    std::snprintf(buf, sizeof buf, " stream time %.3f ms", total);
+    text += buf;
+  }
+  t.last = text;
+  t.call = nullptr;
+}
+
+}  // namespace hd
 
 namespace {
 
@@ -72,6 +130,7 @@ void check_status(hd_ctx *ctx) {
 const uint8_t *stage_input(hd_ctx *ctx, const char *bytes, uint64_t n, int on_device) {
   if (on_device && (reinterpret_cast<uintptr_t>(bytes) & 15u) == 0)
     return reinterpret_cast<const uint8_t *>(bytes);
+  ctx->file_tag.clear();
   if (ctx->file.bytes < n + 16) {
     ctx->file.release();
     ctx->file = DevBuf(hd::round_up(n + 16, 1 << 20), ctx->stream);
@@ -81,6 +140,99 @@ const uint8_t *stage_input(hd_ctx *ctx, const char *bytes, uint64_t n, int on_de
                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                             ctx->stream));
   return ctx->file.as<uint8_t>();
+}
+
+std::string open_failed(const char *path) {
+  return std::string("Error: Failed to open file '") + (path ? path : "") + "'";
+}
+
+// What identifies a file's contents for the device input cache: path, size,
+// inode, device, and the modification and status-change times in ns.
+std::string file_tag(const char *path, const struct stat &sb) {
+  char buf[160];
+  std::snprintf(buf, sizeof buf, "|%llu|%llu|%llu|%lld.%09ld|%lld.%09ld",
+                (unsigned long long)sb.st_size, (unsigned long long)sb.st_ino,
+                (unsigned long long)sb.st_dev, (long long)sb.st_mtim.tv_sec, sb.st_mtim.tv_nsec,
+                (long long)sb.st_ctim.tv_sec, sb.st_ctim.tv_nsec);
+  return std::string(path) + buf;
+}
+
+// Reads a FASTA file into the context's device input buffer: up to 16
+// threads pread 8 MB parts into pinned staging, and each part is copied to
+// the device as soon as it is read, so the upload runs under the read. If the
+// buffer already holds this file, unchanged, nothing is read or copied.
+// Returns the device bytes; *nbytes = the file size.
+const uint8_t *stage_file(hd_ctx *ctx, const char *path, uint64_t *nbytes) {
+  struct stat sb;
+  if (!path || ::stat(path, &sb) != 0 || !S_ISREG(sb.st_mode)) fail(HD_ERR_IO, open_failed(path));
+  const uint64_t n = (uint64_t)sb.st_size;
+  *nbytes = n;
+  const std::string tag = file_tag(path, sb);
+  if (!ctx->file_tag.empty() && ctx->file_tag == tag && ctx->file.bytes >= n + 16) {
+    hd::trace_mark(ctx, "file already on the device");
+    return ctx->file.as<uint8_t>();
+  }
+  ctx->file_tag.clear();
+  if (ctx->file.bytes < n + 16) {
+    ctx->file.release();
+    ctx->file = DevBuf(hd::round_up(n + 16, 1 << 20), ctx->stream);
+  }
+  if (n + 1 > ctx->pin_cap) {
+    if (ctx->pin) cudaFreeHost(ctx->pin);
+    ctx->pin = nullptr;
+    ctx->pin_cap = 0;
+    const size_t cap = (size_t)((n + 1) * 5 / 4 + (1 << 20));
+    HD_CUDA(cudaHostAlloc(&ctx->pin, cap, cudaHostAllocDefault));
+    ctx->pin_cap = cap;
+  }
+  const int fd = ::open(path, O_RDONLY);
+  if (fd < 0) fail(HD_ERR_IO, open_failed(path));
+  char *pin = static_cast<char *>(ctx->pin);
+  uint8_t *dev = ctx->file.as<uint8_t>();
+  const uint64_t kPart = 8ull << 20, parts = hd::ceil_div(n, kPart);
+  std::atomic<uint64_t> next{0};
+  std::atomic<int> bad{0};  // 1 = read error, 2 = copy error
+  auto work = [&] {
+    if (cudaSetDevice(ctx->device) != cudaSuccess) {
+      bad = 2;
+      return;
+    }
+    for (;;) {
+      const uint64_t k = next.fetch_add(1);
+      if (k >= parts || bad.load()) return;
+      const uint64_t off = k * kPart, len = std::min(kPart, n - off);
+      uint64_t got = 0;
+      while (got < len) {
+        const ssize_t r = ::pread(fd, pin + off + got, (size_t)(len - got), (off_t)(off + got));
+        if (r <= 0) {
+          bad = 1;
+          return;
+        }
+        got += (uint64_t)r;
+      }
+      if (cudaMemcpyAsync(dev + off, pin + off, len, cudaMemcpyHostToDevice, ctx->stream) !=
+          cudaSuccess) {
+        bad = 2;
+        return;
+      }
+    }
+  };
+  const unsigned nt = (unsigned)std::min<uint64_t>(16, parts);
+  if (nt <= 1) {
+    work();
+  } else {
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t) th.emplace_back(work);
+    for (auto &x : th) x.join();
+  }
+  ::close(fd);
+  if (bad.load()) {
+    cudaStreamSynchronize(ctx->stream);  // copies already queued still read the staging
+    if (bad.load() == 1) fail(HD_ERR_IO, open_failed(path));
+    fail(HD_ERR_CUDA, "cudaMemcpyAsync of the FASTA file failed");
+  }
+  ctx->file_tag = tag;
+  return dev;
 }
 
 uint64_t words_for(uint64_t L) { return hd::round_up(hd::ceil_div(L ? L : 1, 32), 8); }
@@ -107,6 +259,7 @@ hd_alignment *build_alignment(hd_ctx *ctx, hd::Records &rec, int remove_duplicat
       rows = hd::dedupe(ctx, rec, &nu, aln->seqidx);
       d_rows = rows.as<uint64_t>();
       aln->n_rows = nu;
+      hd::trace_mark(ctx, "dedupe");
     } else {
       aln->n_rows = rec.n;
     }
@@ -121,6 +274,7 @@ hd_alignment *build_alignment(hd_ctx *ctx, hd::Records &rec, int remove_duplicat
         const uint64_t same = hd::consensus_matches(ctx, rec, d_rows, aln->n_rows);
         const double frac = (double)(total - same) / (double)total;
         rule = frac < 0.005 ? HD_RULE_SPARSE : HD_RULE_AND;
+        hd::trace_mark(ctx, "consensus");
       }
     }
     aln->rule = rule;
@@ -132,6 +286,7 @@ hd_alignment *build_alignment(hd_ctx *ctx, hd::Records &rec, int remove_duplicat
       HD_CUDA(cudaMemcpyAsync(aln->d_seqidx.p, aln->seqidx.data(), aln->seqidx.size() * 8,
                               cudaMemcpyHostToDevice, ctx->stream));
     }
+    hd::trace_mark(ctx, "pack");
     HD_CUDA(cudaStreamSynchronize(ctx->stream));
   } catch (...) {
     delete aln;
@@ -245,6 +400,50 @@ void stream_lt_text(hd_ctx *ctx, uint64_t n, int dtype_bytes, const char *path, 
   check_status(ctx);
 }
 
+// fasta_reference_distances (src/hamming.cc:104-141) over FASTA bytes already
+// on the device: parse, one distance per record, copy to a malloc'd array.
+void reference_distances_of(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, const char *ref,
+                            uint64_t ref_len, int include_x, uint32_t **out, uint64_t *n_out) {
+  hd::Records rec = hd::parse_fasta(ctx, d, nbytes, 0);
+  hd::trace_mark(ctx, "parse");
+  if (rec.max_len > ref_len)
+    fail(HD_ERR_REF_LENGTH, "Error: a sequence is longer than the reference sequence");
+  uint32_t *h = static_cast<uint32_t *>(std::malloc((rec.n ? rec.n : 1) * 4));
+  if (!h) throw std::bad_alloc();
+  try {
+    if (rec.n) {
+      DevBuf d_ref(ref_len + 16, ctx->stream), d_out(rec.n * 4, ctx->stream);
+      if (ref_len)
+        HD_CUDA(cudaMemcpyAsync(d_ref.p, ref, ref_len, cudaMemcpyHostToDevice, ctx->stream));
+      hd::reference_distances_device(ctx, rec, d_ref.as<uint8_t>(), include_x, d_out.as<uint32_t>());
+      hd::trace_mark(ctx, "distances");
+      HD_CUDA(cudaMemcpyAsync(h, d_out.p, rec.n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      hd::trace_mark(ctx, "copy to host");
+      HD_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    hd::trace_end(ctx);
+  } catch (...) {
+    std::free(h);
+    throw;
+  }
+  *out = h;
+  *n_out = rec.n;
+}
+
+// fasta_sequence_indices (src/hamming.cc:76-102) over FASTA bytes on the device.
+void sequence_indices_of(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64_t n_limit,
+                         uint64_t **out, uint64_t *n_out) {
+  hd::Records rec = hd::parse_fasta(ctx, d, nbytes, n_limit);
+  std::vector<uint64_t> idx;
+  uint64_t nu = 0;
+  DevBuf rows = hd::dedupe(ctx, rec, &nu, idx);
+  uint64_t *h = static_cast<uint64_t *>(std::malloc((idx.size() ? idx.size() : 1) * 8));
+  if (!h) throw std::bad_alloc();
+  if (!idx.empty()) std::memcpy(h, idx.data(), idx.size() * 8);
+  *out = h;
+  *n_out = idx.size();
+}
+
 }  // namespace
 
 // =================================================================== ABI
@@ -284,6 +483,7 @@ int hd_ctx_create(int device, hd_ctx **out) {
                                              cudaEnableDefault, &q));
     if (!fn || q != cudaDriverEntryPointSuccess) fail(HD_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     ctx->encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    if (const char *t = std::getenv("HAMMINGDIST_TRACE")) ctx->trace.on = t[0] && t[0] != '0';
     // default autotuner table: HAMMINGDIST_TUNING names a file saved by
     // hd_tune_save; it applies only if it was measured on this device kind
     if (const char *path = std::getenv("HAMMINGDIST_TUNING")) {
@@ -319,12 +519,22 @@ void hd_ctx_destroy(hd_ctx *ctx) {
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
   if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+  for (cudaEvent_t e : ctx->trace.pool) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->side) cudaStreamDestroy(ctx->side);
   delete ctx;
 }
 
 const char *hd_last_error(const hd_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int hd_trace_enable(hd_ctx *ctx, int on) {
+  if (!ctx) return HD_ERR_ARG;
+  ctx->trace.on = on != 0;
+  if (!ctx->trace.on) ctx->trace.last.clear();
+  return HD_OK;
+}
+
+const char *hd_trace_last(const hd_ctx *ctx) { return ctx ? ctx->trace.last.c_str() : ""; }
 
 uint64_t hd_ctx_kernel_launches(const hd_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
@@ -355,9 +565,30 @@ int hd_alignment_from_fasta(hd_ctx *ctx, const char *fasta, uint64_t nbytes, int
   if (!ctx || !out || (!fasta && nbytes)) return HD_ERR_ARG;
   *out = nullptr;
   return guard(ctx, [&] {
+    hd::trace_begin(ctx, "hd_alignment_from_fasta");
     const uint8_t *d = stage_input(ctx, fasta, nbytes, fasta_on_device);
+    hd::trace_mark(ctx, "upload");
     hd::Records rec = hd::parse_fasta(ctx, d, nbytes, n_limit);
+    hd::trace_mark(ctx, "parse");
     *out = build_alignment(ctx, rec, remove_duplicates, include_x, semantics);
+    hd::trace_end(ctx);
+  });
+}
+
+int hd_alignment_from_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicates,
+                                 uint64_t n_limit, int include_x, int semantics,
+                                 hd_alignment **out) {
+  if (!ctx || !out || !path) return HD_ERR_ARG;
+  *out = nullptr;
+  return guard(ctx, [&] {
+    hd::trace_begin(ctx, "hd_alignment_from_fasta_file");
+    uint64_t nbytes = 0;
+    const uint8_t *d = stage_file(ctx, path, &nbytes);
+    hd::trace_mark(ctx, "read + upload");
+    hd::Records rec = hd::parse_fasta(ctx, d, nbytes, n_limit);
+    hd::trace_mark(ctx, "parse");
+    *out = build_alignment(ctx, rec, remove_duplicates, include_x, semantics);
+    hd::trace_end(ctx);
   });
 }
 
@@ -412,12 +643,17 @@ int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, int64_
       d_out = tmp.p;
     }
     const uint32_t nb = (uint32_t)hd::ceil_div(n, hd::kTile);
+    hd::trace_begin(ctx, "hd_pairwise_lt");
     HD_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
     hd::pairwise_tiles(ctx, aln, dtype_bytes, md, d_out, 0, 0, nb);
     HD_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
-    if (!out_on_device)
+    hd::trace_mark(ctx, "pairwise");
+    if (!out_on_device) {
       HD_CUDA(cudaMemcpyAsync(out, d_out, entries * dtype_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+      hd::trace_mark(ctx, "copy to host");
+    }
     HD_CUDA(cudaStreamSynchronize(ctx->stream));
+    hd::trace_end(ctx);
     float ms = 0;
     HD_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
     ctx->last_pair_ms = ms;
@@ -521,27 +757,24 @@ int hd_reference_distances(hd_ctx *ctx, const char *ref, uint64_t ref_len, const
   *out = nullptr;
   *n_out = 0;
   return guard(ctx, [&] {
+    hd::trace_begin(ctx, "hd_reference_distances");
     const uint8_t *d = stage_input(ctx, fasta, nbytes, 0);
-    hd::Records rec = hd::parse_fasta(ctx, d, nbytes, 0);
-    if (rec.max_len > ref_len)
-      fail(HD_ERR_REF_LENGTH, "Error: a sequence is longer than the reference sequence");
-    uint32_t *h = static_cast<uint32_t *>(std::malloc((rec.n ? rec.n : 1) * 4));
-    if (!h) throw std::bad_alloc();
-    try {
-      if (rec.n) {
-        DevBuf d_ref(ref_len + 16, ctx->stream), d_out(rec.n * 4, ctx->stream);
-        if (ref_len)
-          HD_CUDA(cudaMemcpyAsync(d_ref.p, ref, ref_len, cudaMemcpyHostToDevice, ctx->stream));
-        hd::reference_distances_device(ctx, rec, d_ref.as<uint8_t>(), include_x, d_out.as<uint32_t>());
-        HD_CUDA(cudaMemcpyAsync(h, d_out.p, rec.n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        HD_CUDA(cudaStreamSynchronize(ctx->stream));
-      }
-    } catch (...) {
-      std::free(h);
-      throw;
-    }
-    *out = h;
-    *n_out = rec.n;
+    hd::trace_mark(ctx, "upload");
+    reference_distances_of(ctx, d, nbytes, ref, ref_len, include_x, out, n_out);
+  });
+}
+
+int hd_reference_distances_file(hd_ctx *ctx, const char *ref, uint64_t ref_len, const char *path,
+                                int include_x, uint32_t **out, uint64_t *n_out) {
+  if (!ctx || !out || !n_out || (!ref && ref_len) || !path) return HD_ERR_ARG;
+  *out = nullptr;
+  *n_out = 0;
+  return guard(ctx, [&] {
+    hd::trace_begin(ctx, "hd_reference_distances_file");
+    uint64_t nbytes = 0;
+    const uint8_t *d = stage_file(ctx, path, &nbytes);
+    hd::trace_mark(ctx, "read + upload");
+    reference_distances_of(ctx, d, nbytes, ref, ref_len, include_x, out, n_out);
   });
 }
 
@@ -569,15 +802,19 @@ int hd_fasta_sequence_indices(hd_ctx *ctx, const char *fasta, uint64_t nbytes, u
   *n_out = 0;
   return guard(ctx, [&] {
     const uint8_t *d = stage_input(ctx, fasta, nbytes, 0);
-    hd::Records rec = hd::parse_fasta(ctx, d, nbytes, n_limit);
-    std::vector<uint64_t> idx;
-    uint64_t nu = 0;
-    DevBuf rows = hd::dedupe(ctx, rec, &nu, idx);
-    uint64_t *h = static_cast<uint64_t *>(std::malloc((idx.size() ? idx.size() : 1) * 8));
-    if (!h) throw std::bad_alloc();
-    if (!idx.empty()) std::memcpy(h, idx.data(), idx.size() * 8);
-    *out = h;
-    *n_out = idx.size();
+    sequence_indices_of(ctx, d, nbytes, n_limit, out, n_out);
+  });
+}
+
+int hd_fasta_sequence_indices_file(hd_ctx *ctx, const char *path, uint64_t n_limit, uint64_t **out,
+                                   uint64_t *n_out) {
+  if (!ctx || !out || !n_out || !path) return HD_ERR_ARG;
+  *out = nullptr;
+  *n_out = 0;
+  return guard(ctx, [&] {
+    uint64_t nbytes = 0;
+    const uint8_t *d = stage_file(ctx, path, &nbytes);
+    sequence_indices_of(ctx, d, nbytes, n_limit, out, n_out);
   });
 }
 

@@ -82,6 +82,20 @@ struct DevBuf {
 }  // namespace hd
 
 // -------------------------------------------------------------- objects
+namespace hd {
+// Per-call phase trace (off unless enabled): a CUDA event is recorded on the
+// context's stream at each phase boundary and the durations are read once
+// at the end of the call, so tracing adds no synchronisation inside a call.
+// NVTX marks the call as a range and each boundary as a mark for profilers.
+struct Trace {
+  bool on = false;
+  const char *call = nullptr;
+  std::vector<cudaEvent_t> pool;
+  std::vector<const char *> names;  // phase ending at event k (k >= 1)
+  std::string last;                 // text of the last traced call
+};
+}  // namespace hd
+
 struct hd_ctx {
   int device = 0;
   int sm_count = 0;
@@ -95,6 +109,8 @@ struct hd_ctx {
   uint64_t last_pair_tiles = 0;
   PFN_cuTensorMapEncodeTiled_v12000 encode_tiled = nullptr;
   hd::DevBuf file;                // device copy of the last FASTA input
+  // identity of the file whose bytes `file` holds (empty: none or other bytes)
+  std::string file_tag;
   // autotuned kernel configurations: key = (n bucket, L bucket, dtype)
   std::vector<std::pair<uint32_t, std::pair<int, int>>> tune;
   // child contexts (own streams) for concurrent ingest of many inputs
@@ -102,6 +118,7 @@ struct hd_ctx {
   // pinned staging for file reads by this context (grows)
   void *pin = nullptr;
   size_t pin_cap = 0;
+  hd::Trace trace;
 };
 
 struct hd_alignment {
@@ -398,5 +415,10 @@ uint64_t format_sparse_rows(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint
 
 // peak.cu
 void measure_int_peaks(hd_ctx *ctx, double *lop3, double *popc, double *mix);
+
+// phase tracing of one API call (no-ops unless ctx->trace.on)
+void trace_begin(hd_ctx *ctx, const char *call);
+void trace_mark(hd_ctx *ctx, const char *phase);
+void trace_end(hd_ctx *ctx);
 
 }  // namespace hd

@@ -42,11 +42,6 @@ namespace {
 
 std::mutex g_mu;         // one context per process; calls are serialised
 hd_ctx *g_ctx = nullptr;
-void *g_pin = nullptr;   // pinned staging for FASTA bytes, grows
-size_t g_pin_cap = 0;
-// identity of the file whose bytes g_pin holds (path, size, inode, mtime):
-// a second call on the same unchanged file skips the read
-std::string g_pin_tag;
 
 hd_ctx *ctx() {
   if (!g_ctx) {
@@ -68,85 +63,61 @@ void check(int rc) {
   throw std::runtime_error("Error: Failed to open file '" + f + "'");
 }
 
-// Pinned staging buffer of at least n bytes (grows, never shrinks).
-char *pinned(uint64_t n) {
-  g_pin_tag.clear();  // the caller is about to overwrite it
-  if (n > g_pin_cap) {
-    if (g_pin) hd_host_free(g_ctx, g_pin);
-    g_pin = nullptr;
-    g_pin_cap = 0;
-    size_t cap = (size_t)(n * 5 / 4 + (1 << 20));
-    if (hd_host_alloc(g_ctx, cap, &g_pin) != HD_OK) throw std::runtime_error(hd_last_error(g_ctx));
-    g_pin_cap = cap;
-  }
-  return static_cast<char *>(g_pin);
-}
-
-// Reads n bytes of `path` into dst with parallel preads (32 MB pieces).
-bool read_into(const std::string &path, char *dst, uint64_t n) {
-  int fd = ::open(path.c_str(), O_RDONLY);
-  if (fd < 0) return false;
-  const uint64_t kPart = 32ull << 20;
-  const unsigned nthreads = n > kPart ? std::min<unsigned>(16, (unsigned)((n + kPart - 1) / kPart)) : 1;
-  std::vector<int> ok(nthreads, 1);
-  const uint64_t per = (n + nthreads - 1) / nthreads;
-  auto work = [&](unsigned t) {
-    uint64_t off = t * per, end = std::min(n, off + per);
-    while (off < end) {
-      ssize_t r = ::pread(fd, dst + off, (size_t)std::min<uint64_t>(end - off, 1ull << 30), (off_t)off);
-      if (r <= 0) {
-        ok[t] = 0;
-        return;
-      }
-      off += (uint64_t)r;
-    }
-  };
-  if (nthreads == 1) {
-    work(0);
-  } else {
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nthreads; ++t) th.emplace_back(work, t);
-    for (auto &x : th) x.join();
-  }
-  ::close(fd);
-  for (int v : ok)
-    if (!v) return false;
-  return true;
-}
-
-// Reads a whole file into the pinned staging buffer (or finds it there: the
-// same path, size, inode and modification time as the last file read).
-std::pair<const char *, uint64_t> read_pinned(const std::string &path) {
-  struct stat sb;
-  if (::stat(path.c_str(), &sb) != 0 || !S_ISREG(sb.st_mode)) open_failed(path);
-  const uint64_t n = (uint64_t)sb.st_size;
-  const std::string tag = path + "|" + std::to_string(n) + "|" + std::to_string(sb.st_ino) + "|" +
-                          std::to_string(sb.st_dev) + "|" + std::to_string(sb.st_mtim.tv_sec) + "." +
-                          std::to_string(sb.st_mtim.tv_nsec);
-  if (!g_pin_tag.empty() && g_pin_tag == tag) return {static_cast<const char *>(g_pin), n};
-  char *dst = pinned(n + 1);
-  if (!read_into(path, dst, n)) open_failed(path);
-  g_pin_tag = tag;
-  return {dst, n};
-}
-
-// memcpy with up to 8 threads (large results).
-void copy_parallel(void *dst, const void *src, size_t n) {
-  const size_t kMin = 16u << 20;
-  if (n < kMin) {
-    std::memcpy(dst, src, n);
+// Runs f(begin, end) over [0, n) bytes on up to 16 threads (4 MB or more each).
+template <class F>
+void split_parallel(size_t n, F &&f) {
+  const size_t kMin = 4u << 20;
+  const unsigned nt = (unsigned)std::max<size_t>(1, std::min<size_t>(16, n / kMin));
+  if (nt == 1) {
+    f(size_t(0), n);
     return;
   }
-  const unsigned nt = (unsigned)std::min<size_t>(8, n / kMin);
   const size_t per = (n + nt - 1) / nt;
   std::vector<std::thread> th;
   for (unsigned t = 0; t < nt; ++t)
-    th.emplace_back([=] {
+    th.emplace_back([&, t] {
       const size_t a = t * per, b = std::min(n, a + per);
-      if (a < b) std::memcpy(static_cast<char *>(dst) + a, static_cast<const char *>(src) + a, b - a);
+      if (a < b) f(a, b);
     });
   for (auto &x : th) x.join();
 }
+
+// memcpy of large results on up to 16 threads.
+void copy_parallel(void *dst, const void *src, size_t n) {
+  split_parallel(n, [&](size_t a, size_t b) {
+    std::memcpy(static_cast<char *>(dst) + a, static_cast<const char *>(src) + a, b - a);
+  });
+}
+
+// Zeroes fresh memory on up to 16 threads, so its pages are first touched in
+// parallel (one thread faulting in ~100 MB costs several ms).
+void zero_parallel(void *dst, size_t n) {
+  split_parallel(n, [&](size_t a, size_t b) { std::memset(static_cast<char *>(dst) + a, 0, b - a); });
+}
+
+// Allocator whose resize() leaves new elements uninitialised; result vectors
+// are sized, zeroed in parallel and then filled by the device copy.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+  using value_type = T;
+  template <class U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <class U>
+  NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
+  template <class U>
+  void construct(U *p) noexcept {
+    ::new (static_cast<void *>(p)) U;
+  }
+  template <class U, class... A>
+  void construct(U *p, A &&...a) {
+    ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+  }
+};
+template <class T>
+using HostVec = std::vector<T, NoInitAlloc<T>>;
 
 struct Aln {
   hd_alignment *p = nullptr;
@@ -154,6 +125,23 @@ struct Aln {
 };
 
 void say(const std::string &s) { std::cout << "# hammingdist :: " << s << std::endl; }
+
+// HAMMINGDIST_TRACE=1: the context traces its calls' phases (CUDA events on
+// its stream); each traced call's line is printed after it, and host-side
+// phases are timed here.
+bool tracing() {
+  static const bool on = [] {
+    const char *t = std::getenv("HAMMINGDIST_TRACE");
+    return t && t[0] && t[0] != '0';
+  }();
+  return on;
+}
+void say_trace() {
+  if (tracing()) say(std::string("trace ") + hd_trace_last(g_ctx));
+}
+void say_host(const char *what, double ms) {
+  if (tracing()) say(std::string("trace host: ") + what + " " + std::to_string(ms) + " ms");
+}
 
 double ms_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -167,7 +155,7 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 template <typename T>
 struct DataSet {
   uint64_t nsamples = 0;
-  std::vector<T> result;
+  HostVec<T> result;
   std::vector<uint64_t> sequence_indices;
 
   int at(const std::array<size_t, 2> &ij) const {
@@ -233,7 +221,10 @@ DataSet<T> compute(hd_alignment *aln, int64_t max_distance, bool announce, const
   int rule = 0;
   check(hd_alignment_info(aln, &n_rows, &L, &n_in, &rule));
   ds.nsamples = n_rows;
+  const auto ta = std::chrono::steady_clock::now();
   ds.result.resize(n_rows < 2 ? 0 : n_rows * (n_rows - 1) / 2);
+  zero_parallel(ds.result.data(), ds.result.size() * sizeof(T));
+  say_host("result allocation", ms_since(ta));
   if (announce) {
     say(std::string("Using GPU (") + what +
         (rule == HD_RULE_AND ? ", dense distance rule)..." : ", sparse distance rule)..."));
@@ -242,6 +233,7 @@ DataSet<T> compute(hd_alignment *aln, int64_t max_distance, bool announce, const
   auto t1 = std::chrono::steady_clock::now();
   if (!ds.result.empty())
     check(hd_pairwise_lt(g_ctx, aln, sizeof(T), max_distance, ds.result.data(), 0));
+  if (!ds.result.empty()) say_trace();
   if (announce)
     say("...distance calculation completed in " + std::to_string((long long)ms_since(t1)) + " ms.");
   return ds;
@@ -253,13 +245,11 @@ DataSet<T> from_fasta(const std::string &filename, bool include_x, bool remove_d
   std::lock_guard<std::mutex> lk(g_mu);
   hd_ctx *c = ctx();
   auto t0 = std::chrono::steady_clock::now();
-  auto [bytes, nbytes] = read_pinned(filename);
-  say("...read " + std::to_string(nbytes) + " bytes in " +
-      std::to_string((long long)ms_since(t0)) + " ms...");
   py::gil_scoped_release nogil;
   Aln a;
-  check(hd_alignment_from_fasta(c, bytes, nbytes, 0, remove_duplicates, n, include_x,
-                                use_gpu ? HD_SEM_GPU : HD_SEM_CPU, &a.p));
+  check(hd_alignment_from_fasta_file(c, filename.c_str(), remove_duplicates, n, include_x,
+                                     use_gpu ? HD_SEM_GPU : HD_SEM_CPU, &a.p));
+  say_trace();
   DataSet<T> ds = compute<T>(a.p, max_distance, true, use_gpu ? "use_gpu=True" : "use_gpu=False", t0);
   if (remove_duplicates) {
     uint64_t n_in = 0;
@@ -294,10 +284,10 @@ void from_fasta_to_lower_triangular(const std::string &in, const std::string &ou
   hd_ctx *c = ctx();
   auto t0 = std::chrono::steady_clock::now();
   if (use_gpu) say("Using GPU...");
-  auto [bytes, nbytes] = read_pinned(in);
   py::gil_scoped_release nogil;
   Aln a;
-  check(hd_alignment_from_fasta(c, bytes, nbytes, 0, remove_duplicates, n, 0, HD_SEM_GPU, &a.p));
+  check(hd_alignment_from_fasta_file(c, in.c_str(), remove_duplicates, n, 0, HD_SEM_GPU, &a.p));
+  say_trace();
   say("...pre-processing completed in " + std::to_string((long long)ms_since(t0)) + " ms...");
   // src/hamming.cc:47-52: the reference computes this on the GPU only
   if (!use_gpu) throw std::runtime_error("from_fasta_to_lower_triangular is currently only available on GPU");
@@ -411,25 +401,24 @@ py::array_t<uint32_t> fasta_reference_distances(const std::string &ref, const st
                                                 bool include_x) {
   std::lock_guard<std::mutex> lk(g_mu);
   hd_ctx *c = ctx();
-  auto [bytes, nbytes] = read_pinned(fasta);
   uint32_t *out = nullptr;
   uint64_t n = 0;
   {
     py::gil_scoped_release nogil;
-    check(hd_reference_distances(c, ref.data(), ref.size(), bytes, nbytes, include_x, &out, &n));
+    check(hd_reference_distances_file(c, ref.data(), ref.size(), fasta.c_str(), include_x, &out, &n));
   }
+  say_trace();
   return owned_array<uint32_t>(out, n);
 }
 
 py::array_t<uint64_t> fasta_sequence_indices(const std::string &fasta, size_t nlim) {
   std::lock_guard<std::mutex> lk(g_mu);
   hd_ctx *c = ctx();
-  auto [bytes, nbytes] = read_pinned(fasta);
   uint64_t *out = nullptr;
   uint64_t n = 0;
   {
     py::gil_scoped_release nogil;
-    check(hd_fasta_sequence_indices(c, bytes, nbytes, nlim, &out, &n));
+    check(hd_fasta_sequence_indices_file(c, fasta.c_str(), nlim, &out, &n));
   }
   return owned_array<uint64_t>(out, n);
 }
@@ -464,6 +453,7 @@ DataSet<uint8_t> from_csv(const std::string &filename) {
   }
   ds.nsamples = n;
   ds.result.resize(n * (n + 1) / 2);
+  zero_parallel(ds.result.data(), ds.result.size());  // entries past the rows read stay 0
   uint64_t i = 0, row = 0;
   while (std::getline(s, line)) {
     std::istringstream ls(line);
@@ -493,7 +483,9 @@ void bind_dataset(py::module_ &m, const char *name, int default_threshold) {
       .def_property_readonly("lt_array", [](const DataSet<T> &self) {
         // a fresh copy on every access, as the reference's py::array(size, ptr)
         py::array_t<T> a((py::ssize_t)self.result.size());
+        const auto tc = std::chrono::steady_clock::now();
         copy_parallel(a.mutable_data(), self.result.data(), self.result.size() * sizeof(T));
+        say_host("lt_array copy", ms_since(tc));
         return a;
       });
 }

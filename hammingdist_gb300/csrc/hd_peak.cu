@@ -55,6 +55,57 @@ __global__ void k_peak_popc(uint32_t iters, uint32_t *sink) {
   if (v == 0x12345678u) sink[0] = v;
 }
 
+__device__ __forceinline__ uint32_t lop3_and(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm volatile("lop3.b32 %0, %1, %2, %1, 0x88;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t lop3_or_and(uint32_t x, uint32_t y, uint32_t z) {
+  uint32_t d;
+  asm volatile("lop3.b32 %0, %1, %2, %3, 0xF8;" : "=r"(d) : "r"(x), "r"(y), "r"(z));
+  return d;
+}
+__device__ __forceinline__ uint32_t mad_asm(uint32_t acc, uint32_t p, uint32_t k) {
+  uint32_t d;
+  asm volatile("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(p), "r"(k), "r"(acc));
+  return d;
+}
+
+// The pairwise inner loop's instruction mix from registers alone: per word
+// (32 pair-sites) one AND, three OR-AND LOP3s, a POPC and an IMAD
+// accumulation; eight chains per thread, each word's operands taken from
+// the other chains. Run at the pairwise kernel's occupancy (16 warps per SM),
+// it gives the rate this mix reaches with no shared-memory loads, barriers
+// or stores.
+__global__ void k_peak_mix(uint32_t iters, uint32_t *sink) {
+  uint32_t x[8], acc[8];
+  const uint32_t c0 = threadIdx.x * 0x1234567u, c1 = blockIdx.x ^ 0x55aa55aau, c2 = c0 * 3u,
+                 c3 = c1 + 7u;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    x[k] = threadIdx.x * 0x9e3779b9u + k * 0x85ebca6bu + blockIdx.x;
+    acc[k] = 0;
+  }
+  const uint32_t one = (blockIdx.x >> 30) + 1u;  // 1, unknown to the compiler
+  for (uint32_t it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        uint32_t m = lop3_and(x[k], c0);
+        m = lop3_or_and(m, x[(k + 1) & 7], c1);
+        m = lop3_or_and(m, x[(k + 2) & 7], c2);
+        m = lop3_or_and(m, x[(k + 3) & 7], c3);
+        acc[k] = mad_asm(acc[k], popc_asm(m), one);
+        x[k] = m;
+      }
+  }
+  uint32_t v = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v ^= x[k] + acc[k];
+  if (v == 0x12345678u) sink[0] = v;
+}
+
 static double time_kernel(hd_ctx *ctx, void (*kern)(uint32_t, uint32_t *), uint32_t iters,
                           uint32_t *sink, unsigned blocks) {
   cudaEvent_t a, b;
@@ -83,8 +134,11 @@ void measure_int_peaks(hd_ctx *ctx, double *lop3, double *popc, double *mix) {
   double t2 = time_kernel(ctx, k_peak_popc, iters / 4, sink.as<uint32_t>(), blocks);
   if (lop3) *lop3 = ops / t1;
   if (popc) *popc = ops / 4 / t2;
-  // pair-sites bound of the 4 LOP3 + 1 POPC mix when the two pipes overlap
-  if (mix) *mix = std::min(8.0 * (ops / t1), 32.0 * (ops / 4 / t2));
+  // the mix at 16 warps per SM: words = blocks x threads x iters x 64
+  const unsigned mix_blocks = (unsigned)ctx->sm_count * 2;
+  const uint32_t mix_iters = 1024;
+  const double t3 = time_kernel(ctx, k_peak_mix, mix_iters, sink.as<uint32_t>(), mix_blocks);
+  if (mix) *mix = 32.0 * (double)mix_blocks * kPeakThreads * mix_iters * 64 / t3;
 }
 
 // Bounded-wait self-test: one thread initialises an mbarrier that nothing

@@ -97,6 +97,17 @@ int hd_alignment_from_fasta(hd_ctx *ctx, const char *fasta, uint64_t nbytes,
                             int fasta_on_device, int remove_duplicates,
                             uint64_t n_limit, int include_x, int semantics,
                             hd_alignment **out);
+/* The same from a FASTA file (read_fasta's own input, src/hamming_impl.cc:
+ * 200-242). Up to 16 threads pread 8 MB parts into pinned staging, and each
+ * part is copied to the device as soon as it is read, so the upload runs
+ * under the read. The context remembers which file its device input buffer
+ * holds (path, size, inode, device, mtime, ctime): the file calls below on
+ * the same unchanged file reuse those device bytes without reading or
+ * copying them again. A call with FASTA bytes replaces the buffer. An
+ * unreadable path fails with HD_ERR_IO, "Error: Failed to open file '<f>'". */
+int hd_alignment_from_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicates,
+                                 uint64_t n_limit, int include_x, int semantics,
+                                 hd_alignment **out);
 /* Same from n sequences held back to back in `bytes` with offsets[0..n]
  * (host memory). Replaces the DataSet(std::vector<std::string>&) path of
  * from_stringlist (src/hamming.cc:16-21). */
@@ -178,6 +189,11 @@ int hd_lower_triangular_text_noalloc(hd_ctx *ctx, const void *d_lt,
 int hd_reference_distances(hd_ctx *ctx, const char *ref, uint64_t ref_len,
                            const char *fasta, uint64_t nbytes, int include_x,
                            uint32_t **out, uint64_t *n_out);
+/* The same from a FASTA file, read as in hd_alignment_from_fasta_file
+ * (reusing the device bytes of the same unchanged file). */
+int hd_reference_distances_file(hd_ctx *ctx, const char *ref, uint64_t ref_len,
+                                const char *path, int include_x, uint32_t **out,
+                                uint64_t *n_out);
 /* Same against a resident alignment: one distance per INPUT record (rows
  * expanded through the sequence indices). ref_len must equal the alignment's
  * length. Used by the serving loop. */
@@ -189,6 +205,9 @@ int hd_alignment_reference_distances(hd_ctx *ctx, const hd_alignment *aln,
 int hd_fasta_sequence_indices(hd_ctx *ctx, const char *fasta, uint64_t nbytes,
                               uint64_t n_limit, uint64_t **out,
                               uint64_t *n_out);
+/* The same from a FASTA file, read as in hd_alignment_from_fasta_file. */
+int hd_fasta_sequence_indices_file(hd_ctx *ctx, const char *path, uint64_t n_limit,
+                                   uint64_t **out, uint64_t *n_out);
 /* Replaces distance (src/hamming.cc:54-74) and distance_cuda
  * (src/distance_cuda.cu:225-230): one pair under the reference-distance rule.
  * Unequal lengths fail with HD_ERR_LENGTH. */
@@ -306,9 +325,22 @@ int hd_tune_save(hd_ctx *ctx, const char *path);
 int hd_tune_load(hd_ctx *ctx, const char *path);
 
 /* ---- measurement --------------------------------------------------------- */
+/* Phase tracing, off by default (HAMMINGDIST_TRACE=1 in the environment
+ * turns it on when a context is created). While on, hd_alignment_from_fasta,
+ * hd_pairwise_lt and hd_reference_distances record a CUDA event on the
+ * context's stream at each phase boundary (upload, parse, dedupe, consensus,
+ * pack, pairwise, copy to host, ...) and an NVTX range per call; the
+ * durations are read once when the call ends. hd_trace_last returns the text
+ * of the last traced call ("<call>: <phase> <ms> ms, ..., stream time <ms>
+ * ms"), valid until the next call on the context. Stands in for the
+ * reference's wall-clock timing lines (include/hamming/hamming_impl.hh:74-87)
+ * and its CUDA-event timers (src/distance_cuda.cu:96-99,167-178). */
+int hd_trace_enable(hd_ctx *ctx, int on);
+const char *hd_trace_last(const hd_ctx *ctx);
 /* Integer-pipe peaks of this device, measured by timing dependent LOP3 and
  * POPC chains (lane operations per second) and the pairwise inner loop's
- * instruction mix (pair-sites per second). No reference counterpart. */
+ * instruction mix from registers alone at 16 warps per SM (4 LOP3 + POPC +
+ * IMAD per 32 pair-sites; pair-sites per second). No reference counterpart. */
 int hd_measure_int_peaks(hd_ctx *ctx, double *lop3_per_s, double *popc_per_s,
                          double *mix_pair_sites_per_s);
 /* Failure-path self-test: a kernel waits, with the bounded wait of the
