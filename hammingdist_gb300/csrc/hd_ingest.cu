@@ -266,6 +266,7 @@ Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_
   rec.max_len = hs.max_len;
   rec.all_equal = hs.unequal == 0;
   rec.base = d_file;
+  rec.bytes = nbytes;
   if (hs.multi) {
     // records spanning several lines: concatenate them into one buffer
     DevBuf len(M * 8, st), dst(M * 8, st), gtot(8, st);
@@ -287,6 +288,7 @@ Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_
       scan_exclusive<uint64_t>(ctx, rec.rec_len.as<uint64_t>(), rec.rec_start.as<uint64_t>(),
                                rec.n, gtot.as<uint64_t>());
     rec.base = rec.gathered.as<uint8_t>();
+    rec.bytes = total_bytes;
   }
   return rec;
 }
@@ -304,6 +306,7 @@ Records records_from_offsets(hd_ctx *ctx, const uint8_t *d_bytes, const uint64_t
     if (len[k] != len[0]) rec.all_equal = false;
   }
   rec.len0 = n ? len[0] : 0;
+  rec.bytes = n ? h_offsets[n] - h_offsets[0] : 0;
   rec.rec_start = DevBuf(start.size() * 8, ctx->stream);
   rec.rec_len = DevBuf(len.size() * 8, ctx->stream);
   HD_CUDA(cudaMemcpyAsync(rec.rec_start.p, start.data(), start.size() * 8, cudaMemcpyHostToDevice,
@@ -325,25 +328,74 @@ __device__ inline uint64_t mix64(uint64_t x) {
 }
 
 constexpr unsigned long long kEmpty = ~0ull;
+constexpr int kHashU = 2;     // 512-byte blocks per warp per step of k_hash and k_tab_verify
+constexpr int kCmpU = 16;     // bytes per lane per step of k_refdist
+
+// 16 bytes at the 16-byte aligned address x, bytes outside the readable
+// range [lo, hi) read as 0 (byte loads only at the ends of the range).
+__device__ inline uint4 load16_in(uint64_t x, uint64_t lo, uint64_t hi) {
+  if (x >= lo && x + 16 <= hi) return *reinterpret_cast<const uint4 *>(x);
+  uint32_t w[4] = {0u, 0u, 0u, 0u};
+  for (int k = 0; k < 16; ++k)
+    if (x + k >= lo && x + k < hi)
+      w[k >> 2] |= (uint32_t)*reinterpret_cast<const uint8_t *>(x + k) << (8 * (k & 3));
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+__device__ inline uint32_t load4_in(uint64_t x, uint64_t lo, uint64_t hi) {
+  if (x >= lo && x + 4 <= hi) return *reinterpret_cast<const uint32_t *>(x);
+  uint32_t w = 0;
+  for (int k = 0; k < 4; ++k)
+    if (x + k >= lo && x + k < hi) w |= (uint32_t)*reinterpret_cast<const uint8_t *>(x + k) << (8 * k);
+  return w;
+}
 
 // Hash of each record's bytes: a sum of position-keyed 64-bit mixes of its
-// 4-byte groups (any two different records collide with probability ~2^-64;
-// equal hashes are verified byte by byte).
-__global__ void k_hash(const uint8_t *base, const uint64_t *rs, const uint64_t *rl, uint64_t R,
-                       uint64_t *out) {
+// 4-byte groups (relative to the record start; a short last group is
+// zero-filled). Any two different records collide with probability ~2^-64;
+// equal hashes are verified byte by byte. The warp reads the record with
+// aligned 16-byte loads (two 512-byte blocks per step); a lane's groups start
+// at byte P mod 4 of its words and are realigned with a funnel shift and the
+// next lane's first word.
+__global__ void k_hash(const uint8_t *base, uint64_t bytes, const uint64_t *rs, const uint64_t *rl,
+                       uint64_t R, uint64_t *out) {
   const int lane = threadIdx.x & 31;
+  const uint64_t lo = reinterpret_cast<uint64_t>(base), hi = lo + bytes;
   uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
   for (uint64_t r = wid; r < R; r += nwarps) {
-    const uint8_t *p = base + rs[r];
+    const uint64_t P = lo + rs[r];
     const uint64_t len = rl[r];
+    const uint64_t A = P & ~15ull;
+    const uint32_t h4 = (uint32_t)(P & 3);
+    const int64_t rel0 = -(int64_t)(P - A);  // position of A relative to the record
+    const uint64_t span = P + len - A;
     uint64_t h = 0;
-    for (uint64_t s = (uint64_t)lane * 4; s < len; s += 128) {
-      uint32_t w = p[s];
-      if (s + 1 < len) w |= (uint32_t)p[s + 1] << 8;
-      if (s + 2 < len) w |= (uint32_t)p[s + 2] << 16;
-      if (s + 3 < len) w |= (uint32_t)p[s + 3] << 24;
-      h += mix64(((s >> 2) << 32) ^ w ^ 0x9e3779b97f4a7c15ull);
+    for (uint64_t b0 = 0; b0 < span; b0 += 512 * kHashU) {
+      uint4 v[kHashU];
+      uint32_t nx[kHashU];
+#pragma unroll
+      for (int k = 0; k < kHashU; ++k) {
+        const uint64_t off = b0 + 512 * k + 16 * lane;
+        v[k] = off < span ? load16_in(A + off, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+        const uint64_t noff = b0 + 512 * k + 512;  // lane 31: the word after its 16 bytes
+        nx[k] = (lane == 31 && noff < span) ? load4_in(A + noff, lo, hi) : 0u;
+      }
+#pragma unroll
+      for (int k = 0; k < kHashU; ++k) {
+        uint32_t nxt = __shfl_down_sync(0xffffffffu, v[k].x, 1);
+        if (lane == 31) nxt = nx[k];
+        const uint32_t wd[5] = {v[k].x, v[k].y, v[k].z, v[k].w, nxt};
+        const int64_t lane_rel = rel0 + (int64_t)(b0 + 512 * k + 16 * lane);
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          const int64_t s = lane_rel + h4 + 4 * g;
+          if (s < 0 || s >= (int64_t)len) continue;
+          uint32_t w = __funnelshift_r(wd[g], wd[g + 1], 8 * h4);
+          const int64_t left = (int64_t)len - s;
+          if (left < 4) w &= (1u << (8 * left)) - 1u;
+          h += mix64((((uint64_t)s >> 2) << 32) ^ w ^ 0x9e3779b97f4a7c15ull);
+        }
+      }
     }
     h = warp_sum(h);
     if (lane == 0) {
@@ -374,7 +426,66 @@ __global__ void k_tab_insert(const uint64_t *hash, const uint64_t *list, uint64_
 
 // Each record against the lowest-index record of equal hash: equal bytes ->
 // duplicate; different bytes (a hash collision) -> next round.
-__global__ void k_tab_verify(const uint8_t *base, const uint64_t *rs, const uint64_t *rl,
+// Whether records a and b (equal length len, at addresses Pa and Pb inside
+// [lo, hi)) hold the same bytes; called by a whole warp, same result in every
+// lane. a is read with aligned 16-byte loads; b's bytes at the same relative
+// positions come from b's aligned loads shifted by d = (Pb - Pa) mod 16 with
+// funnel shifts over its words and the next lane's words.
+__device__ inline bool warp_equal(uint64_t Pa, uint64_t Pb, uint64_t len, uint64_t lo, uint64_t hi,
+                                  int lane) {
+  const uint64_t Aa = Pa & ~15ull;
+  const uint64_t Bs = Pb + Aa - Pa;  // b's byte at a's aligned start (may precede b)
+  const uint64_t Ab = Bs & ~15ull;
+  const uint32_t d = (uint32_t)(Bs - Ab), dw = d >> 2, db = d & 3;
+  const uint64_t span = Pa + len - Aa;
+  const int64_t rel0 = -(int64_t)(Pa - Aa);
+  bool eq = true;
+  for (uint64_t b0 = 0; b0 < span && eq; b0 += 512 * kHashU) {
+    uint32_t diff = 0;
+#pragma unroll
+    for (int k = 0; k < kHashU; ++k) {
+      const uint64_t off = b0 + 512 * k + 16 * lane;
+      const bool in = off < span;
+      const uint4 va = in ? load16_in(Aa + off, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+      // b's 16 bytes are needed while they start before b's end: the window
+      // of the lane before reaches into them when d > 0
+      const uint4 vb = Ab + off < Pb + len ? load16_in(Ab + off, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+      uint4 vn;
+      vn.x = __shfl_down_sync(0xffffffffu, vb.x, 1);
+      vn.y = __shfl_down_sync(0xffffffffu, vb.y, 1);
+      vn.z = __shfl_down_sync(0xffffffffu, vb.z, 1);
+      vn.w = __shfl_down_sync(0xffffffffu, vb.w, 1);
+      if (lane == 31)
+        vn = (d && Ab + off + 16 < Pb + len) ? load16_in(Ab + off + 16, lo, hi)
+                                              : make_uint4(0u, 0u, 0u, 0u);
+      const uint32_t bw[8] = {vb.x, vb.y, vb.z, vb.w, vn.x, vn.y, vn.z, vn.w};
+      const uint32_t aw[4] = {va.x, va.y, va.z, va.w};
+      const int64_t rel = rel0 + (int64_t)off;  // position of aw[0] relative to the records
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        uint32_t blo = bw[j], bhi = bw[j + 1];
+#pragma unroll
+        for (int t = 1; t < 4; ++t)
+          if (dw == (uint32_t)t) {
+            blo = bw[j + t];
+            bhi = bw[j + t + 1];
+          }
+        const uint32_t al = __funnelshift_r(blo, bhi, 8 * db);
+        // compare only the bytes at relative positions [0, len)
+        const int64_t s = rel + 4 * j;
+        uint32_t m = in ? 0xffffffffu : 0u;
+        if (s < 0) m &= s <= -4 ? 0u : (0xffffffffu << (8 * (uint32_t)(-s)));
+        if (s + 4 > (int64_t)len)
+          m &= s >= (int64_t)len ? 0u : (0xffffffffu >> (8 * (uint32_t)(s + 4 - (int64_t)len)));
+        diff |= (aw[j] ^ al) & m;
+      }
+    }
+    eq = !__any_sync(0xffffffffu, diff != 0);
+  }
+  return eq;
+}
+
+__global__ void k_tab_verify(const uint8_t *base, uint64_t bytes, const uint64_t *rs, const uint64_t *rl,
                              const uint64_t *hash, const uint64_t *list, uint64_t cnt,
                              const unsigned long long *keys, const unsigned long long *mins,
                              uint64_t mask, uint64_t *dup, uint64_t *next,
@@ -398,15 +509,8 @@ __global__ void k_tab_verify(const uint8_t *base, const uint64_t *rs, const uint
     }
     bool eq = rl[r] == rl[rep];
     if (eq) {
-      const uint8_t *a = base + rs[r], *b = base + rs[rep];
-      const uint64_t len = rl[r];
-      for (uint64_t s = lane; s < len; s += 32) {
-        if (__any_sync(__activemask(), a[s] != b[s])) {
-          eq = false;
-          break;
-        }
-      }
-      eq = __all_sync(0xffffffffu, eq);
+      const uint64_t lo = reinterpret_cast<uint64_t>(base);
+      eq = warp_equal(lo + rs[r], lo + rs[rep], rl[r], lo, lo + bytes, lane);
     }
     if (lane == 0) {
       if (eq) {
@@ -447,7 +551,7 @@ DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<u
   DevBuf lists[2] = {DevBuf(R * 8, st), DevBuf(R * 8, st)};
   DevBuf cnt(8, st);
   unsigned warps_grid = grid_for(R * 32, 256);
-  k_hash<<<warps_grid, 256, 0, st>>>(rec.base, rec.rec_start.as<uint64_t>(),
+  k_hash<<<warps_grid, 256, 0, st>>>(rec.base, rec.bytes, rec.rec_start.as<uint64_t>(),
                                      rec.rec_len.as<uint64_t>(), R, hash.as<uint64_t>());
   HD_LAUNCHED(ctx);
   uint64_t todo = R;
@@ -462,8 +566,8 @@ DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<u
                                                       mins.as<unsigned long long>(), T - 1);
     HD_LAUNCHED(ctx);
     k_tab_verify<<<grid_for(todo * 32, 256), 256, 0, st>>>(
-        rec.base, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(), hash.as<uint64_t>(),
-        list, todo, keys.as<unsigned long long>(), mins.as<unsigned long long>(), T - 1,
+        rec.base, rec.bytes, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(),
+        hash.as<uint64_t>(), list, todo, keys.as<unsigned long long>(), mins.as<unsigned long long>(), T - 1,
         dup.as<uint64_t>(), next, cnt.as<unsigned long long>());
     HD_LAUNCHED(ctx);
     uint64_t left = 0;
@@ -552,45 +656,66 @@ uint64_t consensus_matches(hd_ctx *ctx, const Records &rec, const uint64_t *d_ro
 }
 
 // ------------------------------------------------------------------- pack
-// One warp packs 32 words (1024 sites) of one row: each lane holds one site's
-// code, one ballot per plane collects 32 sites into a plane word, and lane i
-// keeps word i. Sites past L get the '-' code, which matches everything, so
-// padding never counts (the reference pads with '-' too, src/hamming_impl.cc:
-// 256-264).
+// Packing: a warp job is kPackCPG chunks of 32 words (1024 sites each) of
+// one row. Per chunk the warp reads the 1024 bytes with coalesced byte loads
+// (all issued before use), stages their codes in shared memory, and lane i
+// then builds word i from its 32 consecutive codes: for plane p, the p bits
+// of 4 codes (one per byte) are gathered into 4 bits by one multiply
+// ((v & 0x01010101) * 0x01020408 moves bit 8j to bit 24 + j). Sites past L
+// get the '-' code, which matches everything, so padding never counts (the
+// reference pads with '-' too, src/hamming_impl.cc:256-264).
+constexpr int kPackThreads = 256;
+constexpr int kPackCPG = 4;
 template <int P>
-__global__ void k_pack(const uint8_t *base, const uint64_t *rs, const uint64_t *rows,
-                       uint64_t n_rows, uint64_t L, uint64_t words, Table256 table, uint4 *g0,
-                       uint4 *g1) {
+__global__ void __launch_bounds__(kPackThreads)
+    k_pack(const uint8_t *base, const uint64_t *rs, const uint64_t *rows, uint64_t n_rows,
+           uint64_t L, uint64_t words, Table256 table, uint4 *g0, uint4 *g1) {
   __shared__ uint8_t tbl[256];
+  __shared__ __align__(16) uint8_t stage[kPackThreads / 32][1024 + 16];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tbl[i] = table.v[i];
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  uint8_t *sw = stage[threadIdx.x >> 5];
   const uint64_t chunks = (words + 31) / 32;
+  const uint64_t groups = (chunks + kPackCPG - 1) / kPackCPG;
   uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
-  const uint8_t pad = tbl['-'];
-  for (uint64_t job = wid; job < n_rows * chunks; job += nwarps) {
-    uint64_t u = job / chunks, q = job % chunks;
-    uint64_t r = rows ? rows[u] : u;
+  for (uint64_t job = wid; job < n_rows * groups; job += nwarps) {
+    const uint64_t u = job / groups;
+    const uint64_t q0 = (job - u * groups) * kPackCPG;
+    const uint64_t r = rows ? rows[u] : u;
     const uint8_t *src = base + rs[r];
-    uint32_t x[P];
+    for (uint64_t q = q0; q < q0 + kPackCPG && q < chunks; ++q) {
+      const uint8_t *cs = src + q * 1024;
+      const int64_t rem64 = (int64_t)L - (int64_t)(q * 1024);
+      const int rem = rem64 <= 0 ? 0 : (rem64 >= 1024 ? 1024 : (int)rem64);
+      uint8_t ch[32];
 #pragma unroll
-    for (int p = 0; p < P; ++p) x[p] = 0;
-    for (int i = 0; i < 32; ++i) {
-      uint64_t w = q * 32 + i;
-      if (w >= words) break;
-      uint64_t s = w * 32 + lane;
-      uint8_t code = s < L ? tbl[src[s]] : pad;
+      for (int i = 0; i < 32; ++i) {
+        const int s = i * 32 + lane;
+        ch[i] = s < rem ? cs[s] : (uint8_t)'-';
+      }
+#pragma unroll
+      for (int i = 0; i < 32; ++i) sw[i * 32 + lane] = tbl[ch[i]];
+      __syncwarp();
+      const uint4 c0 = *reinterpret_cast<const uint4 *>(sw + lane * 32);
+      const uint4 c1 = *reinterpret_cast<const uint4 *>(sw + lane * 32 + 16);
+      __syncwarp();  // the next chunk overwrites the staging
+      const uint32_t cw[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+      uint32_t x[6] = {0u, 0u, 0u, 0u, 0u, 0u};
 #pragma unroll
       for (int p = 0; p < P; ++p) {
-        uint32_t b = __ballot_sync(0xffffffffu, (code >> p) & 1u);
-        if (lane == i) x[p] = b;
+        uint32_t acc = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          acc |= ((((cw[k] >> p) & 0x01010101u) * 0x01020408u) >> 24 & 0xFu) << (4 * k);
+        x[p] = acc;
       }
-    }
-    uint64_t w = q * 32 + lane;
-    if (w < words) {
-      g0[u * words + w] = make_uint4(x[0], x[1], x[2], x[3]);
-      if (P > 4) g1[u * words + w] = make_uint4(x[4 % P], P > 5 ? x[5 % P] : 0u, 0u, 0u);
+      const uint64_t w = q * 32 + lane;
+      if (w < words) {
+        g0[u * words + w] = make_uint4(x[0], x[1], x[2], x[3]);
+        if (P > 4) g1[u * words + w] = make_uint4(x[4], x[5], 0u, 0u);
+      }
     }
   }
 }
@@ -604,18 +729,18 @@ void pack_rows(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, hd_align
   aln->plane_buf[0] = DevBuf(bytes ? bytes : 16, ctx->stream);
   if (aln->groups > 1) aln->plane_buf[1] = DevBuf(bytes ? bytes : 16, ctx->stream);
   if (!aln->n_rows) return;
-  uint64_t jobs = aln->n_rows * ((aln->words + 31) / 32);
-  unsigned grid = grid_for(jobs * 32, 256);
+  const uint64_t jobs = aln->n_rows * hd::ceil_div((aln->words + 31) / 32, (uint64_t)kPackCPG);
+  unsigned grid = grid_for(jobs * 32, kPackThreads);
   uint4 *g0 = aln->plane_buf[0].as<uint4>(), *g1 = aln->plane_buf[1].as<uint4>();
   const uint64_t *rs = rec.rec_start.as<uint64_t>();
   if (aln->planes == 4)
-    k_pack<4><<<grid, 256, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
+    k_pack<4><<<grid, kPackThreads, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
                                              aln->words, t, g0, g1);
   else if (aln->planes == 5)
-    k_pack<5><<<grid, 256, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
+    k_pack<5><<<grid, kPackThreads, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
                                              aln->words, t, g0, g1);
   else
-    k_pack<6><<<grid, 256, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
+    k_pack<6><<<grid, kPackThreads, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
                                              aln->words, t, g0, g1);
   HD_LAUNCHED(ctx);
 }
@@ -635,12 +760,23 @@ __global__ void k_refdist(const uint8_t *base, const uint64_t *rs, const uint64_
     const uint8_t *p = base + rs[r];
     const uint64_t len = rl[r];
     uint32_t cnt = 0;
-    for (uint64_t s = lane; s < len; s += 32) {
-      uint8_t a = p[s], b = ref[s];
-      uint8_t la = lk[a], lb = lk[b];
-      bool invalid = (la & lb) == 0;
-      bool count = invalid || (a != b && la != 0xff && lb != 0xff);
-      cnt += count ? 1u : 0u;
+    // kCmpU sites per lane per step, loaded before any is used
+    for (uint64_t s0 = lane; s0 < len; s0 += 32 * kCmpU) {
+      uint8_t av[kCmpU], bv[kCmpU];
+#pragma unroll
+      for (int k = 0; k < kCmpU; ++k) {
+        const uint64_t s = s0 + 32 * k;
+        av[k] = s < len ? p[s] : (uint8_t)'-';
+        bv[k] = s < len ? ref[s] : (uint8_t)'-';
+      }
+#pragma unroll
+      for (int k = 0; k < kCmpU; ++k) {
+        const uint8_t a = av[k], b = bv[k];
+        const uint8_t la = lk[a], lb = lk[b];
+        const bool invalid = (la & lb) == 0;
+        const bool count = invalid || (a != b && la != 0xff && lb != 0xff);
+        cnt += count ? 1u : 0u;
+      }
     }
     cnt = warp_sum(cnt);
     if (lane == 0) out[r] = cnt;
@@ -689,7 +825,8 @@ void query_distances_async(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *
   q_planes = DevBuf(aln->words * 16, ctx->stream);
   DevBuf rs(8, ctx->stream);  // record start 0, freed after the kernels in stream order
   HD_CUDA(cudaMemsetAsync(rs.p, 0, 8, ctx->stream));
-  k_pack<4><<<grid_for(((aln->words + 31) / 32) * 32, 256), 256, 0, ctx->stream>>>(
+  k_pack<4><<<grid_for(hd::ceil_div((aln->words + 31) / 32, (uint64_t)kPackCPG) * 32, kPackThreads),
+              kPackThreads, 0, ctx->stream>>>(
       d_query, rs.as<uint64_t>(), nullptr, 1, aln->length, aln->words, t, q_planes.as<uint4>(),
       nullptr);
   HD_LAUNCHED(ctx);

@@ -322,6 +322,7 @@ struct Records {
   uint64_t max_len = 0;
   bool all_equal = true;
   const uint8_t *base = nullptr;
+  uint64_t bytes = 0;         // readable bytes from base: [base, base + bytes)
   DevBuf rec_start, rec_len;  // uint64 [n]
   DevBuf gathered;            // concatenation when records span several lines
 };
