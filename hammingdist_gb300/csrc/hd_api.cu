@@ -235,6 +235,24 @@ const uint8_t *stage_file(hd_ctx *ctx, const char *path, uint64_t *nbytes) {
   return dev;
 }
 
+// Writes zeros over a large host output on up to 16 threads: the first touch
+// of fresh pageable pages costs several ms per 100 MB on one thread. Called
+// after the kernel is launched, so it runs while the GPU computes and the copy
+// back then finds the pages present.
+void prefault_host(void *p, uint64_t n) {
+  const uint64_t kMin = 16ull << 20, kPart = 4ull << 20;
+  if (n < kMin) return;
+  const unsigned nt = (unsigned)std::min<uint64_t>(16, n / kPart);
+  const uint64_t per = hd::ceil_div(n, nt);
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nt; ++t)
+    th.emplace_back([=] {
+      const uint64_t a = t * per, b = std::min(n, a + per);
+      if (a < b) std::memset(static_cast<char *>(p) + a, 0, b - a);
+    });
+  for (auto &x : th) x.join();
+}
+
 uint64_t words_for(uint64_t L) { return hd::round_up(hd::ceil_div(L ? L : 1, 32), 8); }
 
 // validate_data (src/hamming_impl.cc:80-91) + the include_x/use_gpu check
@@ -649,6 +667,7 @@ int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, int64_
     HD_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
     hd::trace_mark(ctx, "pairwise");
     if (!out_on_device) {
+      prefault_host(out, entries * dtype_bytes);  // while the kernel runs
       HD_CUDA(cudaMemcpyAsync(out, d_out, entries * dtype_bytes, cudaMemcpyDeviceToHost, ctx->stream));
       hd::trace_mark(ctx, "copy to host");
     }

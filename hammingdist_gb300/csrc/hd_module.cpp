@@ -222,8 +222,8 @@ DataSet<T> compute(hd_alignment *aln, int64_t max_distance, bool announce, const
   check(hd_alignment_info(aln, &n_rows, &L, &n_in, &rule));
   ds.nsamples = n_rows;
   const auto ta = std::chrono::steady_clock::now();
+  // left uninitialised: hd_pairwise_lt touches the pages while the kernel runs
   ds.result.resize(n_rows < 2 ? 0 : n_rows * (n_rows - 1) / 2);
-  zero_parallel(ds.result.data(), ds.result.size() * sizeof(T));
   say_host("result allocation", ms_since(ta));
   if (announce) {
     say(std::string("Using GPU (") + what +

@@ -132,7 +132,9 @@ void hd_alignment_free(hd_alignment *aln);
  * 4 = uint32). max_distance is clamped like safe_int_cast
  * (include/hamming/hamming_impl.hh:37-45): above the dtype maximum it
  * saturates, negative values wrap. `out` is host memory (out_on_device = 0)
- * or device memory (1). */
+ * or device memory (1). A host output of 16 MB or more need not have been
+ * touched: its pages are first written (zeros) on up to 16 threads while
+ * the kernel runs, then the results are copied in. */
 int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes,
                    int64_t max_distance, void *out, int out_on_device);
 
