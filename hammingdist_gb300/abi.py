@@ -74,6 +74,7 @@ SIGNATURES = {
     "hd_tune_lookup": (ci, [vp, u64, u64, ci, P(ci), P(ci)]),
     "hd_tune_save": (ci, [vp, cp]),
     "hd_tune_load": (ci, [vp, cp]),
+    "hd_pairwise_lt_files": (ci, [vp, u64, vp, ci, u64, ci, ci, vp, vp, vp, vp, vp]),
     "hd_trace_enable": (ci, [vp, ctypes.c_int]),
     "hd_trace_last": (ctypes.c_char_p, [vp]),
     "hd_measure_int_peaks": (ci, [vp, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
@@ -96,6 +97,11 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+# void *(*hd_output_fn)(void *user, uint64_t index, uint64_t n_rows, uint64_t entries)
+OUTPUT_FN = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
+                             ctypes.c_uint64)
 
 
 class HDError(RuntimeError):
@@ -359,6 +365,40 @@ class Context:
         self._check(lib().hd_selftest_wait_timeout(self.h, limit_ns, ctypes.byref(st),
                                                    ctypes.byref(ms)))
         return st.value, ms.value
+
+    def pairwise_lt_files(self, paths, dtypes=None, max_distances=None, remove_duplicates=False,
+                          n=0, include_x=False, semantics=SEM_GPU):
+        """Lower triangles of many FASTA files through the pipelined file
+        batch (hd_pairwise_lt_files). Returns (list of arrays, list of
+        sequence-index arrays)."""
+        k = len(paths)
+        dtypes = [np.dtype(d if d is not None else np.uint8) for d in (dtypes or [None] * k)]
+        mds = max_distances or [np.iinfo(d).max for d in dtypes]
+        outs = [None] * k
+
+        @OUTPUT_FN
+        def alloc(user, index, n_rows, entries):
+            arr = np.empty(max(int(entries), 1), dtype=dtypes[index])
+            outs[index] = arr[: int(entries)]
+            return arr.ctypes.data
+
+        raw = [os.fsencode(p) for p in paths]
+        c_paths = (ctypes.c_char_p * k)(*raw)
+        c_dt = (ctypes.c_int * k)(*[d.itemsize for d in dtypes])
+        c_md = (ctypes.c_int64 * k)(*[int(m) for m in mds])
+        handles = (vp * k)()
+        self._check(lib().hd_pairwise_lt_files(self.h, k, ctypes.cast(c_paths, vp),
+                                               int(remove_duplicates), n, int(include_x),
+                                               semantics, ctypes.cast(c_dt, vp),
+                                               ctypes.cast(c_md, vp),
+                                               ctypes.cast(alloc, vp), None,
+                                               ctypes.cast(handles, vp)))
+        idx = []
+        for h in handles:
+            a = Alignment(self, h)
+            idx.append(a.sequence_indices())
+            a.free()
+        return outs, idx
 
     def trace(self, on=True):
         """Turns per-phase tracing of this context's calls on or off."""

@@ -6,6 +6,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <mutex>
 #include <cstdio>
 #include <cstdlib>
@@ -1118,6 +1121,338 @@ int hd_alignments_from_fasta_files(hd_ctx *ctx, uint64_t count, const char *cons
       hd_alignment_free(out[i]);
       out[i] = nullptr;
     }
+  return rc;
+}
+
+
+int hd_pairwise_lt_files(hd_ctx *ctx, uint64_t count, const char *const *paths,
+                         int remove_duplicates, uint64_t n_limit, int include_x, int semantics,
+                         const int *dtype_bytes, const int64_t *max_distance, hd_output_fn out_fn,
+                         void *user, hd_alignment **alns) {
+  if (!ctx || (count && (!paths || !dtype_bytes || !max_distance || !out_fn))) return HD_ERR_ARG;
+  if (alns)
+    for (uint64_t i = 0; i < count; ++i) alns[i] = nullptr;
+  std::vector<hd_alignment *> A(count, nullptr);
+  int rc = guard(ctx, [&] {
+    std::vector<uint32_t> md(count);
+    for (uint64_t i = 0; i < count; ++i) {
+      check_dtype(dtype_bytes[i]);
+      md[i] = clamp_max(max_distance[i], dtype_bytes[i]);
+    }
+    // one pinned arena slice per file (grown once, then reused)
+    std::vector<uint64_t> size(count), off(count + 1, 0);
+    for (uint64_t i = 0; i < count; ++i) {
+      struct stat sb;
+      if (!paths[i] || ::stat(paths[i], &sb) != 0 || !S_ISREG(sb.st_mode))
+        fail(HD_ERR_IO, open_failed(paths[i]));
+      size[i] = (uint64_t)sb.st_size;
+      off[i + 1] = off[i] + hd::round_up(size[i] + 1, 256);
+    }
+    if (off[count] > ctx->pin_cap) {
+      if (ctx->pin) cudaFreeHost(ctx->pin);
+      ctx->pin = nullptr;
+      ctx->pin_cap = 0;
+      const size_t cap = (size_t)(off[count] * 5 / 4 + (1 << 20));
+      HD_CUDA(cudaHostAlloc(&ctx->pin, cap, cudaHostAllocDefault));
+      ctx->pin_cap = cap;
+    }
+    ctx->file_tag.clear();
+    char *arena = static_cast<char *>(ctx->pin);
+    // host threads: readers copy from the page cache and ingest workers spin
+    // while they wait for their streams, so together they stay within the
+    // cores (half read, 3/8 ingest; 8 and 6 on 16 cores)
+    const unsigned hw = std::max(4u, std::thread::hardware_concurrency());
+    const size_t n_workers = (size_t)std::min<uint64_t>(count, std::min(12u, std::max(2u, hw * 3 / 8)));
+    const unsigned max_readers = std::min(16u, std::max(2u, hw / 2));
+    while (ctx->workers.size() < n_workers) {
+      hd_ctx *w = nullptr;
+      const int r = hd_ctx_create(ctx->device, &w);
+      if (r != HD_OK) fail(r, "could not create a worker context");
+      ctx->workers.push_back(w);
+    }
+    std::vector<uint64_t> launches0;
+    for (hd_ctx *w : ctx->workers) {
+      w->tune = ctx->tune;
+      launches0.push_back(w->launches);
+    }
+
+    // timeline for the trace (host ms since the start of the call)
+    const auto t_start = std::chrono::steady_clock::now();
+    auto now_ms = [&] {
+      return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start)
+          .count();
+    };
+    double t_read_end = 0, t_ingest_end = 0;
+    struct GroupLog {
+      double launch, done;
+      size_t jobs;
+      uint64_t tiles;
+    };
+    std::vector<GroupLog> glog;
+    // shared state of the pipeline
+    std::mutex mu;
+    std::condition_variable cv;
+    std::vector<char> read_done(count, 0);
+    std::deque<uint64_t> ready;  // ingested, not yet launched
+    uint64_t ingested = 0;
+    int err = HD_OK;
+    std::string err_msg;
+    auto set_err = [&](int code, const std::string &m) {
+      std::lock_guard<std::mutex> lk(mu);
+      if (err == HD_OK) {
+        err = code;
+        err_msg = m;
+      }
+      cv.notify_all();
+    };
+    auto failed = [&] {
+      std::lock_guard<std::mutex> lk(mu);
+      return err != HD_OK;
+    };
+
+    // largest files first: their matrices cost the most (~ rows^2), so their
+    // kernels start early and the small ones fill in behind them
+    std::vector<uint64_t> order(count);
+    for (uint64_t i = 0; i < count; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint64_t a, uint64_t b) { return size[a] > size[b]; });
+    // readers: 8 MB parts of the files in that order, shared by all reader
+    // threads, never waiting for the GPU; a file is read when its last part is
+    std::vector<int> fds(count, -1);
+    for (uint64_t i = 0; i < count; ++i) {
+      fds[i] = ::open(paths[i], O_RDONLY);
+      if (fds[i] < 0) {
+        for (uint64_t j = 0; j < i; ++j) ::close(fds[j]);
+        fail(HD_ERR_IO, open_failed(paths[i]));
+      }
+    }
+    struct Part {
+      uint64_t file, off, len;
+    };
+    const uint64_t kPart = 8ull << 20;
+    std::vector<Part> parts;
+    std::vector<std::atomic<uint64_t>> parts_left(count);
+    for (uint64_t q = 0; q < count; ++q) {
+      const uint64_t i = order[q];
+      uint64_t np = 0;
+      for (uint64_t o = 0; o < size[i]; o += kPart, ++np) parts.push_back({i, o, std::min(kPart, size[i] - o)});
+      if (size[i] == 0) {
+        parts.push_back({i, 0, 0});
+        np = 1;
+      }
+      parts_left[i] = np;
+    }
+    std::atomic<uint64_t> next_part{0};
+    auto reader = [&] {
+      for (uint64_t k = next_part++; k < parts.size() && !failed(); k = next_part++) {
+        const Part &pt = parts[k];
+        bool ok = true;
+        for (uint64_t o = 0; ok && o < pt.len;) {
+          const ssize_t r = ::pread(fds[pt.file], arena + off[pt.file] + pt.off + o,
+                                    (size_t)(pt.len - o), (off_t)(pt.off + o));
+          if (r <= 0) ok = false;
+          else o += (uint64_t)r;
+        }
+        if (!ok) {
+          set_err(HD_ERR_IO, open_failed(paths[pt.file]));
+          return;
+        }
+        if (parts_left[pt.file].fetch_sub(1) == 1) {
+          std::lock_guard<std::mutex> lk(mu);
+          read_done[pt.file] = 1;
+          t_read_end = std::max(t_read_end, now_ms());
+          cv.notify_all();
+        }
+      }
+    };
+    // ingest workers: each file once it is read, on the worker's own stream
+    std::atomic<uint64_t> next_ingest{0};
+    auto ingester = [&](hd_ctx *w) {
+      for (uint64_t q = next_ingest++; q < count; q = next_ingest++) {
+        const uint64_t i = order[q];
+        {
+          std::unique_lock<std::mutex> lk(mu);
+          cv.wait(lk, [&] { return read_done[i] || err != HD_OK; });
+          if (err != HD_OK) return;
+        }
+        hd_alignment *a = nullptr;
+        const int r = hd_alignment_from_fasta(w, arena + off[i], size[i], 0, remove_duplicates,
+                                              n_limit, include_x, semantics, &a);
+        if (r != HD_OK) {
+          set_err(r, std::string(hd_last_error(w)) + " (input " + std::to_string(i) + ")");
+          return;
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        A[i] = a;
+        ready.push_back(i);
+        ++ingested;
+        t_ingest_end = std::max(t_ingest_end, now_ms());
+        cv.notify_all();
+      }
+    };
+
+    // a launched group: its kernels' event, job tables and device outputs
+    struct Group {
+      size_t log = 0;  // index in glog
+      cudaEvent_t done = nullptr;
+      hd::PairLaunchPlan plan;
+      std::vector<DevBuf> dev;
+      std::vector<void *> host;
+      std::vector<uint64_t> bytes;
+    };
+    std::deque<std::unique_ptr<Group>> to_copy;
+    bool launcher_done = false;
+    // completion: copies each finished group to its host outputs in order
+    auto completer = [&] {
+      if (cudaSetDevice(ctx->device) != cudaSuccess) {
+        set_err(HD_ERR_CUDA, "cudaSetDevice failed");
+        return;
+      }
+      for (;;) {
+        std::unique_ptr<Group> g;
+        {
+          std::unique_lock<std::mutex> lk(mu);
+          cv.wait(lk, [&] { return !to_copy.empty() || launcher_done; });
+          if (to_copy.empty()) return;
+          g = std::move(to_copy.front());
+          to_copy.pop_front();
+        }
+        bool ok = cudaEventSynchronize(g->done) == cudaSuccess;
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          glog[g->log].done = now_ms();
+        }
+        for (size_t j = 0; ok && j < g->dev.size(); ++j) {
+          prefault_host(g->host[j], g->bytes[j]);
+          ok = cudaMemcpyAsync(g->host[j], g->dev[j].p, g->bytes[j], cudaMemcpyDeviceToHost,
+                               ctx->side) == cudaSuccess &&
+               cudaStreamSynchronize(ctx->side) == cudaSuccess;
+        }
+        cudaEventDestroy(g->done);
+        if (!ok) set_err(HD_ERR_CUDA, "copying results to the host failed");
+        // g's device buffers and job tables are freed here, after their last use
+      }
+    };
+
+    std::vector<std::thread> threads;
+    const unsigned n_readers = (unsigned)std::min<uint64_t>(parts.size(), max_readers);
+    for (unsigned t = 0; t < n_readers; ++t) threads.emplace_back(reader);
+    for (size_t t = 0; t < n_workers; ++t) threads.emplace_back(ingester, ctx->workers[t]);
+    std::thread completion(completer);
+
+    // launcher (this thread): whenever the previous group's kernels are done,
+    // every ingested alignment not yet computed goes into one persistent launch
+    uint64_t launched = 0, tiles = 0;
+    // the launcher's own event, re-recorded after each group: the GPU is idle
+    // when it has completed (the groups' events belong to the completer)
+    cudaEvent_t last = nullptr;
+    bool any = false;
+    HD_CUDA(cudaEventCreateWithFlags(&last, cudaEventDisableTiming));
+    try {
+      while (launched < count) {
+        std::vector<uint64_t> take;
+        {
+          std::unique_lock<std::mutex> lk(mu);
+          for (;;) {
+            if (err != HD_OK) break;
+            const bool idle = !any || cudaEventQuery(last) == cudaSuccess;
+            if (!ready.empty() && (idle || ingested == count)) break;
+            cv.wait_for(lk, std::chrono::microseconds(100));
+          }
+          if (err != HD_OK) break;
+          take.assign(ready.begin(), ready.end());
+          ready.clear();
+        }
+        auto g = std::make_unique<Group>();
+        std::vector<hd::PairJobSpec> specs;
+        for (uint64_t i : take) {
+          const hd_alignment *a = A[i];
+          const uint64_t entries = a->n_rows < 2 ? 0 : tri(a->n_rows);
+          void *host = out_fn(user, i, a->n_rows, entries);
+          if (!host && entries) fail(HD_ERR_ARG, "output callback returned no buffer");
+          if (!entries) continue;
+          g->dev.emplace_back(entries * dtype_bytes[i], ctx->stream);
+          g->host.push_back(host);
+          g->bytes.push_back(entries * dtype_bytes[i]);
+          hd::PairJobSpec sp;
+          sp.aln = a;
+          sp.dtype = dtype_bytes[i];
+          sp.max_dist = md[i];
+          sp.d_out = g->dev.back().p;
+          sp.out_base = 0;
+          sp.cfg = hd::tile_config_for(ctx, a->n_rows, a->length, dtype_bytes[i]);
+          sp.tile_lo = 0;
+          sp.tile_hi = (uint32_t)hd::ceil_div(a->n_rows, sp.cfg.tile);
+          specs.push_back(sp);
+        }
+        launched += take.size();
+        uint64_t g_tiles = 0;
+        if (!specs.empty()) {
+          // while files are still being ingested, 16 SMs stay free for their
+          // kernels (a persistent grid holds its SMs until it ends)
+          bool pending;
+          {
+            std::lock_guard<std::mutex> lk(mu);
+            pending = ingested < count;
+          }
+          hd::prepare_pairwise_jobs(ctx, specs, ctx->stream, &g->plan,
+                                    pending ? std::max(1, ctx->sm_count - 16) : 0);
+          hd::launch_pairwise_plan(ctx, g->plan, ctx->stream);
+          for (auto &L : g->plan.launches) g_tiles += L.tiles;
+          tiles += g_tiles;
+        }
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          g->log = glog.size();
+          glog.push_back({now_ms(), 0.0, specs.size(), g_tiles});
+        }
+        HD_CUDA(cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming));
+        HD_CUDA(cudaEventRecord(g->done, ctx->stream));
+        HD_CUDA(cudaEventRecord(last, ctx->stream));
+        any = true;
+        std::lock_guard<std::mutex> lk(mu);
+        to_copy.push_back(std::move(g));
+        cv.notify_all();
+      }
+    } catch (const hd::Error &e) {
+      set_err(e.code, e.msg);
+    }
+    for (auto &t : threads) t.join();
+    for (int fd : fds) ::close(fd);
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      launcher_done = true;
+      cv.notify_all();
+    }
+    completion.join();
+    cudaEventDestroy(last);
+    for (size_t t = 0; t < ctx->workers.size() && t < launches0.size(); ++t)
+      ctx->launches += ctx->workers[t]->launches - launches0[t];
+    ctx->last_pair_tiles = tiles;
+    if (err != HD_OK) fail(err, err_msg);
+    HD_CUDA(cudaStreamSynchronize(ctx->stream));
+    check_status(ctx);
+    if (ctx->trace.on) {
+      char buf[160];
+      std::snprintf(buf, sizeof buf,
+                    "hd_pairwise_lt_files: %llu files read by %.3f ms, ingested by %.3f ms, "
+                    "%zu groups:",
+                    (unsigned long long)count, t_read_end, t_ingest_end, glog.size());
+      std::string text = buf;
+      for (const auto &g : glog) {
+        std::snprintf(buf, sizeof buf, " [%.3f-%.3f ms, %zu jobs, %llu tiles]", g.launch, g.done,
+                      g.jobs, (unsigned long long)g.tiles);
+        text += buf;
+      }
+      std::snprintf(buf, sizeof buf, ", done at %.3f ms", now_ms());
+      text += buf;
+      ctx->trace.last = text;
+    }
+  });
+  for (uint64_t i = 0; i < count; ++i) {
+    if (rc == HD_OK && alns) alns[i] = A[i];
+    else hd_alignment_free(A[i]);
+  }
   return rc;
 }
 

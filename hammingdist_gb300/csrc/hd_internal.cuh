@@ -388,7 +388,8 @@ struct PairLaunchPlan {
   std::vector<DevBuf> blocks;  // job tables + tensor maps + tile counters
 };
 void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStream_t stream,
-                           PairLaunchPlan *plan);
+                           PairLaunchPlan *plan,
+                           int sm_limit = 0);
 void launch_pairwise_plan(hd_ctx *ctx, PairLaunchPlan &plan, cudaStream_t stream);
 void run_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStream_t stream,
                        PairLaunchPlan *keep);

@@ -321,46 +321,48 @@ py::list from_fasta_batch(const std::vector<std::string> &files, bool include_x,
   std::vector<hd_alignment *> alns(k, nullptr);
   std::vector<DataSet<uint8_t>> small(k);
   std::vector<DataSet<uint16_t>> wide(k);
+  std::vector<int> dtype(k);
+  for (size_t i = 0; i < k; ++i) dtype[i] = big[i] ? 2 : 1;
+  struct Out {
+    std::vector<int> *big;
+    std::vector<DataSet<uint8_t>> *small;
+    std::vector<DataSet<uint16_t>> *wide;
+  } o{&big, &small, &wide};
+  // sizes each result when its row count is known (distinct indices only)
+  hd_output_fn alloc = [](void *user, uint64_t i, uint64_t rows, uint64_t entries) -> void * {
+    Out *q = static_cast<Out *>(user);
+    if ((*q->big)[i]) {
+      auto &d = (*q->wide)[i];
+      d.nsamples = rows;
+      d.result.resize(entries);
+      return d.result.data();
+    }
+    auto &d = (*q->small)[i];
+    d.nsamples = rows;
+    d.result.resize(entries);
+    return d.result.data();
+  };
   {
     py::gil_scoped_release nogil;
     auto t1 = std::chrono::steady_clock::now();
-    check(hd_alignments_from_fasta_files(c, k, paths.data(), remove_duplicates, n, include_x,
-                                         use_gpu ? HD_SEM_GPU : HD_SEM_CPU, alns.data()));
-    const double t_ingest = ms_since(t1);
+    check(hd_pairwise_lt_files(c, k, paths.data(), remove_duplicates, n, include_x,
+                               use_gpu ? HD_SEM_GPU : HD_SEM_CPU, dtype.data(), md.data(), alloc, &o,
+                               alns.data()));
     std::vector<Aln> own(k);
     for (size_t i = 0; i < k; ++i) own[i].p = alns[i];
-    hd_batch *b = nullptr;
-    check(hd_batch_create(c, &b));
-    std::unique_ptr<hd_batch, void (*)(hd_batch *)> bguard(b, hd_batch_free);
     for (size_t i = 0; i < k; ++i) {
-      uint64_t rows = 0, n_in = 0;
-      check(hd_alignment_info(alns[i], &rows, nullptr, &n_in, nullptr));
-      const uint64_t e = rows < 2 ? 0 : rows * (rows - 1) / 2;
-      if (big[i]) {
-        wide[i].nsamples = rows;
-        wide[i].result.resize(e);
-        check(hd_batch_add(b, alns[i], 2, md[i], wide[i].result.data(), 0));
-      } else {
-        small[i].nsamples = rows;
-        small[i].result.resize(e);
-        check(hd_batch_add(b, alns[i], 1, md[i], small[i].result.data(), 0));
-      }
-      if (remove_duplicates) {
-        auto &idx = big[i] ? wide[i].sequence_indices : small[i].sequence_indices;
-        idx.resize(n_in);
-        check(hd_alignment_sequence_indices(alns[i], idx.data()));
-      }
+      if (!remove_duplicates) continue;
+      uint64_t n_in = 0;
+      check(hd_alignment_info(alns[i], nullptr, nullptr, &n_in, nullptr));
+      auto &idx = big[i] ? wide[i].sequence_indices : small[i].sequence_indices;
+      idx.resize(n_in);
+      check(hd_alignment_sequence_indices(alns[i], idx.data()));
     }
-    auto t2 = std::chrono::steady_clock::now();
-    check(hd_batch_run(b));
-    double graph_ms = 0;
-    uint64_t launches = 0, tiles = 0;
-    hd_batch_timing(b, &graph_ms, &launches, &tiles);
-    say("batch of " + std::to_string(k) + " alignments: read + ingest " +
-        std::to_string(t_ingest) + " ms, distances " +
-        std::to_string(ms_since(t2)) + " ms (" + std::to_string(launches) +
-        " persistent launches, " + std::to_string(tiles) + " tiles, device " +
-        std::to_string(graph_ms) + " ms).");
+    double pair_ms = 0;
+    uint64_t tiles = 0;
+    hd_last_pairwise_timing(c, &pair_ms, &tiles);
+    say("batch of " + std::to_string(k) + " alignments: read, ingest and distances pipelined in " +
+        std::to_string(ms_since(t1)) + " ms (" + std::to_string(tiles) + " tiles).");
   }
   py::list out;
   for (size_t i = 0; i < k; ++i) {

@@ -357,7 +357,7 @@ bool tile_config_valid(int tile, int stages) {
 // launch_pairwise_plan issues them. Outside a graph the two run back to back;
 // a batch captures only the launch step and replays it.
 void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStream_t stream,
-                           PairLaunchPlan *plan) {
+                           PairLaunchPlan *plan, int sm_limit) {
   struct Group {
     const Variant *v;
     std::vector<size_t> idx;
@@ -426,7 +426,9 @@ void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStr
     L.d_jobs = dev.as<uint8_t>() + tm_bytes;
     L.d_counter = reinterpret_cast<unsigned long long *>(dev.as<uint8_t>() + tm_bytes + job_bytes);
     const int per_sm = resident_ctas(v);
-    L.grid = std::min<uint64_t>(tiles, (uint64_t)per_sm * ctx->sm_count);
+    // sm_limit > 0 leaves the other SMs to kernels of other streams
+    const int sms = sm_limit > 0 && sm_limit < ctx->sm_count ? sm_limit : ctx->sm_count;
+    L.grid = std::min<uint64_t>(tiles, (uint64_t)per_sm * sms);
     plan->launches.push_back(L);
     plan->blocks.push_back(std::move(dev));
   }

@@ -255,6 +255,32 @@ int hd_alignments_from_fasta_files(hd_ctx *ctx, uint64_t count,
                                    int include_x, int semantics,
                                    hd_alignment **out);
 
+/* Output buffers of hd_pairwise_lt_files: called once per file, from a
+ * library thread, when the file's unique row count is known; returns the
+ * host buffer for its `entries` = n_rows(n_rows-1)/2 values (of that file's
+ * dtype_bytes). It need not be touched yet. NULL with entries > 0 fails the
+ * call with HD_ERR_ARG. Calls for different indices may run concurrently. */
+typedef void *(*hd_output_fn)(void *user, uint64_t index, uint64_t n_rows, uint64_t entries);
+
+/* Many FASTA files to their lower triangles in one pipelined call (no
+ * reference counterpart: the reference computes one matrix per call, as in
+ * from_fasta, include/hamming/hamming.hh:169-177).
+ * - Reader threads read the files into pinned memory without waiting for
+ *   the GPU.
+ * - Worker contexts ingest each file as soon as it is read, on their own
+ *   streams.
+ * - Whenever the context's stream is idle, every ingested alignment not yet
+ *   computed goes into one persistent pairwise launch.
+ * - A completion thread copies each finished group to its host outputs
+ *   while later files are still being read.
+ * dtype_bytes[i] and max_distance[i] apply to file i as in hd_pairwise_lt.
+ * alns (optional, count entries) receives the alignments, e.g. for their
+ * sequence indices; free them with hd_alignment_free. */
+int hd_pairwise_lt_files(hd_ctx *ctx, uint64_t count, const char *const *paths,
+                         int remove_duplicates, uint64_t n_limit, int include_x, int semantics,
+                         const int *dtype_bytes, const int64_t *max_distance,
+                         hd_output_fn out_fn, void *user, hd_alignment **alns);
+
 /* A view of rows [row0, row0 + n_rows) of an alignment, usable wherever an
  * alignment is (pairwise, batches, serving). It borrows the base's device
  * memory: free the view before the base. No reference counterpart. */

@@ -146,3 +146,40 @@ def test_from_fasta_batch_matches_per_file_calls(tmp_path):
     bad = write(tmp_path, "bad.fasta", b">a\nACGT\n>b\nAC\n")
     with pytest.raises(RuntimeError, match="same length"):
         hd.from_fasta_batch(files[:2] + [bad])
+
+
+def test_pipelined_file_batch_abi(ctx, tmp_path):
+    # many files of uneven size, some tiny (0 or 1 row after dedupe), through
+    # hd_pairwise_lt_files: every matrix and every sequence index vs the oracle
+    rng = np.random.default_rng(21)
+    paths, dts, mds, fastas = [], [], [], []
+    for k in range(40):
+        n = int(np.exp(rng.uniform(np.log(1), np.log(1500))))
+        L = int(rng.choice([1, 33, 1000, 5000]))
+        rows, _, _ = synth.alignment(n, L, p=float(rng.uniform(1e-4, 1e-2)), seed=300 + k,
+                                     dup_frac=0.25, dash_max=min(200, L // 4))
+        fa = synth.to_fasta(rows)
+        paths.append(write(tmp_path, f"p{k}.fasta", fa))
+        fastas.append(fa)
+        big = k % 4 == 0
+        dts.append(np.uint16 if big else np.uint8)
+        mds.append(int(rng.integers(0, 300)) if not big else 65535)
+    outs, idx = ctx.pairwise_lt_files(paths, dtypes=dts, max_distances=mds, remove_duplicates=True)
+    for fa, out, ix, dt, md in zip(fastas, outs, idx, dts, mds):
+        want, want_idx = o.from_fasta_dense(fa, remove_duplicates=True, max_distance=md, dtype=dt)
+        np.testing.assert_array_equal(out, want)
+        np.testing.assert_array_equal(ix, want_idx)
+
+
+def test_pipelined_file_batch_errors(ctx, tmp_path):
+    from hammingdist_gb300 import abi
+
+    good = write(tmp_path, "g.fasta", b">a\nACGT\n>b\nACGA\n")
+    with pytest.raises(abi.HDError, match="Failed to open file"):
+        ctx.pairwise_lt_files([good, str(tmp_path / "nope.fasta"), good])
+    bad = write(tmp_path, "bad2.fasta", b">a\nACGT\n>b\nAC\n")
+    with pytest.raises(abi.HDError, match="same length"):
+        ctx.pairwise_lt_files([good] * 5 + [bad] + [good] * 5)
+    # the context stays usable
+    outs, _ = ctx.pairwise_lt_files([good, good])
+    assert [list(x) for x in outs] == [[1], [1]]
