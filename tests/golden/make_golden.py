@@ -278,7 +278,107 @@ for name, fa in PARSE.items():
         put(f"parse/{name}/seqidx_n{nlim}", np.asarray(ref.fasta_sequence_indices(path, nlim)))
     meta["parse"].append(entry)
 
-# lower-triangular file of the reference's python test (3 sequences, LT text)
+# ------------------------------------------------------- result file formats
+# dump() (full matrix text, include/hamming/hamming.hh:63-73) of DataSets built
+# from some of the alignments above; from_lower_triangular[_large]
+# (hamming.hh:152-166) and from_csv (hamming.hh:34-55) on valid files and on
+# malformed ones, with the exception the reference raises.
+def describe(ds):
+    """lt_array and the dump() text (which shows nsamples) of a reference DataSet."""
+    f = os.path.join(TMP, "describe.txt")
+    ds.dump(f)
+    return np.asarray(ds.lt_array), open(f, "rb").read()
+
+
+def try_load(fn, data: bytes):
+    path = os.path.join(TMP, "load.txt")
+    with open(path, "wb") as f:
+        f.write(data)
+    try:
+        ds = fn(path)
+    except Exception as e:  # noqa: BLE001  (the reference's own exception)
+        return {"error_type": type(e).__name__, "error": str(e)}
+    lt, text = describe(ds)
+    return {"lt": lt, "dump": text}
+
+
+meta["formats"] = {"dump": [], "lt": [], "csv": []}
+by_name = {name: rows for name, rows, _, _ in ALIGNMENTS}
+for name in ("uniform5", "dups", "covid_small", "len1", "len33", "wide", "uniform_invalid"):
+    path = write_fasta_bytes(fasta_of(by_name[name]))
+    for large in (0, 1):
+        r = run_from_fasta(path, bool(large))
+        f = os.path.join(TMP, "dump.txt")
+        r["ds"].dump(f)
+        put(f"fmt/dump/{name}{large}", np.frombuffer(open(f, "rb").read(), dtype=np.uint8))
+        meta["formats"]["dump"].append({"name": name, "large": large})
+
+LT_CASES = {
+    "basic": b"1\n2,3\n",
+    "no_final_newline": b"1\n2,3",
+    "crlf": b"1\r\n2,3\r\n",
+    "spaces": b" 1\n\t2, 3\n",
+    "signs": b"+1\n-2,3\n",
+    "saturate": b"300\n70000,5\n",
+    "negative_wrap": b"-1\n-300,-70000\n",
+    "trailing_comma": b"1\n2,3,\n",
+    "empty_line": b"1\n\n2,3\n",
+    "letters": b"1\n2,x\n",
+    "out_of_range": b"1\n99999999999,3\n",
+    "digits_then_text": b"12abc\n3,4z\n",
+    "empty_file": b"",
+    "only_newline": b"\n",
+    "non_triangular4": b"1,2,3,4\n",
+    "non_triangular7": b"1,2\n3,4,5\n6,7\n",
+    "single": b"5\n",
+    "leading_zeros": b"0007\n00,010\n",
+    "sign_only": b"1\n+,3\n",
+    "space_only": b"1\n ,3\n",
+    "big_negative": b"1\n-99999999999,3\n",
+    "int_max": b"2147483647\n-2147483648,0\n",
+}
+for key in ("dups", "covid_small", "wide"):
+    LT_CASES[f"lttext_{key}"] = bytes(arrays[f"aln/{key}/lttext1"])
+for cname, data in LT_CASES.items():
+    put(f"fmt/lt/{cname}/input", np.frombuffer(data, dtype=np.uint8))
+    entry = {"name": cname}
+    for large, fn in ((0, ref.from_lower_triangular), (1, ref.from_lower_triangular_large)):
+        res = try_load(fn, data)
+        if "error" in res:
+            entry[f"error{large}"] = [res["error_type"], res["error"]]
+        else:
+            put(f"fmt/lt/{cname}/lt{large}", res["lt"])
+            put(f"fmt/lt/{cname}/dump{large}", np.frombuffer(res["dump"], dtype=np.uint8))
+    meta["formats"]["lt"].append(entry)
+
+CSV_CASES = {
+    "two": b"0, 1\n1, 0\n",
+    "one": b"0\n",
+    "no_final_newline": b"0, 1\n1, 0",
+    "wrap": b"0, 300\n300, 0\n",
+    "negative": b"0, -1\n-1, 0\n",
+    "short_row": b"0, 5\n\n",
+    "extra_fields": b"9, 9, 9\n1, 9, 9\n2, 3, 9\n",
+    "letters": b"a, b\nc, d\n",
+    "row0_garbage": b"zz\n4, 0\n",
+    "crlf": b"0, 1\r\n1, 0\r\n",
+    "empty_file": b"",
+    "too_few_in_row2": b"0\n1\n2\n",
+    "out_of_range": b"0\n99999999999, 0\n",
+}
+for key in ("dups", "uniform5"):
+    CSV_CASES[f"dump_{key}"] = bytes(arrays[f"fmt/dump/{key}0"])
+for cname, data in CSV_CASES.items():
+    put(f"fmt/csv/{cname}/input", np.frombuffer(data, dtype=np.uint8))
+    entry = {"name": cname}
+    res = try_load(ref.from_csv, data)
+    if "error" in res:
+        entry["error"] = [res["error_type"], res["error"]]
+    else:
+        put(f"fmt/csv/{cname}/lt", res["lt"])
+        put(f"fmt/csv/{cname}/dump", np.frombuffer(res["dump"], dtype=np.uint8))
+    meta["formats"]["csv"].append(entry)
+
 out = os.path.join(HERE, "golden.npz")
 np.savez_compressed(out, **arrays)
 with open(os.path.join(HERE, "golden.json"), "w") as f:

@@ -33,3 +33,20 @@ class Golden:
             fa = self.bytes(f"parse/{entry['name']}/fasta")
             for run in entry["runs"]:
                 yield entry["name"], fa, run
+
+
+_CACHE = {}
+
+
+def golden_meta():
+    """The fixtures' metadata (json), loaded once per process."""
+    if "g" not in _CACHE:
+        _CACHE["g"] = Golden()
+    return _CACHE["g"].meta
+
+
+def golden_arrays():
+    """The fixtures' arrays (npz), loaded once per process."""
+    if "g" not in _CACHE:
+        _CACHE["g"] = Golden()
+    return _CACHE["g"].npz
