@@ -75,6 +75,9 @@ SIGNATURES = {
     "hd_tune_save": (ci, [vp, cp]),
     "hd_tune_load": (ci, [vp, cp]),
     "hd_pairwise_lt_files": (ci, [vp, u64, vp, ci, u64, ci, ci, vp, vp, vp, vp, vp]),
+    "hd_write_full_matrix": (ci, [vp, vp, u64, u64, ci, cp]),
+    "hd_read_lower_triangular": (ci, [vp, cp, ci, vp, vp, P(u64), P(u64), P(ci)]),
+    "hd_read_csv": (ci, [vp, cp, vp, vp, P(u64), P(u64), P(ci)]),
     "hd_trace_enable": (ci, [vp, ctypes.c_int]),
     "hd_trace_last": (ctypes.c_char_p, [vp]),
     "hd_measure_int_peaks": (ci, [vp, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
@@ -399,6 +402,41 @@ class Context:
             idx.append(a.sequence_indices())
             a.free()
         return outs, idx
+
+    def write_full_matrix(self, lt, nsamples, path):
+        """DataSet::dump text of a host lower triangle (hd_write_full_matrix)."""
+        lt = np.ascontiguousarray(lt)
+        self._check(lib().hd_write_full_matrix(self.h, lt.ctypes.data if lt.size else None,
+                                               lt.size, nsamples, lt.dtype.itemsize,
+                                               os.fsencode(path)))
+
+    def _read_values(self, fn, path, dtype, *lead):
+        box = {}
+
+        @OUTPUT_FN
+        def alloc(user, index, n, entries):
+            arr = np.empty(max(int(entries), 1), dtype=dtype)
+            box["arr"], box["n"] = arr[: int(entries)], int(n)
+            return arr.ctypes.data
+
+        entries, n, kind = u64(), u64(), ci()
+        rc = fn(self.h, os.fsencode(path), *lead, ctypes.cast(alloc, vp), None,
+                ctypes.byref(entries), ctypes.byref(n), ctypes.byref(kind))
+        if rc == -12:
+            err = HDError(rc, "stoi")
+            err.parse_error = kind.value
+            raise err
+        self._check(rc)
+        return box["arr"], box["n"]
+
+    def read_lower_triangular(self, path, dtype=np.uint8):
+        """from_lower_triangular on the device: (values, nsamples)."""
+        return self._read_values(lib().hd_read_lower_triangular, path, dtype,
+                                 np.dtype(dtype).itemsize)
+
+    def read_csv(self, path):
+        """from_csv on the device: (values, nsamples)."""
+        return self._read_values(lib().hd_read_csv, path, np.uint8)
 
     def trace(self, on=True):
         """Turns per-phase tracing of this context's calls on or off."""

@@ -698,6 +698,95 @@ int hd_pairwise_lt_to_file(hd_ctx *ctx, const hd_alignment *aln, int64_t max_dis
   });
 }
 
+int hd_write_full_matrix(hd_ctx *ctx, const void *lt, uint64_t entries, uint64_t nsamples,
+                         int dtype_bytes, const char *path) {
+  if (!ctx || !path || (!lt && entries)) return HD_ERR_ARG;
+  return guard(ctx, [&] {
+    check_dtype(dtype_bytes);
+    OutFile f(path, true);
+    if (!nsamples) return;
+    DevBuf d_lt((entries ? entries : 1) * dtype_bytes, ctx->stream);
+    if (entries)
+      HD_CUDA(cudaMemcpyAsync(d_lt.p, lt, entries * dtype_bytes, cudaMemcpyHostToDevice,
+                              ctx->stream));
+    // rows per chunk: text of at most kTextChunkBytes (at least one row)
+    const uint64_t row_bound = hd::full_text_bound(nsamples, 0, 1, dtype_bytes);
+    const uint64_t rows_per = std::max<uint64_t>(1, kTextChunkBytes / row_bound);
+    const uint64_t max_text = hd::full_text_bound(nsamples, 0, std::min(rows_per, nsamples),
+                                                  dtype_bytes);
+    DevBuf d_text(max_text + 16, ctx->stream);
+    PinnedPair pin(max_text + 16);
+    int pending = -1;
+    uint64_t pending_bytes = 0;
+    for (uint64_t r0 = 0, k = 0; r0 < nsamples; r0 += rows_per, ++k) {
+      const uint64_t r1 = std::min(nsamples, r0 + rows_per);
+      const uint64_t nb =
+          hd::format_full_rows(ctx, d_lt.p, entries, dtype_bytes, nsamples, r0, r1, d_text.as<char>());
+      // write the previous chunk while this one copies
+      if (pending >= 0) {
+        HD_CUDA(cudaEventSynchronize(pin.ev[pending]));
+        f.write(pin.buf[pending], pending_bytes);
+      }
+      const int slot = (int)(k & 1);
+      if (nb)
+        HD_CUDA(cudaMemcpyAsync(pin.buf[slot], d_text.p, nb, cudaMemcpyDeviceToHost, ctx->stream));
+      HD_CUDA(cudaEventRecord(pin.ev[slot], ctx->stream));
+      pending = slot;
+      pending_bytes = nb;
+    }
+    if (pending >= 0) {
+      HD_CUDA(cudaEventSynchronize(pin.ev[pending]));
+      f.write(pin.buf[pending], pending_bytes);
+    }
+  });
+}
+
+namespace {
+// Copies parsed values to the caller's buffer from out_fn.
+void deliver(hd_ctx *ctx, const hd::ParsedValues &pv, int dtype_bytes, hd_output_fn out_fn,
+             void *user) {
+  void *host = out_fn(user, 0, pv.nsamples, pv.entries);
+  if (!host && pv.entries) fail(HD_ERR_ARG, "output callback returned no buffer");
+  if (!pv.entries) return;
+  const uint64_t bytes = pv.entries * dtype_bytes;
+  prefault_host(host, bytes);
+  HD_CUDA(cudaMemcpyAsync(host, pv.values.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  HD_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+}  // namespace
+
+int hd_read_lower_triangular(hd_ctx *ctx, const char *path, int dtype_bytes, hd_output_fn out_fn,
+                             void *user, uint64_t *entries, uint64_t *nsamples, int *parse_error) {
+  if (!ctx || !path || !out_fn || (dtype_bytes != 1 && dtype_bytes != 2)) return HD_ERR_ARG;
+  if (parse_error) *parse_error = 0;
+  return guard(ctx, [&] {
+    uint64_t nbytes = 0;
+    const uint8_t *d = stage_file(ctx, path, &nbytes);
+    hd::ParsedValues pv = hd::read_lower_triangular_device(ctx, d, nbytes, dtype_bytes);
+    if (entries) *entries = pv.entries;
+    if (nsamples) *nsamples = pv.nsamples;
+    if (parse_error) *parse_error = pv.error;
+    if (pv.error) fail(HD_ERR_PARSE, "stoi");
+    deliver(ctx, pv, dtype_bytes, out_fn, user);
+  });
+}
+
+int hd_read_csv(hd_ctx *ctx, const char *path, hd_output_fn out_fn, void *user, uint64_t *entries,
+                uint64_t *nsamples, int *parse_error) {
+  if (!ctx || !path || !out_fn) return HD_ERR_ARG;
+  if (parse_error) *parse_error = 0;
+  return guard(ctx, [&] {
+    uint64_t nbytes = 0;
+    const uint8_t *d = stage_file(ctx, path, &nbytes);
+    hd::ParsedValues pv = hd::read_csv_device(ctx, d, nbytes);
+    if (entries) *entries = pv.entries;
+    if (nsamples) *nsamples = pv.nsamples;
+    if (parse_error) *parse_error = pv.error;
+    if (pv.error) fail(HD_ERR_PARSE, "stoi");
+    deliver(ctx, pv, 1, out_fn, user);
+  });
+}
+
 int hd_write_lower_triangular(hd_ctx *ctx, const void *lt, uint64_t nsamples, int dtype_bytes,
                               const char *path) {
   if (!ctx || !path || (!lt && nsamples > 1)) return HD_ERR_ARG;

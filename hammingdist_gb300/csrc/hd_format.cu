@@ -115,6 +115,100 @@ uint64_t format_lt_rows(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint64_t
   return total;
 }
 
+// ------------------------------------------------------ full matrix text
+// DataSet::dump (include/hamming/hamming.hh:63-73): row i of the n x n matrix,
+// entries (*this)[{i, j}] (0 on the diagonal, lt[i(i-1)/2 + j] below it and
+// lt[j(j-1)/2 + i] above it), ", " between entries, '\n' after the row. An
+// index past the `entries` values read as 0 (a triangle whose size is not
+// n(n-1)/2, where the reference reads out of bounds).
+template <typename T>
+__device__ inline uint32_t full_entry(const T *lt, uint64_t entries, uint64_t i, uint64_t j) {
+  if (i == j) return 0u;
+  const uint64_t k = i > j ? row_index(i) + j : row_index(j) + i;
+  return k < entries ? (uint32_t)lt[k] : 0u;
+}
+
+template <typename T>
+__global__ void k_full_len(const T *lt, uint64_t entries, uint64_t n, uint64_t i_lo, uint64_t rows,
+                           uint64_t *row_len) {
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t q = wid; q < rows; q += nwarps) {
+    const uint64_t i = i_lo + q;
+    uint64_t len = 0;
+    for (uint64_t j = lane; j < n; j += 32) len += ndig(full_entry(lt, entries, i, j)) + 2;
+    len = warp_sum(len);
+    if (lane == 0) row_len[q] = len - 1;  // the last entry has "\n" instead of ", "
+  }
+}
+
+template <typename T>
+__global__ void k_full_write(const T *lt, uint64_t entries, uint64_t n, uint64_t i_lo, uint64_t rows,
+                             const uint64_t *row_off, char *text) {
+  const int lane = threadIdx.x & 31;
+  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t q = wid; q < rows; q += nwarps) {
+    const uint64_t i = i_lo + q;
+    uint64_t pos = row_off[q];
+    for (uint64_t j0 = 0; j0 < n; j0 += 32) {
+      const uint64_t j = j0 + lane;
+      const bool on = j < n;
+      const bool last = j + 1 == n;
+      const uint32_t v = on ? full_entry(lt, entries, i, j) : 0u;
+      const uint32_t nd = on ? ndig(v) : 0u;
+      const uint32_t len = on ? nd + (last ? 1u : 2u) : 0u;
+      const uint32_t inc = warp_incl_scan(len);
+      if (on) {
+        char *dst = text + pos + inc - len;
+        put_dec(dst, v, nd);
+        if (last) {
+          dst[nd] = '\n';
+        } else {
+          dst[nd] = ',';
+          dst[nd + 1] = ' ';
+        }
+      }
+      pos += __shfl_sync(0xffffffffu, inc, 31);
+    }
+  }
+}
+
+uint64_t full_text_bound(uint64_t n, uint64_t i_lo, uint64_t i_hi, int dtype_bytes) {
+  if (i_hi <= i_lo) return 0;
+  const uint64_t per = dtype_bytes == 1 ? 5 : dtype_bytes == 2 ? 7 : 12;  // digits + ", "
+  return (i_hi - i_lo) * (n * per + 1);
+}
+
+uint64_t format_full_rows(hd_ctx *ctx, const void *d_lt, uint64_t entries, int dtype_bytes,
+                          uint64_t n, uint64_t i_lo, uint64_t i_hi, char *d_text) {
+  if (i_hi <= i_lo) return 0;
+  const uint64_t rows = i_hi - i_lo;
+  cudaStream_t st = ctx->stream;
+  DevBuf len(rows * 8, st), off(rows * 8, st), tot(8, st);
+  const unsigned g = warp_grid(ctx, rows);
+  if (dtype_bytes == 1)
+    k_full_len<uint8_t><<<g, 256, 0, st>>>((const uint8_t *)d_lt, entries, n, i_lo, rows, len.as<uint64_t>());
+  else if (dtype_bytes == 2)
+    k_full_len<uint16_t><<<g, 256, 0, st>>>((const uint16_t *)d_lt, entries, n, i_lo, rows, len.as<uint64_t>());
+  else
+    k_full_len<uint32_t><<<g, 256, 0, st>>>((const uint32_t *)d_lt, entries, n, i_lo, rows, len.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+  scan_exclusive<uint64_t>(ctx, len.as<uint64_t>(), off.as<uint64_t>(), rows, tot.as<uint64_t>());
+  if (dtype_bytes == 1)
+    k_full_write<uint8_t><<<g, 256, 0, st>>>((const uint8_t *)d_lt, entries, n, i_lo, rows, off.as<uint64_t>(), d_text);
+  else if (dtype_bytes == 2)
+    k_full_write<uint16_t><<<g, 256, 0, st>>>((const uint16_t *)d_lt, entries, n, i_lo, rows, off.as<uint64_t>(), d_text);
+  else
+    k_full_write<uint32_t><<<g, 256, 0, st>>>((const uint32_t *)d_lt, entries, n, i_lo, rows, off.as<uint64_t>(), d_text);
+  HD_LAUNCHED(ctx);
+  uint64_t total = 0;
+  HD_CUDA(cudaMemcpyAsync(&total, tot.p, 8, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  return total;
+}
+
 // ----------------------------------------------------------- sparse text
 // Lines "i j d\n" for j < i with d <= threshold (integer compare, as the
 // reference's `*d <= threshold`).

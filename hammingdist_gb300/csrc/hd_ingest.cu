@@ -210,6 +210,27 @@ static unsigned grid_for(uint64_t n, int threads) {
   return (unsigned)(g > 0x7fffffffull ? 0x7fffffffull : g);
 }
 
+DevBuf newline_positions(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64_t *m_nl) {
+  cudaStream_t st = ctx->stream;
+  const uint64_t nblk = ceil_div(nbytes ? nbytes : 1, kNlBlockBytes);
+  DevBuf counts(nblk * 8, st), offs(nblk * 8, st), total(8, st);
+  k_nl_count<<<(unsigned)nblk, kNlThreads, 0, st>>>(d, nbytes, counts.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+  scan_exclusive<uint64_t>(ctx, counts.as<uint64_t>(), offs.as<uint64_t>(), nblk,
+                           total.as<uint64_t>());
+  uint64_t h = 0;
+  HD_CUDA(cudaMemcpyAsync(&h, total.p, 8, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  *m_nl = h;
+  DevBuf nl((h + 1) * 8, st);
+  if (h) {
+    k_nl_write<<<(unsigned)nblk, kNlThreads, 0, st>>>(d, nbytes, offs.as<uint64_t>(),
+                                                       nl.as<uint64_t>());
+    HD_LAUNCHED(ctx);
+  }
+  return nl;
+}
+
 Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_t n_limit) {
   cudaStream_t st = ctx->stream;
   Records rec;

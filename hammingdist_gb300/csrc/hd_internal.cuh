@@ -404,6 +404,23 @@ TileConfig tile_config_for(hd_ctx *ctx, uint64_t n_rows, uint64_t length, int dt
 // device (lt index lt_base at d_lt[0]). Returns bytes written to d_text
 // (capacity checked by the caller via the *_bound functions).
 uint64_t lt_text_bound(uint64_t i_lo, uint64_t i_hi, int dtype_bytes);
+// full n x n matrix text (DataSet::dump) of rows [i_lo, i_hi) from the whole
+// device-resident triangle of `entries` values
+uint64_t full_text_bound(uint64_t n, uint64_t i_lo, uint64_t i_hi, int dtype_bytes);
+uint64_t format_full_rows(hd_ctx *ctx, const void *d_lt, uint64_t entries, int dtype_bytes,
+                          uint64_t n, uint64_t i_lo, uint64_t i_hi, char *d_text);
+// positions of every '\n' of a device buffer, in order (*m_nl of them)
+DevBuf newline_positions(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64_t *m_nl);
+// result-file readers (hd_results.cu): see hd_read_lower_triangular / hd_read_csv
+struct ParsedValues {
+  uint64_t entries = 0;   // values produced
+  uint64_t nsamples = 0;  // as the reference infers it
+  int error = 0;          // 0, or 1 = a field without digits, 2 = a value outside int
+  DevBuf values;          // entries x dtype bytes on the device
+};
+ParsedValues read_lower_triangular_device(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes,
+                                          int dtype_bytes);
+ParsedValues read_csv_device(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes);
 uint64_t format_lt_rows(hd_ctx *ctx, const void *d_lt, int dtype_bytes, uint64_t lt_base,
                         uint64_t i_lo, uint64_t i_hi, char *d_text);
 // Sparse lines of rows [i_lo, i_hi): counts text bytes per row into

@@ -89,12 +89,6 @@ void copy_parallel(void *dst, const void *src, size_t n) {
   });
 }
 
-// Zeroes fresh memory on up to 16 threads, so its pages are first touched in
-// parallel (one thread faulting in ~100 MB costs several ms).
-void zero_parallel(void *dst, size_t n) {
-  split_parallel(n, [&](size_t a, size_t b) { std::memset(static_cast<char *>(dst) + a, 0, b - a); });
-}
-
 // Allocator whose resize() leaves new elements uninitialised; result vectors
 // are sized, zeroed in parallel and then filled by the device copy.
 template <class T>
@@ -167,15 +161,13 @@ struct DataSet {
 
   // hamming.hh:63-73 (full matrix, ", " separators): host formatting, not on
   // the device path
+  // hamming.hh:63-73: the full matrix, formatted on the device
   void dump(const std::string &filename) const {
-    std::ofstream s(filename);
-    for (uint64_t i = 0; i < nsamples; ++i) {
-      for (uint64_t j = 0; j < nsamples; ++j) {
-        s << at({i, j});
-        if (j != nsamples - 1) s << ", ";
-      }
-      s << std::endl;
-    }
+    std::lock_guard<std::mutex> lk(g_mu);
+    hd_ctx *c = ctx();
+    py::gil_scoped_release nogil;
+    check(hd_write_full_matrix(c, result.data(), result.size(), nsamples, sizeof(T),
+                               filename.c_str()));
   }
 
   void dump_lower_triangular(const std::string &filename) const {
@@ -204,14 +196,6 @@ struct DataSet {
 };
 
 namespace {
-
-// infer n from n(n-1)/2 entries (hamming.hh:57-61)
-uint64_t n_from_entries(uint64_t e) {
-  uint64_t n = (uint64_t)std::llround((std::sqrt(8.0 * (double)e + 1.0) + 1.0) / 2.0);
-  while (n > 1 && n * (n - 1) / 2 > e) --n;
-  while (n * (n - 1) / 2 < e) ++n;
-  return n;
-}
 
 template <typename T>
 DataSet<T> compute(hd_alignment *aln, int64_t max_distance, bool announce, const char *what,
@@ -425,48 +409,52 @@ py::array_t<uint64_t> fasta_sequence_indices(const std::string &fasta, size_t nl
   return owned_array<uint64_t>(out, n);
 }
 
-// Readers (hamming.hh:34-55, :152-166): host parsing of result files.
+// Readers (hamming.hh:34-55, :152-166), parsed on the device. A field that
+// std::stoi rejects raises the exception the reference raises there; a file
+// that cannot be read gives an empty DataSet, as the reference's ifstream
+// reads nothing from it.
+[[noreturn]] void throw_parse(int kind) {
+  if (kind == 2) throw std::out_of_range("stoi");
+  throw std::invalid_argument("stoi");
+}
+
 template <typename T>
-DataSet<T> from_lower_triangular(const std::string &filename) {
-  std::ifstream s(filename);
+DataSet<T> read_result_file(const std::string &filename, bool csv) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
   DataSet<T> ds;
-  std::string line, d;
-  while (std::getline(s, line)) {
-    std::istringstream ls(line);
-    while (ls.good()) {
-      std::getline(ls, d, ',');
-      int v = std::stoi(d);
-      ds.result.push_back(v > (int)std::numeric_limits<T>::max() ? std::numeric_limits<T>::max()
-                                                                  : (T)v);
-    }
+  hd_output_fn alloc = [](void *user, uint64_t, uint64_t n, uint64_t entries) -> void * {
+    auto *d = static_cast<DataSet<T> *>(user);
+    d->nsamples = n;
+    d->result.resize(entries);
+    return d->result.data();
+  };
+  uint64_t entries = 0, n = 0;
+  int kind = 0;
+  int rc;
+  {
+    py::gil_scoped_release nogil;
+    rc = csv ? hd_read_csv(c, filename.c_str(), alloc, &ds, &entries, &n, &kind)
+             : hd_read_lower_triangular(c, filename.c_str(), sizeof(T), alloc, &ds, &entries, &n,
+                                        &kind);
   }
-  ds.nsamples = n_from_entries(ds.result.size());
+  if (rc == HD_ERR_PARSE) throw_parse(kind);
+  if (rc == HD_ERR_IO) {
+    DataSet<T> empty;
+    empty.nsamples = csv ? 0 : 1;  // no lines: 0 newlines / (round(sqrt(1)) + 1) / 2
+    return empty;
+  }
+  check(rc);
   return ds;
 }
 
+template <typename T>
+DataSet<T> from_lower_triangular(const std::string &filename) {
+  return read_result_file<T>(filename, false);
+}
+
 DataSet<uint8_t> from_csv(const std::string &filename) {
-  std::ifstream s(filename);
-  DataSet<uint8_t> ds;
-  std::string line;
-  uint64_t n = 0;
-  {
-    std::ifstream c(filename);
-    n = std::count(std::istreambuf_iterator<char>(c), std::istreambuf_iterator<char>(), '\n');
-  }
-  ds.nsamples = n;
-  ds.result.resize(n * (n + 1) / 2);
-  zero_parallel(ds.result.data(), ds.result.size());  // entries past the rows read stay 0
-  uint64_t i = 0, row = 0;
-  while (std::getline(s, line)) {
-    std::istringstream ls(line);
-    std::string d;
-    for (uint64_t j = 0; j < row; ++j) {
-      std::getline(ls, d, ',');
-      ds.result[i++] = (uint8_t)std::stoi(d);
-    }
-    ++row;
-  }
-  return ds;
+  return read_result_file<uint8_t>(filename, true);
 }
 
 template <typename T>

@@ -38,6 +38,16 @@ extern "C" {
 #define HD_ERR_REF_LENGTH -9     /* a record is longer than the reference sequence */
 #define HD_ERR_OOM -10           /* device or pinned host allocation failed */
 #define HD_ERR_STATE -11         /* object in the wrong state (e.g. released) */
+#define HD_ERR_PARSE -12         /* a field std::stoi rejects (see hd_read_*) */
+
+/* Output buffers of hd_pairwise_lt_files and the hd_read_* readers: called
+ * once per output, possibly from a library thread, when its size is known
+ * (hd_pairwise_lt_files: file `index`, its unique row count and
+ * n_rows(n_rows-1)/2 entries; the readers: index 0, nsamples and the number
+ * of values); returns the host buffer for `entries` values of the output's
+ * dtype. It need not be touched yet. NULL with entries > 0 fails the call
+ * with HD_ERR_ARG. Calls for different indices may run concurrently. */
+typedef void *(*hd_output_fn)(void *user, uint64_t index, uint64_t n_rows, uint64_t entries);
 
 /* ---- semantics of a pairwise matrix ------------------------------------- */
 /* HD_SEM_GPU: the reference's use_gpu=True semantics — the dense AND rule of
@@ -150,6 +160,38 @@ int hd_pairwise_lt_to_file(hd_ctx *ctx, const hd_alignment *aln,
 /* Replaces write_lower_triangular (include/hamming/hamming_utils.hh:106-110)
  * as used by DataSet::dump_lower_triangular (include/hamming/hamming.hh:
  * 75-77). `lt` is host memory with nsamples(nsamples-1)/2 entries. */
+/* ---- result files ------------------------------------------------------- */
+/* Replaces DataSet::dump (include/hamming/hamming.hh:63-73): the full
+ * nsamples x nsamples matrix as text, entries of row i separated by ", ",
+ * one line per row, 0 on the diagonal and the matrix symmetric, read from
+ * the `entries` lower-triangle values lt[i(i-1)/2 + j] (host memory; an
+ * index past `entries` reads as 0). Formatted on the device, written to the
+ * file in chunks while the next chunk formats. Output of the device
+ * formatter is byte-identical to the reference's ofstream output. */
+int hd_write_full_matrix(hd_ctx *ctx, const void *lt, uint64_t entries, uint64_t nsamples,
+                         int dtype_bytes, const char *path);
+/* Replaces from_lower_triangular<T> (include/hamming/hamming.hh:152-166;
+ * dtype_bytes 1 = uint8_t, 2 = uint16_t): every comma-separated field of
+ * every line of the file, parsed on the device with std::stoi's rules and
+ * stored through safe_int_cast<T> (include/hamming/hamming_impl.hh:37-45).
+ * out_fn (see hd_output_fn; index 0) receives *nsamples, inferred as the
+ * reference does ((round(sqrt(8 entries + 1)) + 1) / 2), and the number of
+ * values, and returns the host buffer they are copied to. A field std::stoi
+ * rejects fails the call with HD_ERR_PARSE before out_fn is called, and
+ * *parse_error says which exception the reference raises there: 1 =
+ * std::invalid_argument (no digits), 2 = std::out_of_range (outside int).
+ * An unreadable path fails with HD_ERR_IO. */
+int hd_read_lower_triangular(hd_ctx *ctx, const char *path, int dtype_bytes, hd_output_fn out_fn,
+                             void *user, uint64_t *entries, uint64_t *nsamples, int *parse_error);
+/* Replaces from_csv / DataSet(filename) (include/hamming/hamming.hh:34-55,
+ * src/hamming.cc:23-25): nsamples = number of '\n' in the file; the result
+ * has nsamples(nsamples+1)/2 uint8 values, zero-initialised; line i gives
+ * its first i comma-separated fields to value i(i-1)/2 + j (a line with
+ * fewer repeats its last field, as std::getline leaves it in place), each
+ * through std::stoi truncated to uint8. Errors and out_fn as in
+ * hd_read_lower_triangular. */
+int hd_read_csv(hd_ctx *ctx, const char *path, hd_output_fn out_fn, void *user, uint64_t *entries,
+                uint64_t *nsamples, int *parse_error);
 int hd_write_lower_triangular(hd_ctx *ctx, const void *lt, uint64_t nsamples,
                               int dtype_bytes, const char *path);
 /* Replaces DataSet::dump_sparse (include/hamming/hamming.hh:79-114): lines
@@ -254,13 +296,6 @@ int hd_alignments_from_fasta_files(hd_ctx *ctx, uint64_t count,
                                    int remove_duplicates, uint64_t n_limit,
                                    int include_x, int semantics,
                                    hd_alignment **out);
-
-/* Output buffers of hd_pairwise_lt_files: called once per file, from a
- * library thread, when the file's unique row count is known; returns the
- * host buffer for its `entries` = n_rows(n_rows-1)/2 values (of that file's
- * dtype_bytes). It need not be touched yet. NULL with entries > 0 fails the
- * call with HD_ERR_ARG. Calls for different indices may run concurrently. */
-typedef void *(*hd_output_fn)(void *user, uint64_t index, uint64_t n_rows, uint64_t entries);
 
 /* Many FASTA files to their lower triangles in one pipelined call (no
  * reference counterpart: the reference computes one matrix per call, as in
