@@ -27,7 +27,8 @@ reference compiled from source where available, else the C restatement in
 oracle/) on the host cores, on a bounded sample of the same workload.
 
 Other workloads, each printing its own JSON line: --small (n=1,000
-from_fasta vs the CPU port), --kernel-only (the pairwise kernel alone),
+from_fasta vs the CPU port), --formats (dump / from_lower_triangular /
+from_csv of the headline matrix vs the CPU port), --kernel-only (the pairwise kernel alone),
 --batched (64 uneven alignments), --streaming (from_fasta_large n=50,000,
 from_fasta_to_lower_triangular n=100,000, dump_sparse), --serve (Poisson
 request stream over resident alignments).
@@ -646,6 +647,76 @@ def run_small(args):
         "bit_exact": bool(np.array_equal(np.asarray(lt), want))}), flush=True)
 
 
+def run_formats(args):
+    """Result files of the headline matrix (14,000 unique rows of the n=20,000,
+    L=29,903 workload, uint8): DataSet.dump (full matrix text),
+    from_lower_triangular (the dump_lower_triangular text) and from_csv (the
+    dump text), on the device through the public API. The CPU leg is the C
+    restatement of the reference's single-threaded host code on the first
+    --formats-cpu-rows rows (a prefix of the triangle is the matrix of those
+    rows). Checks: the sample's dump text is byte-identical between device and
+    CPU, and both readers give the matrix back at full size."""
+    import hammingdist_gb300 as hd
+    from oracle import hd_oracle as o
+
+    def rate(entries, s):
+        return entries / s / 1e6
+
+    with tempfile.TemporaryDirectory(dir=args.tmpdir or None) as d:
+        fa, root, path, rows = make_workload(d)
+        with quiet_stdout():
+            ds = hd.from_fasta(path, use_gpu=True, remove_duplicates=True)
+        lt = np.asarray(ds.lt_array)
+        n = int(round((1 + (1 + 8 * lt.size) ** 0.5) / 2))
+        full_entries = n * n
+        ltp, dmp = os.path.join(d, "lt.txt"), os.path.join(d, "dump.txt")
+        ds.dump_lower_triangular(ltp)
+        times = {}
+        t = time.perf_counter()
+        ds.dump(dmp)
+        times["dump"] = time.perf_counter() - t
+        for name, fn, arg in (("from_lower_triangular", hd.from_lower_triangular, ltp),
+                              ("from_csv", hd.from_csv, dmp)):
+            best = 1e30
+            for _ in range(3):
+                t = time.perf_counter()
+                back = fn(arg)
+                best = min(best, time.perf_counter() - t)
+            times[name] = best
+            got = np.asarray(back.lt_array)[: lt.size]
+            assert np.array_equal(got, lt), name
+        sizes = {"dump": os.path.getsize(dmp), "lt_text": os.path.getsize(ltp)}
+        # CPU leg on a prefix sample
+        m = args.formats_cpu_rows
+        sub = np.ascontiguousarray(lt[: m * (m - 1) // 2])
+        s_lt, s_dmp, c_dmp = (os.path.join(d, x) for x in ("s_lt.txt", "s_dump.txt", "c_dump.txt"))
+        with open(s_lt, "wb") as fh:
+            fh.write(o.format_lower_triangular(sub))
+        cpu = {}
+        t = time.perf_counter()
+        o.dump_full(sub, m, c_dmp)
+        cpu["dump"] = time.perf_counter() - t
+        t = time.perf_counter()
+        c_lt, _ = o.read_lower_triangular(s_lt)
+        cpu["from_lower_triangular"] = time.perf_counter() - t
+        t = time.perf_counter()
+        c_csv, _ = o.read_csv(c_dmp)
+        cpu["from_csv"] = time.perf_counter() - t
+        sample_ds = hd.from_lower_triangular(s_lt)
+        sample_ds.dump(s_dmp)
+        parity = (open(s_dmp, "rb").read() == open(c_dmp, "rb").read()
+                  and np.array_equal(c_lt, sub) and np.array_equal(c_csv[: sub.size], sub))
+    entries = {"dump": full_entries, "from_lower_triangular": lt.size, "from_csv": lt.size}
+    s_entries = {"dump": m * m, "from_lower_triangular": sub.size, "from_csv": sub.size}
+    out = {"mode": "formats", "n": n, "dtype": "u8", "text_bytes": sizes,
+           "parity": "bit-exact" if parity else "MISMATCH", "cpu_sample_rows": m, "cpu_threads": 1}
+    for k in times:
+        g, c = rate(entries[k], times[k]), rate(s_entries[k], cpu[k])
+        out[k] = {"gpu_s": times[k], "gpu_Mentries_per_s": g, "cpu_Mentries_per_s": c,
+                  "speedup": g / c}
+    print(json.dumps(out), flush=True)
+
+
 def run_serve(args):
     """Serving: 8 alignments resident in HBM (n = 200k, 100k, 50k, 50k, 20k,
     20k, 10k, 10k at --serve-scale 1; L=29,903; generated on the device), a
@@ -802,6 +873,9 @@ def main():
     ap.add_argument("--n-stream", type=int, default=100000)
     ap.add_argument("--sparse-check", type=int, default=2000)
     ap.add_argument("--tmpdir", default="")
+    ap.add_argument("--formats", action="store_true",
+                    help="result files (dump, from_lower_triangular, from_csv) vs the CPU port")
+    ap.add_argument("--formats-cpu-rows", type=int, default=3500)
     ap.add_argument("--small", action="store_true",
                     help="n=1,000 from_fasta through the public API vs the CPU port")
     ap.add_argument("--serve", action="store_true", help="serving workload (Poisson stream)")
@@ -811,7 +885,9 @@ def main():
     ap.add_argument("--serve-budget-gb", type=int, default=8)
     ap.add_argument("--serve-serial", type=int, default=600)
     args = ap.parse_args()
-    if args.small:
+    if args.formats:
+        run_formats(args)
+    elif args.small:
         run_small(args)
     elif args.streaming:
         run_streaming(args)

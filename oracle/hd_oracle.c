@@ -17,6 +17,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <math.h>
 #include <stdio.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -625,4 +626,171 @@ int hdo_num_threads(void) {
 #else
   return 1;
 #endif
+}
+
+/* ------------------------------------------------------ result file formats
+ * Single-threaded, like the reference's host code. */
+
+/* DataSet::dump (include/hamming/hamming.hh:63-73): the full matrix, entries
+ * (*this)[{i, j}] (129-138: 0 on the diagonal, symmetric), ", " between
+ * entries, one line per row; an index past `entries` reads as 0. */
+int hdo_dump_full(const void *lt, uint64_t entries, uint64_t n, int dtype_bytes, const char *path) {
+  FILE *f = fopen(path, "wb");
+  if (!f) return -5;
+  char *line = (char *)malloc(n * 12 + 2);
+  if (!line && n) {
+    fclose(f);
+    return -10;
+  }
+  for (uint64_t i = 0; i < n; ++i) {
+    size_t m = 0;
+    for (uint64_t j = 0; j < n; ++j) {
+      uint64_t v = 0;
+      if (i != j) {
+        const uint64_t k = i > j ? i * (i - 1) / 2 + j : j * (j - 1) / 2 + i;
+        v = k < entries ? hdo_lt_get(lt, dtype_bytes, k) : 0;
+      }
+      m += hdo_utoa(v, line + m);
+      if (j != n - 1) {
+        line[m++] = ',';
+        line[m++] = ' ';
+      }
+    }
+    line[m++] = '\n';
+    if (fwrite(line, 1, m, f) != m) {
+      free(line);
+      fclose(f);
+      return -5;
+    }
+  }
+  free(line);
+  return fclose(f) == 0 ? 0 : -5;
+}
+
+/* std::stoi on [p, end): C whitespace, sign, digits; 0 ok, 1 no digits
+ * (std::invalid_argument), 2 outside int (std::out_of_range). */
+static int hdo_stoi(const char *p, const char *end, int *v) {
+  while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\v' || *p == '\f' || *p == '\r'))
+    ++p;
+  int neg = 0;
+  if (p < end && (*p == '+' || *p == '-')) neg = *p++ == '-';
+  const char *d0 = p;
+  long long acc = 0;
+  while (p < end && *p >= '0' && *p <= '9') {
+    if (acc < (1ll << 40)) acc = acc * 10 + (*p - '0');
+    ++p;
+  }
+  if (p == d0) return 1;
+  if (neg) acc = -acc;
+  if (acc > 2147483647ll || acc < -2147483648ll) return 2;
+  *v = (int)acc;
+  return 0;
+}
+
+static char *hdo_slurp(const char *path, uint64_t *n) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return NULL;
+  fseek(f, 0, SEEK_END);
+  long sz = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  char *buf = (char *)malloc((size_t)sz + 1);
+  if (buf && sz > 0 && fread(buf, 1, (size_t)sz, f) != (size_t)sz) {
+    free(buf);
+    buf = NULL;
+  }
+  fclose(f);
+  *n = (uint64_t)sz;
+  return buf;
+}
+
+/* from_lower_triangular<T> (hamming.hh:152-166): every comma-separated field
+ * of every line (std::getline while the stream is good), safe_int_cast<T>
+ * (include/hamming/hamming_impl.hh:37-45); nsamples = (round(sqrt(8 size +
+ * 1)) + 1) / 2. *out from malloc. */
+int hdo_read_lower_triangular(const char *path, int dtype_bytes, void **out, uint64_t *entries,
+                              uint64_t *nsamples, int *parse_error) {
+  uint64_t n = 0;
+  *parse_error = 0;
+  char *buf = hdo_slurp(path, &n);
+  if (!buf) return -5;
+  uint64_t cap = 1024, cnt = 0;
+  uint8_t *vals = (uint8_t *)malloc(cap * dtype_bytes);
+  const int mx = dtype_bytes == 1 ? 255 : 65535;
+  uint64_t s = 0;
+  while (s < n) {  /* one line [s, e) */
+    uint64_t e = s;
+    while (e < n && buf[e] != '\n') ++e;
+    uint64_t a = s;
+    for (;;) {  /* field [a, b) */
+      uint64_t b = a;
+      while (b < e && buf[b] != ',') ++b;
+      int v = 0;
+      const int r = hdo_stoi(buf + a, buf + e, &v);
+      if (r) {
+        *parse_error = r;
+        free(vals);
+        free(buf);
+        return -12;
+      }
+      if (cnt == cap) {
+        cap *= 2;
+        vals = (uint8_t *)realloc(vals, cap * dtype_bytes);
+      }
+      const unsigned u = v > mx ? (unsigned)mx : (unsigned)v;
+      if (dtype_bytes == 1) vals[cnt] = (uint8_t)u;
+      else ((uint16_t *)vals)[cnt] = (uint16_t)u;
+      ++cnt;
+      if (b >= e) break;
+      a = b + 1;
+    }
+    s = e + 1;
+  }
+  free(buf);
+  *out = vals;
+  *entries = cnt;
+  *nsamples = ((uint64_t)llround(sqrt((double)(8 * cnt + 1))) + 1) / 2;
+  return 0;
+}
+
+/* from_csv / DataSet(filename) (hamming.hh:34-55): nsamples = number of
+ * '\n', n(n+1)/2 zeroed values; line i gives its first i fields (missing
+ * ones repeat the last field, as std::getline leaves it), std::stoi
+ * truncated to uint8. */
+int hdo_read_csv(const char *path, uint8_t **out, uint64_t *entries, uint64_t *nsamples,
+                 int *parse_error) {
+  uint64_t n = 0;
+  *parse_error = 0;
+  char *buf = hdo_slurp(path, &n);
+  if (!buf) return -5;
+  uint64_t nl = 0;
+  for (uint64_t k = 0; k < n; ++k) nl += buf[k] == '\n';
+  const uint64_t total = nl * (nl + 1) / 2;
+  uint8_t *vals = (uint8_t *)calloc(total ? total : 1, 1);
+  uint64_t s = 0, line = 0, pos = 0;
+  while (s < n) {
+    uint64_t e = s;
+    while (e < n && buf[e] != '\n') ++e;
+    uint64_t a = s;
+    for (uint64_t j = 0; j < line; ++j) {
+      int v = 0;
+      const int r = hdo_stoi(buf + a, buf + e, &v);
+      if (r) {
+        *parse_error = r;
+        free(vals);
+        free(buf);
+        return -12;
+      }
+      vals[pos++] = (uint8_t)(unsigned)v;
+      uint64_t b = a;
+      while (b < e && buf[b] != ',') ++b;
+      if (b < e) a = b + 1;  /* else the line is exhausted: the same field again */
+    }
+    ++line;
+    s = e + 1;
+  }
+  free(buf);
+  *out = vals;
+  *entries = total;
+  *nsamples = nl;
+  return 0;
 }

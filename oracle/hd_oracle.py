@@ -43,7 +43,7 @@ def build(force: bool = False) -> str:
         os.makedirs(os.path.dirname(_OUT), exist_ok=True)
         tmp = _OUT + f".tmp{os.getpid()}"
         subprocess.check_call(
-            ["gcc", "-O3", "-std=c11", "-fopenmp", "-shared", "-fPIC", _SRC, "-o", tmp]
+            ["gcc", "-O3", "-std=c11", "-fopenmp", "-shared", "-fPIC", _SRC, "-o", tmp, "-lm"]
         )
         os.replace(tmp, _OUT)
         with open(stamp, "w") as f:
@@ -76,6 +76,10 @@ def lib():
             L.hdo_pack_row.argtypes = [cp, u64, vp]
             L.hdo_packed_row_bytes.argtypes = [u64]
             L.hdo_packed_row_bytes.restype = u64
+            L.hdo_dump_full.argtypes = [vp, u64, u64, ctypes.c_int, cp]
+            L.hdo_read_lower_triangular.argtypes = [cp, ctypes.c_int, P(vp), P(u64), P(u64),
+                                                    P(ctypes.c_int)]
+            L.hdo_read_csv.argtypes = [cp, P(vp), P(u64), P(u64), P(ctypes.c_int)]
             L.hdo_free.argtypes = [vp]
             L.hdo_num_threads.restype = ctypes.c_int
             _lib = L
@@ -232,6 +236,33 @@ def format_sparse(lt: np.ndarray, nsamples: int, threshold: int) -> bytes:
     L.hdo_format_sparse(lt.ctypes.data, nsamples, lt.dtype.itemsize, threshold, buf,
                         ctypes.byref(nl))
     return buf.raw[: int(nb)]
+
+
+def dump_full(lt: np.ndarray, nsamples: int, path: str) -> None:
+    """DataSet::dump text (include/hamming/hamming.hh:63-73), one thread."""
+    lt = np.ascontiguousarray(lt)
+    _check(lib().hdo_dump_full(lt.ctypes.data if lt.size else None, lt.size, nsamples,
+                               lt.dtype.itemsize, os.fsencode(path)))
+
+
+def _read_values(fn, path, dtype, *lead):
+    out, entries, n, kind = ctypes.c_void_p(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_int()
+    rc = fn(os.fsencode(path), *lead, ctypes.byref(out), ctypes.byref(entries), ctypes.byref(n),
+            ctypes.byref(kind))
+    if rc == -12:
+        raise (IndexError if kind.value == 2 else ValueError)("stoi")
+    _check(rc)
+    return _take(out.value, entries.value, dtype), n.value
+
+
+def read_lower_triangular(path: str, dtype=np.uint8):
+    """from_lower_triangular<T> (hamming.hh:152-166), one thread: (values, nsamples)."""
+    return _read_values(lib().hdo_read_lower_triangular, path, dtype, np.dtype(dtype).itemsize)
+
+
+def read_csv(path: str):
+    """from_csv (hamming.hh:34-55), one thread: (values, nsamples)."""
+    return _read_values(lib().hdo_read_csv, path, np.uint8)
 
 
 def num_threads() -> int:
