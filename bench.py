@@ -679,6 +679,9 @@ def run_formats(args):
                               ("from_csv", hd.from_csv, dmp)):
             best = 1e30
             for _ in range(3):
+                # a new mtime: the file is read and uploaded again every time
+                stamp = time.time_ns()
+                os.utime(arg, ns=(stamp, stamp))
                 t = time.perf_counter()
                 back = fn(arg)
                 best = min(best, time.perf_counter() - t)
