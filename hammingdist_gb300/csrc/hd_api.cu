@@ -220,7 +220,10 @@ const uint8_t *stage_file(hd_ctx *ctx, const char *path, uint64_t *nbytes) {
       }
     }
   };
-  const unsigned nt = (unsigned)std::min<uint64_t>(16, parts);
+  // reader threads: HAMMINGDIST_READ_THREADS, else 16
+  unsigned want = 16;
+  if (const char *e = std::getenv("HAMMINGDIST_READ_THREADS")) want = (unsigned)std::max(1, std::atoi(e));
+  const unsigned nt = (unsigned)std::min<uint64_t>(want, parts);
   if (nt <= 1) {
     work();
   } else {
@@ -1307,13 +1310,18 @@ int hd_pairwise_lt_files(hd_ctx *ctx, uint64_t count, const char *const *paths,
                      [&](uint64_t a, uint64_t b) { return size[a] > size[b]; });
     // readers: 8 MB parts of the files in that order, shared by all reader
     // threads, never waiting for the GPU; a file is read when its last part is
-    std::vector<int> fds(count, -1);
+    struct Fds {  // closed on every way out
+      std::vector<int> v;
+      ~Fds() {
+        for (int fd : v)
+          if (fd >= 0) ::close(fd);
+      }
+    } fdset;
+    fdset.v.assign(count, -1);
+    std::vector<int> &fds = fdset.v;
     for (uint64_t i = 0; i < count; ++i) {
       fds[i] = ::open(paths[i], O_RDONLY);
-      if (fds[i] < 0) {
-        for (uint64_t j = 0; j < i; ++j) ::close(fds[j]);
-        fail(HD_ERR_IO, open_failed(paths[i]));
-      }
+      if (fds[i] < 0) fail(HD_ERR_IO, open_failed(paths[i]));
     }
     struct Part {
       uint64_t file, off, len;
@@ -1507,7 +1515,6 @@ int hd_pairwise_lt_files(hd_ctx *ctx, uint64_t count, const char *const *paths,
       set_err(e.code, e.msg);
     }
     for (auto &t : threads) t.join();
-    for (int fd : fds) ::close(fd);
     {
       std::lock_guard<std::mutex> lk(mu);
       launcher_done = true;

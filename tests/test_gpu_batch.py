@@ -183,3 +183,27 @@ def test_pipelined_file_batch_errors(ctx, tmp_path):
     # the context stays usable
     outs, _ = ctx.pairwise_lt_files([good, good])
     assert [list(x) for x in outs] == [[1], [1]]
+
+
+def test_file_batch_cpu_semantics(tmp_path):
+    # use_gpu=False semantics through the pipelined batch: low-diversity files
+    # take the sparse rule (5/6-plane kernels), others the dense rule; every
+    # matrix equals the per-file call and the oracle's CPU semantics
+    rng = np.random.default_rng(77)
+    files, fastas = [], []
+    for k in range(10):
+        n = int(rng.integers(20, 400))
+        L = int(rng.choice([500, 2000, 3001]))
+        p = 1e-4 if k % 2 else 2e-2
+        rows, _, _ = synth.alignment(n, L, p=p, seed=700 + k, dup_frac=0.2, dash_max=20)
+        fa = synth.to_fasta(rows)
+        files.append(write(tmp_path, f"c{k}.fasta", fa))
+        fastas.append(fa)
+    for incl_x in (False, True):
+        got = hd.from_fasta_batch(files, use_gpu=False, include_x=incl_x, remove_duplicates=True)
+        for f, fa, ds in zip(files, fastas, got):
+            ref = hd.from_fasta(f, use_gpu=False, include_x=incl_x, remove_duplicates=True)
+            np.testing.assert_array_equal(np.asarray(ds.lt_array), np.asarray(ref.lt_array))
+            seqs, _ = o.read_fasta(fa, remove_duplicates=True)
+            want, _ = o.lt_cpu(seqs, include_x=incl_x)
+            np.testing.assert_array_equal(np.asarray(ds.lt_array), want)
