@@ -241,6 +241,23 @@ const uint8_t *stage_file(hd_ctx *ctx, const char *path, uint64_t *nbytes) {
   return dev;
 }
 
+// The records of the FASTA file in the context's input buffer, parsed once
+// per (file, record limit): a second call on the same unchanged file (e.g.
+// fasta_reference_distances after from_fasta) reuses them.
+hd::Records &file_records(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64_t n_limit) {
+  if (ctx->parsed && !ctx->file_tag.empty() && ctx->parsed_tag == ctx->file_tag &&
+      ctx->parsed_limit == n_limit) {
+    hd::trace_mark(ctx, "records already parsed");
+    return *static_cast<hd::Records *>(ctx->parsed.get());
+  }
+  ctx->parsed.reset();
+  auto rec = std::make_shared<hd::Records>(hd::parse_fasta(ctx, d, nbytes, n_limit));
+  ctx->parsed = rec;
+  ctx->parsed_tag = ctx->file_tag;
+  ctx->parsed_limit = n_limit;
+  return *rec;
+}
+
 // Writes zeros over a large host output on up to 16 threads: the first touch
 // of fresh pageable pages costs several ms per 100 MB on one thread. Called
 // after the kernel is launched, so it runs while the GPU computes and the copy
@@ -426,9 +443,14 @@ void stream_lt_text(hd_ctx *ctx, uint64_t n, int dtype_bytes, const char *path, 
 
 // fasta_reference_distances (src/hamming.cc:104-141) over FASTA bytes already
 // on the device: parse, one distance per record, copy to a malloc'd array.
+// from_file: d is the context's input buffer holding a file (stage_file), so
+// its parsed records may be reused
 void reference_distances_of(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, const char *ref,
-                            uint64_t ref_len, int include_x, uint32_t **out, uint64_t *n_out) {
-  hd::Records rec = hd::parse_fasta(ctx, d, nbytes, 0);
+                            uint64_t ref_len, int include_x, uint32_t **out, uint64_t *n_out,
+                            bool from_file) {
+  hd::Records parsed;
+  if (!from_file) parsed = hd::parse_fasta(ctx, d, nbytes, 0);
+  const hd::Records &rec = from_file ? file_records(ctx, d, nbytes, 0) : parsed;
   hd::trace_mark(ctx, "parse");
   if (rec.max_len > ref_len)
     fail(HD_ERR_REF_LENGTH, "Error: a sequence is longer than the reference sequence");
@@ -456,8 +478,10 @@ void reference_distances_of(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, cons
 
 // fasta_sequence_indices (src/hamming.cc:76-102) over FASTA bytes on the device.
 void sequence_indices_of(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64_t n_limit,
-                         uint64_t **out, uint64_t *n_out) {
-  hd::Records rec = hd::parse_fasta(ctx, d, nbytes, n_limit);
+                         uint64_t **out, uint64_t *n_out, bool from_file) {
+  hd::Records parsed;
+  if (!from_file) parsed = hd::parse_fasta(ctx, d, nbytes, n_limit);
+  const hd::Records &rec = from_file ? file_records(ctx, d, nbytes, n_limit) : parsed;
   std::vector<uint64_t> idx;
   uint64_t nu = 0;
   DevBuf rows = hd::dedupe(ctx, rec, &nu, idx);
@@ -537,6 +561,7 @@ void hd_ctx_destroy(hd_ctx *ctx) {
   for (hd_ctx *w : ctx->workers) hd_ctx_destroy(w);
   ctx->workers.clear();
   cudaSetDevice(ctx->device);
+  ctx->parsed.reset();  // its buffers are freed on ctx->stream
   ctx->file.release();
   if (ctx->pin) cudaFreeHost(ctx->pin);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -609,7 +634,7 @@ int hd_alignment_from_fasta_file(hd_ctx *ctx, const char *path, int remove_dupli
     uint64_t nbytes = 0;
     const uint8_t *d = stage_file(ctx, path, &nbytes);
     hd::trace_mark(ctx, "read + upload");
-    hd::Records rec = hd::parse_fasta(ctx, d, nbytes, n_limit);
+    hd::Records &rec = file_records(ctx, d, nbytes, n_limit);
     hd::trace_mark(ctx, "parse");
     *out = build_alignment(ctx, rec, remove_duplicates, include_x, semantics);
     hd::trace_end(ctx);
@@ -874,7 +899,7 @@ int hd_reference_distances(hd_ctx *ctx, const char *ref, uint64_t ref_len, const
     hd::trace_begin(ctx, "hd_reference_distances");
     const uint8_t *d = stage_input(ctx, fasta, nbytes, 0);
     hd::trace_mark(ctx, "upload");
-    reference_distances_of(ctx, d, nbytes, ref, ref_len, include_x, out, n_out);
+    reference_distances_of(ctx, d, nbytes, ref, ref_len, include_x, out, n_out, false);
   });
 }
 
@@ -888,7 +913,7 @@ int hd_reference_distances_file(hd_ctx *ctx, const char *ref, uint64_t ref_len, 
     uint64_t nbytes = 0;
     const uint8_t *d = stage_file(ctx, path, &nbytes);
     hd::trace_mark(ctx, "read + upload");
-    reference_distances_of(ctx, d, nbytes, ref, ref_len, include_x, out, n_out);
+    reference_distances_of(ctx, d, nbytes, ref, ref_len, include_x, out, n_out, true);
   });
 }
 
@@ -916,7 +941,7 @@ int hd_fasta_sequence_indices(hd_ctx *ctx, const char *fasta, uint64_t nbytes, u
   *n_out = 0;
   return guard(ctx, [&] {
     const uint8_t *d = stage_input(ctx, fasta, nbytes, 0);
-    sequence_indices_of(ctx, d, nbytes, n_limit, out, n_out);
+    sequence_indices_of(ctx, d, nbytes, n_limit, out, n_out, false);
   });
 }
 
@@ -928,7 +953,7 @@ int hd_fasta_sequence_indices_file(hd_ctx *ctx, const char *path, uint64_t n_lim
   return guard(ctx, [&] {
     uint64_t nbytes = 0;
     const uint8_t *d = stage_file(ctx, path, &nbytes);
-    sequence_indices_of(ctx, d, nbytes, n_limit, out, n_out);
+    sequence_indices_of(ctx, d, nbytes, n_limit, out, n_out, true);
   });
 }
 

@@ -10,6 +10,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <utility>
 #include <vector>
@@ -111,6 +112,11 @@ struct hd_ctx {
   hd::DevBuf file;                // device copy of the last FASTA input
   // identity of the file whose bytes `file` holds (empty: none or other bytes)
   std::string file_tag;
+  // records parsed from that file (an hd::Records), valid while parsed_tag ==
+  // file_tag, for the record limit parsed_limit
+  std::shared_ptr<void> parsed;
+  std::string parsed_tag;
+  uint64_t parsed_limit = 0;
   // autotuned kernel configurations: key = (n bucket, L bucket, dtype)
   std::vector<std::pair<uint32_t, std::pair<int, int>>> tune;
   // child contexts (own streams) for concurrent ingest of many inputs
