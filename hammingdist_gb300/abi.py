@@ -32,6 +32,7 @@ SIGNATURES = {
     "hd_ctx_stream": (vp, [vp]),
     "hd_alignment_from_fasta": (ci, [vp, vp, u64, ci, ci, u64, ci, ci, P(vp)]),
     "hd_alignment_from_fasta_file": (ci, [vp, cp, ci, u64, ci, ci, P(vp)]),
+    "hd_pairwise_lt_fasta_file": (ci, [vp, cp, ci, ci, i64, vp, vp, P(vp)]),
     "hd_alignment_from_sequences": (ci, [vp, vp, vp, u64, ci, ci, P(vp)]),
     "hd_alignment_info": (ci, [vp, P(u64), P(u64), P(u64), P(ci)]),
     "hd_alignment_sequence_indices": (ci, [vp, vp]),
@@ -215,6 +216,27 @@ class Context:
                                                        int(include_x), semantics,
                                                        ctypes.byref(a)))
         return Alignment(self, a)
+
+    def pairwise_lt_fasta_file(self, path, dtype=np.uint8, max_distance=None,
+                               remove_duplicates=False):
+        """from_fasta(use_gpu=True) of a file in one call (distances overlap
+        the read for large files): (lower triangle, Alignment)."""
+        dt = np.dtype(dtype)
+        md = np.iinfo(dt).max if max_distance is None else max_distance
+        box = {}
+
+        @OUTPUT_FN
+        def alloc(user, index, n_rows, entries):
+            arr = np.empty(max(int(entries), 1), dtype=dt)
+            box["lt"] = arr[: int(entries)]
+            return arr.ctypes.data
+
+        a = vp()
+        self._check(lib().hd_pairwise_lt_fasta_file(self.h, os.fsencode(path),
+                                                    int(remove_duplicates), dt.itemsize, int(md),
+                                                    ctypes.cast(alloc, vp), None,
+                                                    ctypes.byref(a)))
+        return box["lt"], Alignment(self, a)
 
     def alignment_from_sequences(self, seqs, include_x=False, semantics=SEM_GPU) -> Alignment:
         seqs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]

@@ -1,12 +1,14 @@
 // The C ABI (include/hammingdist_gb300.h): argument checks, error mapping,
 // host<->device movement and the orchestration of the device stages.
 #include <fcntl.h>
+#include <sys/mman.h>
 #include <sys/stat.h>
 #include <unistd.h>
 
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cerrno>
 #include <condition_variable>
 #include <deque>
 #include <mutex>
@@ -160,11 +162,224 @@ std::string file_tag(const char *path, const struct stat &sb) {
   return std::string(path) + buf;
 }
 
-// Reads a FASTA file into the context's device input buffer: up to 16
-// threads pread 8 MB parts into pinned staging, and each part is copied to
-// the device as soon as it is read, so the upload runs under the read. If the
-// buffer already holds this file, unchanged, nothing is read or copied.
-// Returns the device bytes; *nbytes = the file size.
+// Worker threads for a file read: pread into staging, or populating a
+// mapping that is not all in the page cache (the workers then read it from
+// storage), HAMMINGDIST_READ_THREADS, else 16; populating a mapping of a
+// cached file, HAMMINGDIST_MAP_THREADS, else 1 (page-table updates from more
+// threads contend and are slower: 598 MB took 3.4 ms to upload with 1, 4.0 ms
+// with 16).
+unsigned read_threads(bool cached_map) {
+  const char *e = std::getenv(cached_map ? "HAMMINGDIST_MAP_THREADS" : "HAMMINGDIST_READ_THREADS");
+  return e ? (unsigned)std::max(1, std::atoi(e)) : cached_map ? 1u : 16u;
+}
+
+// Whether every page of a mapping is in the page cache.
+bool all_cached(void *map, size_t len) {
+  const size_t page = (size_t)::sysconf(_SC_PAGESIZE);
+  std::vector<unsigned char> v(hd::ceil_div(len, page));
+  if (::mincore(map, len, v.data()) != 0) return false;
+  for (unsigned char c : v)
+    if (!(c & 1)) return false;
+  return true;
+}
+
+// Background reader of a file into a device buffer. Worker threads take 8 MB
+// parts in file order; one uploader thread copies the parts that are ready to
+// the device, in file order, on ctx->up, and records an event after each.
+//   mapped (ctx->map_files): the file is mapped read-only and a worker
+//     populates a part's page-table entries (MADV_POPULATE_READ, which also
+//     reads the part from storage if it is not cached); the copy then reads
+//     the page cache directly, with no CPU copy.
+//   staged: a worker preads a part into the context's pinned staging, which
+//     is copied.
+// host() holds the file's bytes [0, prefix_bytes()); wait_bytes(x) waits
+// until it holds [0, x); stream_wait_bytes(s, x) makes stream s wait for the
+// copies of [0, x) only, not for the copies queued after them. The destructor
+// stops the threads, joins them, waits for the copies, unmaps and closes.
+struct PartReader {
+  hd_ctx *ctx;
+  const char *path;
+  uint64_t n;
+  uint8_t *dev;
+  static constexpr uint64_t kPart = 8ull << 20;
+  static constexpr uint64_t kCopyParts = 8;  // parts per copy at most
+  uint64_t parts;
+  int fd = -1;
+  void *map = nullptr;
+  size_t map_len = 0;
+  char *host_ = nullptr;  // the mapping, or pinned staging
+  std::atomic<uint64_t> next{0};
+  std::atomic<int> bad{0};  // 1 = read error, 2 = copy error, 3 = stopped
+  std::mutex mu;
+  std::condition_variable cv;
+  std::vector<char> done;
+  uint64_t prefix = 0;  // parts [0, prefix) on the host
+  uint64_t queued = 0;  // parts [0, queued) copies queued on ctx->up, events recorded
+  std::vector<std::thread> th;
+
+  PartReader(hd_ctx *c, const char *p, uint64_t bytes, uint8_t *d)
+      : ctx(c), path(p), n(bytes), dev(d), parts(hd::ceil_div(bytes, kPart)), done(parts, 0) {}
+  ~PartReader() {
+    fault(3);
+    join();
+    cudaStreamSynchronize(ctx->up);
+    if (map) ::munmap(map, map_len);
+    if (fd >= 0) ::close(fd);
+  }
+  const char *host() const { return host_; }
+
+  void start() {
+    fd = ::open(path, O_RDONLY);
+    if (fd < 0) fail(HD_ERR_IO, open_failed(path));
+    if (ctx->map_files && n) {
+      const uint64_t page = (uint64_t)::sysconf(_SC_PAGESIZE);
+      const size_t len = (size_t)hd::round_up(n, page);
+      void *m = ::mmap(nullptr, len, PROT_READ, MAP_SHARED, fd, 0);
+      if (m != MAP_FAILED) {
+        map = m;
+        map_len = len;
+        host_ = static_cast<char *>(m);
+      }
+    }
+    if (!host_) {
+      if (n + 1 > ctx->pin_cap) {
+        if (ctx->pin) cudaFreeHost(ctx->pin);
+        ctx->pin = nullptr;
+        ctx->pin_cap = 0;
+        const size_t cap = (size_t)((n + 1) * 5 / 4 + (1 << 20));
+        HD_CUDA(cudaHostAlloc(&ctx->pin, cap, cudaHostAllocDefault));
+        ctx->pin_cap = cap;
+      }
+      host_ = static_cast<char *>(ctx->pin);
+    }
+    while (ctx->part_ev.size() < parts + 1) {
+      cudaEvent_t e;
+      HD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      ctx->part_ev.push_back(e);
+    }
+    // the device buffer is allocated (and earlier work on it ordered) on
+    // ctx->stream: the copies on ctx->up come after that
+    HD_CUDA(cudaEventRecord(ctx->part_ev[parts], ctx->stream));
+    HD_CUDA(cudaStreamWaitEvent(ctx->up, ctx->part_ev[parts], 0));
+    if (parts) th.emplace_back([this] { upload(); });
+    const bool cached_map = map && all_cached(map, map_len);
+    const unsigned nt = (unsigned)std::min<uint64_t>(read_threads(cached_map), parts);
+    for (unsigned t = 0; t < nt; ++t) th.emplace_back([this] { work(); });
+  }
+  void join() {
+    for (auto &x : th)
+      if (x.joinable()) x.join();
+  }
+  bool read_part(uint64_t off, uint64_t len) {
+    if (map) {
+      char *a = host_ + off;  // off is a multiple of 8 MB: page aligned
+      for (;;) {
+        if (::madvise(a, (size_t)len, MADV_POPULATE_READ) == 0) return true;
+        if (errno == EINTR || errno == EAGAIN) continue;
+        if (errno != EINVAL) return false;  // EFAULT/EIO: the file shrank or cannot be read
+        // a kernel without MADV_POPULATE_READ: touch one byte per page
+        const uint64_t page = (uint64_t)::sysconf(_SC_PAGESIZE);
+        volatile const char *v = a;
+        char sink = 0;
+        for (uint64_t o = 0; o < len; o += page) sink ^= v[o];
+        (void)sink;
+        return true;
+      }
+    }
+    uint64_t got = 0;
+    while (got < len) {
+      const ssize_t r = ::pread(fd, host_ + off + got, (size_t)(len - got), (off_t)(off + got));
+      if (r <= 0) return false;
+      got += (uint64_t)r;
+    }
+    return true;
+  }
+  void work() {
+    for (;;) {
+      const uint64_t k = next.fetch_add(1);
+      if (k >= parts || bad.load()) return;
+      const uint64_t off = k * kPart;
+      if (!read_part(off, std::min(kPart, n - off))) {
+        fault(1);
+        return;
+      }
+      std::lock_guard<std::mutex> lk(mu);
+      done[k] = 1;
+      while (prefix < parts && done[prefix]) ++prefix;
+      cv.notify_all();
+    }
+  }
+  // the host prefix, in order, up to kCopyParts parts per copy
+  void upload() {
+    if (cudaSetDevice(ctx->device) != cudaSuccess) {
+      fault(2);
+      return;
+    }
+    for (uint64_t k = 0; k < parts;) {
+      uint64_t e;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return bad.load() || prefix > k; });
+        if (bad.load()) return;
+        e = std::min(prefix, k + kCopyParts);
+      }
+      const uint64_t off = k * kPart, len = std::min(e * kPart, n) - off;
+      if (cudaMemcpyAsync(dev + off, host_ + off, len, cudaMemcpyHostToDevice, ctx->up) !=
+          cudaSuccess) {
+        fault(2);
+        return;
+      }
+      for (uint64_t j = k; j < e; ++j)
+        if (cudaEventRecord(ctx->part_ev[j], ctx->up) != cudaSuccess) {
+          fault(2);
+          return;
+        }
+      std::lock_guard<std::mutex> lk(mu);
+      queued = k = e;
+      cv.notify_all();
+    }
+  }
+  void fault(int code) {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!bad.load()) bad = code;
+    cv.notify_all();
+  }
+  uint64_t prefix_bytes() {
+    std::lock_guard<std::mutex> lk(mu);
+    return std::min(n, prefix * kPart);
+  }
+  bool wait_bytes(uint64_t x) {
+    std::unique_lock<std::mutex> lk(mu);
+    cv.wait(lk, [&] { return bad.load() || std::min(n, prefix * kPart) >= std::min(x, n); });
+    return !bad.load();
+  }
+  // stream s waits for the copies of bytes [0, x); false after an error
+  bool stream_wait_bytes(cudaStream_t s, uint64_t x) {
+    const uint64_t k = hd::ceil_div(std::min(x, n), kPart);
+    if (k == 0) return !bad.load();
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv.wait(lk, [&] { return bad.load() || queued >= k; });
+      if (bad.load()) return false;
+    }
+    return cudaStreamWaitEvent(s, ctx->part_ev[k - 1], 0) == cudaSuccess;
+  }
+  // waits for the whole file: ctx->stream then waits for every copy; throws
+  // HD_ERR_IO after a read error, HD_ERR_CUDA after a copy error
+  void finish() {
+    const bool ok = stream_wait_bytes(ctx->stream, n);
+    join();
+    if (!ok || bad.load()) {
+      if (bad.load() == 1) fail(HD_ERR_IO, open_failed(path));
+      fail(HD_ERR_CUDA, "cudaMemcpyAsync of the FASTA file failed");
+    }
+  }
+};
+
+// Reads a FASTA file into the context's device input buffer with a
+// PartReader: 8 MB parts are copied as they become ready, so the upload runs
+// under the read. If the buffer already holds this file, unchanged, nothing
+// is read or copied. Returns the device bytes; *nbytes = the file size.
 const uint8_t *stage_file(hd_ctx *ctx, const char *path, uint64_t *nbytes) {
   struct stat sb;
   if (!path || ::stat(path, &sb) != 0 || !S_ISREG(sb.st_mode)) fail(HD_ERR_IO, open_failed(path));
@@ -180,62 +395,11 @@ const uint8_t *stage_file(hd_ctx *ctx, const char *path, uint64_t *nbytes) {
     ctx->file.release();
     ctx->file = DevBuf(hd::round_up(n + 16, 1 << 20), ctx->stream);
   }
-  if (n + 1 > ctx->pin_cap) {
-    if (ctx->pin) cudaFreeHost(ctx->pin);
-    ctx->pin = nullptr;
-    ctx->pin_cap = 0;
-    const size_t cap = (size_t)((n + 1) * 5 / 4 + (1 << 20));
-    HD_CUDA(cudaHostAlloc(&ctx->pin, cap, cudaHostAllocDefault));
-    ctx->pin_cap = cap;
-  }
-  const int fd = ::open(path, O_RDONLY);
-  if (fd < 0) fail(HD_ERR_IO, open_failed(path));
-  char *pin = static_cast<char *>(ctx->pin);
   uint8_t *dev = ctx->file.as<uint8_t>();
-  const uint64_t kPart = 8ull << 20, parts = hd::ceil_div(n, kPart);
-  std::atomic<uint64_t> next{0};
-  std::atomic<int> bad{0};  // 1 = read error, 2 = copy error
-  auto work = [&] {
-    if (cudaSetDevice(ctx->device) != cudaSuccess) {
-      bad = 2;
-      return;
-    }
-    for (;;) {
-      const uint64_t k = next.fetch_add(1);
-      if (k >= parts || bad.load()) return;
-      const uint64_t off = k * kPart, len = std::min(kPart, n - off);
-      uint64_t got = 0;
-      while (got < len) {
-        const ssize_t r = ::pread(fd, pin + off + got, (size_t)(len - got), (off_t)(off + got));
-        if (r <= 0) {
-          bad = 1;
-          return;
-        }
-        got += (uint64_t)r;
-      }
-      if (cudaMemcpyAsync(dev + off, pin + off, len, cudaMemcpyHostToDevice, ctx->stream) !=
-          cudaSuccess) {
-        bad = 2;
-        return;
-      }
-    }
-  };
-  // reader threads: HAMMINGDIST_READ_THREADS, else 16
-  unsigned want = 16;
-  if (const char *e = std::getenv("HAMMINGDIST_READ_THREADS")) want = (unsigned)std::max(1, std::atoi(e));
-  const unsigned nt = (unsigned)std::min<uint64_t>(want, parts);
-  if (nt <= 1) {
-    work();
-  } else {
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nt; ++t) th.emplace_back(work);
-    for (auto &x : th) x.join();
-  }
-  ::close(fd);
-  if (bad.load()) {
-    cudaStreamSynchronize(ctx->stream);  // copies already queued still read the staging
-    if (bad.load() == 1) fail(HD_ERR_IO, open_failed(path));
-    fail(HD_ERR_CUDA, "cudaMemcpyAsync of the FASTA file failed");
+  {
+    PartReader rd(ctx, path, n, dev);
+    rd.start();
+    rd.finish();
   }
   ctx->file_tag = tag;
   return dev;
@@ -517,6 +681,16 @@ int hd_ctx_create(int device, hd_ctx **out) {
     HD_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+    HD_CUDA(cudaStreamCreateWithFlags(&ctx->up, cudaStreamNonBlocking));
+    // files are copied from their page-cache mapping where the device reads
+    // pageable memory through the host's page tables (Grace: NVLink-C2C);
+    // HAMMINGDIST_READ_MODE=pread keeps the pread + pinned staging order
+    int host_pt = 0;
+    HD_CUDA(cudaDeviceGetAttribute(&host_pt, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                                   device));
+    ctx->map_files = host_pt == 1;
+    if (const char *m = std::getenv("HAMMINGDIST_READ_MODE"))
+      if (std::string(m) == "pread") ctx->map_files = 0;
     HD_CUDA(cudaEventCreate(&ctx->ev_start));
     HD_CUDA(cudaEventCreate(&ctx->ev_stop));
     HD_CUDA(cudaMalloc(&ctx->d_status, 64));
@@ -569,8 +743,11 @@ void hd_ctx_destroy(hd_ctx *ctx) {
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
   if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
   for (cudaEvent_t e : ctx->trace.pool) cudaEventDestroy(e);
+  if (ctx->up) cudaStreamSynchronize(ctx->up);
+  for (cudaEvent_t e : ctx->part_ev) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->side) cudaStreamDestroy(ctx->side);
+  if (ctx->up) cudaStreamDestroy(ctx->up);
   delete ctx;
 }
 
@@ -637,6 +814,233 @@ int hd_alignment_from_fasta_file(hd_ctx *ctx, const char *path, int remove_dupli
     hd::Records &rec = file_records(ctx, d, nbytes, n_limit);
     hd::trace_mark(ctx, "parse");
     *out = build_alignment(ctx, rec, remove_duplicates, include_x, semantics);
+    hd::trace_end(ctx);
+  });
+}
+
+int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicates,
+                              int dtype_bytes, int64_t max_distance, hd_output_fn out_fn,
+                              void *user, hd_alignment **aln_out) {
+  if (!ctx || !path || !out_fn || !aln_out) return HD_ERR_ARG;
+  *aln_out = nullptr;
+  return guard(ctx, [&] {
+    check_dtype(dtype_bytes);
+    const uint32_t md = clamp_max(max_distance, dtype_bytes);
+    hd::trace_begin(ctx, "hd_pairwise_lt_fasta_file");
+    struct stat sb;
+    if (::stat(path, &sb) != 0 || !S_ISREG(sb.st_mode)) fail(HD_ERR_IO, open_failed(path));
+    const uint64_t n = (uint64_t)sb.st_size;
+    const std::string tag = file_tag(path, sb);
+    // the whole matrix after the whole file: the file call + one pairwise call
+    auto whole = [&] {
+      hd_alignment *a = nullptr;
+      uint64_t nbytes = 0;
+      const uint8_t *d = stage_file(ctx, path, &nbytes);
+      hd::trace_mark(ctx, "read + upload");
+      hd::Records &rec = file_records(ctx, d, nbytes, 0);
+      hd::trace_mark(ctx, "parse");
+      a = build_alignment(ctx, rec, remove_duplicates, 0, HD_SEM_GPU);
+      std::unique_ptr<hd_alignment> own(a);
+      const uint64_t entries = a->n_rows < 2 ? 0 : tri(a->n_rows);
+      void *host = out_fn(user, 0, a->n_rows, entries);
+      if (!host && entries) fail(HD_ERR_ARG, "output callback returned no buffer");
+      if (entries) {
+        DevBuf d_out(entries * dtype_bytes, ctx->stream);
+        hd::pairwise_tiles(ctx, a, dtype_bytes, md, d_out.p, 0, 0,
+                           (uint32_t)hd::ceil_div(a->n_rows, hd::kTile));
+        hd::trace_mark(ctx, "pairwise");
+        prefault_host(host, entries * dtype_bytes);
+        HD_CUDA(cudaMemcpyAsync(host, d_out.p, entries * dtype_bytes, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        HD_CUDA(cudaStreamSynchronize(ctx->stream));
+        check_status(ctx);
+      }
+      *aln_out = own.release();
+    };
+    // small files, or a file already on the device: nothing to overlap
+    if (n < (64ull << 20) || (!ctx->file_tag.empty() && ctx->file_tag == tag)) {
+      whole();
+      hd::trace_end(ctx);
+      return;
+    }
+    ctx->file_tag.clear();
+    ctx->parsed.reset();
+    if (ctx->file.bytes < n + 16) {
+      ctx->file.release();
+      ctx->file = DevBuf(hd::round_up(n + 16, 1 << 20), ctx->stream);
+    }
+    uint8_t *dev = ctx->file.as<uint8_t>();
+    auto reader = std::make_unique<PartReader>(ctx, path, n, dev);
+    reader->start();
+    const char *text = reader->host();
+    hd::trace_mark(ctx, "setup");
+    auto read_all = [&] {
+      reader->finish();
+      ctx->file_tag = tag;
+    };
+    // split at the first record header at or after 40% of the file
+    uint64_t B = 0;
+    {
+      const uint64_t target = n / 10 * 4;
+      uint64_t pos = target;
+      while (!B) {
+        if (!reader->wait_bytes(std::min(n, pos + PartReader::kPart))) break;
+        const uint64_t avail = reader->prefix_bytes();
+        for (; pos < avail; ++pos)
+          if (text[pos] == '>' && text[pos - 1] == '\n') {
+            B = pos;
+            break;
+          }
+        if (avail >= n) break;
+      }
+    }
+    hd::trace_mark(ctx, "first part read");
+    hd::Records recA;
+    if (B && !reader->stream_wait_bytes(ctx->stream, B)) read_all();  // reports the error
+    if (B) recA = hd::parse_fasta(ctx, dev, B, 0);
+    if (!B || recA.gathered.p || recA.n == 0 || recA.len0 == 0 || !recA.all_equal) {
+      // multi-line records, no header past 40%, or an input the whole path
+      // reports on: the matrix after the whole file
+      recA = hd::Records();
+      read_all();
+      whole();
+      hd::trace_end(ctx);
+      return;
+    }
+    hd::trace_mark(ctx, "first part uploaded + parsed");
+    const uint64_t L = recA.len0, words = words_for(L);
+    uint64_t KA = recA.n;
+    std::vector<uint64_t> seqA;
+    DevBuf uniqA;
+    if (remove_duplicates) uniqA = hd::dedupe(ctx, recA, &KA, seqA);
+    // rows that can still come: a record of L sites takes at least L + 2
+    // bytes (">\n" and the sites; the last one may lack its '\n')
+    const uint64_t R_max = recA.n + (n - B) / (L + 2) + 1;
+    auto owner = std::make_unique<hd_alignment>();
+    owner->ctx = ctx;
+    owner->device = ctx->device;
+    owner->length = L;
+    owner->words = words;
+    owner->rule = HD_RULE_AND;
+    owner->groups = 1;
+    owner->planes = 4;
+    owner->plane_buf[0] = DevBuf(R_max * words * 16, ctx->stream);
+    uint4 *g0 = owner->plane_buf[0].as<uint4>();
+    hd::pack_rows_and(ctx, recA, remove_duplicates ? uniqA.as<uint64_t>() : nullptr, KA, L, words, g0);
+    DevBuf d_lt((R_max < 2 ? 1 : tri(R_max)) * dtype_bytes, ctx->stream);
+    const hd::TileConfig cfg =
+        hd::tile_config_for(ctx, KA * (n / std::max<uint64_t>(B, 1)), L, dtype_bytes);
+    const uint32_t T = (uint32_t)cfg.tile;
+    // the first part's complete tile rows run on the side stream while the
+    // rest of the file is read; 16 SMs stay free for the second part's ingest
+    cudaEvent_t ev = nullptr;
+    HD_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    struct SideSync {  // waits for the side stream before any buffer is freed
+      hd_ctx *c;
+      cudaEvent_t e;
+      ~SideSync() {
+        cudaStreamSynchronize(c->side);
+        cudaEventDestroy(e);
+      }
+    } side_sync{ctx, ev};
+    hd::PairLaunchPlan planA, planB;
+    hd_alignment viewA;
+    viewA.base = owner.get();
+    viewA.n_rows = KA;
+    viewA.length = L;
+    viewA.words = words;
+    viewA.device = ctx->device;
+    const uint32_t tA = (uint32_t)(KA / T);
+    uint64_t tiles = 0;
+    if (tA > 0) {
+      HD_CUDA(cudaEventRecord(ev, ctx->stream));
+      HD_CUDA(cudaStreamWaitEvent(ctx->side, ev, 0));
+      std::vector<hd::PairJobSpec> specs(1);
+      specs[0].aln = &viewA;
+      specs[0].dtype = dtype_bytes;
+      specs[0].max_dist = md;
+      specs[0].d_out = d_lt.p;
+      specs[0].cfg = cfg;
+      specs[0].tile_lo = 0;
+      specs[0].tile_hi = tA;
+      hd::prepare_pairwise_jobs(ctx, specs, ctx->side, &planA, std::max(1, ctx->sm_count - 16));
+      hd::launch_pairwise_plan(ctx, planA, ctx->side);
+      tiles += ctx->last_pair_tiles;
+    }
+    hd::trace_mark(ctx, "first part ingested");
+    read_all();
+    // parse_fasta reads 16-byte vectors from a 16-byte aligned start: the
+    // second part is parsed from B rounded down. The bytes before B end the
+    // first part's last line; parsed as a FASTA's first line they are skipped
+    // and give an empty record 0, which is dropped.
+    const uint64_t B0 = B & ~15ull;
+    hd::Records recB = hd::parse_fasta(ctx, dev + B0, n - B0, 0);
+    if (!recB.gathered.p && B0 < B) recB = hd::drop_first_record(ctx, std::move(recB));
+    if (recB.gathered.p) {
+      // a multi-line record in the second part: the matrix after the whole file
+      cudaStreamSynchronize(ctx->side);
+      recB = hd::Records();
+      whole();
+      hd::trace_end(ctx);
+      return;
+    }
+    hd::Records all = hd::concat_records(ctx, recA, recB, B0, n);
+    if (!all.all_equal) fail(HD_ERR_LENGTH, kMsgLength);
+    uint64_t K = all.n;
+    DevBuf uniq;
+    std::vector<uint64_t> seq;
+    if (remove_duplicates) {
+      uniq = hd::dedupe(ctx, all, &K, seq);
+    } else {
+      std::vector<uint64_t> iota(all.n);
+      for (uint64_t i = 0; i < all.n; ++i) iota[i] = i;
+      uniq = DevBuf(all.n * 8, ctx->stream);
+      HD_CUDA(cudaMemcpyAsync(uniq.p, iota.data(), all.n * 8, cudaMemcpyHostToDevice, ctx->stream));
+      HD_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    if (K > R_max || K < KA) fail(HD_ERR_CUDA, "streamed ingest: inconsistent row counts");
+    hd::pack_rows_and(ctx, all, uniq.as<uint64_t>() + KA, K - KA, L, words, g0 + KA * words);
+    hd::trace_mark(ctx, "second part ingested");
+    owner->n_rows = K;
+    owner->n_input = all.n;
+    owner->seqidx = std::move(seq);
+    if (!owner->seqidx.empty()) {
+      owner->d_seqidx = DevBuf(owner->seqidx.size() * 8, ctx->stream);
+      HD_CUDA(cudaMemcpyAsync(owner->d_seqidx.p, owner->seqidx.data(), owner->seqidx.size() * 8,
+                              cudaMemcpyHostToDevice, ctx->stream));
+    }
+    const uint32_t tAll = (uint32_t)hd::ceil_div(K, T);
+    if (K >= 2 && tAll > tA) {
+      HD_CUDA(cudaEventRecord(ev, ctx->stream));
+      HD_CUDA(cudaStreamWaitEvent(ctx->side, ev, 0));
+      std::vector<hd::PairJobSpec> specs(1);
+      specs[0].aln = owner.get();
+      specs[0].dtype = dtype_bytes;
+      specs[0].max_dist = md;
+      specs[0].d_out = d_lt.p;
+      specs[0].cfg = cfg;
+      specs[0].tile_lo = tA;
+      specs[0].tile_hi = tAll;
+      hd::prepare_pairwise_jobs(ctx, specs, ctx->side, &planB);
+      hd::launch_pairwise_plan(ctx, planB, ctx->side);
+    }
+    const uint64_t entries = K < 2 ? 0 : tri(K);
+    void *host = out_fn(user, 0, K, entries);
+    if (!host && entries) fail(HD_ERR_ARG, "output callback returned no buffer");
+    if (entries) {
+      prefault_host(host, entries * dtype_bytes);  // while the kernels run
+      HD_CUDA(cudaMemcpyAsync(host, d_lt.p, entries * dtype_bytes, cudaMemcpyDeviceToHost,
+                              ctx->side));
+    }
+    HD_CUDA(cudaStreamSynchronize(ctx->side));
+    HD_CUDA(cudaStreamSynchronize(ctx->stream));
+    hd::trace_mark(ctx, "pairwise + copy");
+    check_status(ctx);
+    // the file and its records stay for later calls on the same file
+    ctx->parsed = std::make_shared<hd::Records>(std::move(all));
+    ctx->parsed_tag = tag;
+    ctx->parsed_limit = 0;
+    *aln_out = owner.release();
     hd::trace_end(ctx);
   });
 }

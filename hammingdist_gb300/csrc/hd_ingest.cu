@@ -741,6 +741,89 @@ __global__ void __launch_bounds__(kPackThreads)
   }
 }
 
+void pack_rows_and(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, uint64_t n_rows,
+                   uint64_t length, uint64_t words, uint4 *g0) {
+  if (!n_rows) return;
+  Table256 t;
+  code_table(kCodesAnd, t.v);
+  const uint64_t jobs = n_rows * hd::ceil_div((words + 31) / 32, (uint64_t)kPackCPG);
+  k_pack<4><<<grid_for(jobs * 32, kPackThreads), kPackThreads, 0, ctx->stream>>>(
+      rec.base, rec.rec_start.as<uint64_t>(), d_rows, n_rows, length, words, t, g0, nullptr);
+  HD_LAUNCHED(ctx);
+}
+
+__global__ void k_concat_starts(const uint64_t *a, uint64_t na, const uint64_t *b, uint64_t nb,
+                                uint64_t b_off, uint64_t *out) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < na) out[i] = a[i];
+  else if (i < na + nb) out[i] = b[i - na] + b_off;
+}
+
+Records concat_records(hd_ctx *ctx, const Records &a, const Records &b, uint64_t b_off,
+                       uint64_t bytes) {
+  cudaStream_t st = ctx->stream;
+  Records r;
+  r.n = a.n + b.n;
+  r.len0 = a.n ? a.len0 : b.len0;
+  r.max_len = a.max_len > b.max_len ? a.max_len : b.max_len;
+  r.all_equal = a.all_equal && b.all_equal && (!a.n || !b.n || a.len0 == b.len0);
+  r.base = a.base;
+  r.bytes = bytes;
+  r.rec_start = DevBuf((r.n ? r.n : 1) * 8, st);
+  r.rec_len = DevBuf((r.n ? r.n : 1) * 8, st);
+  if (r.n) {
+    k_concat_starts<<<grid_for(r.n, 256), 256, 0, st>>>(a.rec_start.as<uint64_t>(), a.n,
+                                                        b.rec_start.as<uint64_t>(), b.n, b_off,
+                                                        r.rec_start.as<uint64_t>());
+    HD_LAUNCHED(ctx);
+    if (a.n)
+      HD_CUDA(cudaMemcpyAsync(r.rec_len.p, a.rec_len.p, a.n * 8, cudaMemcpyDeviceToDevice, st));
+    if (b.n)
+      HD_CUDA(cudaMemcpyAsync(r.rec_len.as<uint64_t>() + a.n, b.rec_len.p, b.n * 8,
+                              cudaMemcpyDeviceToDevice, st));
+  }
+  return r;
+}
+
+__global__ void k_len_range(const uint64_t *len, uint64_t n, unsigned long long *mn,
+                            unsigned long long *mx) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    atomicMin(mn, (unsigned long long)len[i]);
+    atomicMax(mx, (unsigned long long)len[i]);
+  }
+}
+
+Records drop_first_record(hd_ctx *ctx, Records &&b) {
+  cudaStream_t st = ctx->stream;
+  Records r;
+  r.base = b.base;
+  r.bytes = b.bytes;
+  r.n = b.n ? b.n - 1 : 0;
+  r.rec_start = DevBuf((r.n ? r.n : 1) * 8, st);
+  r.rec_len = DevBuf((r.n ? r.n : 1) * 8, st);
+  r.gathered = std::move(b.gathered);
+  if (!r.n) return r;
+  HD_CUDA(cudaMemcpyAsync(r.rec_start.p, b.rec_start.as<uint64_t>() + 1, r.n * 8,
+                          cudaMemcpyDeviceToDevice, st));
+  HD_CUDA(cudaMemcpyAsync(r.rec_len.p, b.rec_len.as<uint64_t>() + 1, r.n * 8,
+                          cudaMemcpyDeviceToDevice, st));
+  DevBuf mm(16, st);
+  const unsigned long long init[2] = {~0ull, 0ull};
+  HD_CUDA(cudaMemcpyAsync(mm.p, init, 16, cudaMemcpyHostToDevice, st));
+  k_len_range<<<grid_for(r.n, 256) > 4096 ? 4096 : grid_for(r.n, 256), 256, 0, st>>>(
+      r.rec_len.as<uint64_t>(), r.n, mm.as<unsigned long long>(), mm.as<unsigned long long>() + 1);
+  HD_LAUNCHED(ctx);
+  unsigned long long h[3] = {0, 0, 0};
+  HD_CUDA(cudaMemcpyAsync(h, mm.p, 16, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaMemcpyAsync(h + 2, r.rec_len.p, 8, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  r.max_len = h[1];
+  r.len0 = h[2];
+  r.all_equal = h[0] == h[1];
+  return r;
+}
+
 void pack_rows(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, hd_alignment *aln) {
   Table256 t;
   int table = aln->rule == HD_RULE_AND ? kCodesAnd

@@ -124,6 +124,13 @@ struct hd_ctx {
   // pinned staging for file reads by this context (grows)
   void *pin = nullptr;
   size_t pin_cap = 0;
+  // file reads: the copies into `file` run on `up`, with one event per 8 MB
+  // part from part_ev (grows). map_files: the device reads pageable host
+  // memory through the host's page tables, so a file's read-only mapping of
+  // the page cache is copied directly (no CPU copy into `pin`).
+  cudaStream_t up = nullptr;
+  std::vector<cudaEvent_t> part_ev;
+  int map_files = 0;
   hd::Trace trace;
 };
 
@@ -340,6 +347,7 @@ inline int planes_of(int rule) { return rule == HD_RULE_AND ? 4 : rule == HD_RUL
 
 // ----------------------------------------------------- stage launchers
 // ingest.cu
+// d_file must be 16-byte aligned (the newline scan reads 16-byte vectors)
 Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_t n_limit);
 Records records_from_offsets(hd_ctx *ctx, const uint8_t *d_bytes, const uint64_t *h_offsets,
                              uint64_t n);
@@ -351,6 +359,16 @@ uint64_t consensus_matches(hd_ctx *ctx, const Records &rec, const uint64_t *d_ro
                            uint64_t n_rows);
 // Packs rows (record ids d_rows, or identity if null) into bit planes.
 void pack_rows(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, hd_alignment *aln);
+// AND-rule planes of n_rows records (d_rows: record indices) into g0
+// (n_rows x words uint4, already allocated)
+void pack_rows_and(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, uint64_t n_rows,
+                   uint64_t length, uint64_t words, uint4 *g0);
+// b without its first record, with len0 / max_len / all_equal recomputed
+Records drop_first_record(hd_ctx *ctx, Records &&b);
+// records of a then b (b's starts shifted by b_off), one base; b parsed from
+// bytes that follow a's in the same buffer
+Records concat_records(hd_ctx *ctx, const Records &a, const Records &b, uint64_t b_off,
+                       uint64_t bytes);
 void reference_distances_device(hd_ctx *ctx, const Records &rec, const uint8_t *d_ref,
                                 int include_x, uint32_t *d_out);
 void alignment_query_distances(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,

@@ -231,6 +231,29 @@ DataSet<T> from_fasta(const std::string &filename, bool include_x, bool remove_d
   auto t0 = std::chrono::steady_clock::now();
   py::gil_scoped_release nogil;
   Aln a;
+  if (use_gpu && !include_x && n == 0) {
+    // one call: for large files the distances overlap the read
+    DataSet<T> ds;
+    hd_output_fn alloc = [](void *user, uint64_t, uint64_t rows, uint64_t entries) -> void * {
+      auto *d = static_cast<DataSet<T> *>(user);
+      d->nsamples = rows;
+      d->result.resize(entries);  // its pages are first touched while the kernels run
+      return d->result.data();
+    };
+    say("Using GPU (use_gpu=True, dense distance rule)...");
+    check(hd_pairwise_lt_fasta_file(c, filename.c_str(), remove_duplicates, sizeof(T), max_distance,
+                                    alloc, &ds, &a.p));
+    say_trace();
+    say("...pre-processing and distance calculation completed in " +
+        std::to_string((long long)ms_since(t0)) + " ms.");
+    if (remove_duplicates) {
+      uint64_t n_in = 0;
+      check(hd_alignment_info(a.p, nullptr, nullptr, &n_in, nullptr));
+      ds.sequence_indices.resize(n_in);
+      check(hd_alignment_sequence_indices(a.p, ds.sequence_indices.data()));
+    }
+    return ds;
+  }
   check(hd_alignment_from_fasta_file(c, filename.c_str(), remove_duplicates, n, include_x,
                                      use_gpu ? HD_SEM_GPU : HD_SEM_CPU, &a.p));
   say_trace();

@@ -102,3 +102,46 @@ def test_file_errors(ctx, tmp_path):
     p.write_bytes(b"")
     with pytest.raises(abi.HDError, match="Empty sequence"):
         ctx.alignment_from_fasta_file(str(p))
+
+
+@pytest.mark.parametrize("mode", ["map", "pread"])
+def test_read_modes(tmp_path, monkeypatch, mode):
+    # HAMMINGDIST_READ_MODE=pread: pread into pinned staging; else, where the
+    # device reads pageable memory through the host's page tables, the file's
+    # mapping is copied directly. Both give the bytes' results: a 72 MB file
+    # (9 parts, more than one copy), and a small one of odd size.
+    from hammingdist_gb300 import abi
+
+    if mode == "pread":
+        monkeypatch.setenv("HAMMINGDIST_READ_MODE", "pread")
+    else:
+        monkeypatch.delenv("HAMMINGDIST_READ_MODE", raising=False)
+    c = abi.Context(0)
+    try:
+        rows, root, _ = synth.alignment(2400, 29903, p=1e-3, seed=5, dup_frac=0.2)
+        big = synth.to_fasta(rows)
+        small = _fasta(synth.random_strings(37, 1001, b"ACGT-", seed=6))[:-1]  # no final '\n'
+        for name, fa in (("big.fasta", big), ("small.fasta", small)):
+            p = tmp_path / name
+            p.write_bytes(fa)
+            a = c.alignment_from_fasta_file(str(p), remove_duplicates=True)
+            b = c.alignment_from_fasta(fa, remove_duplicates=True)
+            np.testing.assert_array_equal(c.pairwise_lt(a), c.pairwise_lt(b))
+            np.testing.assert_array_equal(a.sequence_indices(), b.sequence_indices())
+            a.free()
+            b.free()
+            ref = fa[fa.index(b"\n") + 1:].split(b"\n")[0]
+            os.utime(p)  # a new modification time: read again
+            np.testing.assert_array_equal(c.reference_distances_file(ref, str(p)),
+                                          o.reference_distances(ref, fa))
+        # the streamed from_fasta on the big file
+        p = tmp_path / "big.fasta"
+        st = os.stat(p)
+        os.utime(p, ns=(st.st_atime_ns, st.st_mtime_ns + 1000))
+        lt, aln = c.pairwise_lt_fasta_file(str(p), remove_duplicates=True)
+        b = c.alignment_from_fasta(big, remove_duplicates=True)
+        np.testing.assert_array_equal(lt, c.pairwise_lt(b))
+        aln.free()
+        b.free()
+    finally:
+        c.close()

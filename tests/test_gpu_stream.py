@@ -1,0 +1,141 @@
+"""from_fasta with the distances overlapping the read (hd_pairwise_lt_fasta_file):
+for files of 64 MB or more the first ~40% is ingested and its distances run
+while the rest is read. Every result must equal the plain order (read,
+ingest, distances) bit for bit: duplicates that cross the split, dtypes,
+max_distance, no dedupe, the multi-line fallback, errors after the split, a
+file already on the device, and the module's from_fasta."""
+import numpy as np
+import pytest
+
+from hammingdist_gb300 import synth
+from oracle import hd_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from hammingdist_gb300 import abi
+
+    c = abi.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def big(tmp_path_factory):
+    # 3,000 records x 29,903 sites = 90 MB, 30% duplicates of earlier rows
+    rows, root, _ = synth.alignment(3000, 29903, p=1e-3, seed=41, dup_frac=0.3)
+    fa = synth.to_fasta(rows)
+    path = tmp_path_factory.mktemp("stream") / "big.fasta"
+    path.write_bytes(fa)
+    return str(path), fa, rows
+
+
+def _plain(ctx, path, dtype, md, dedup):
+    a = ctx.alignment_from_fasta(open(path, "rb").read(), remove_duplicates=dedup)
+    lt = ctx.pairwise_lt(a, dtype=dtype, max_distance=md)
+    idx = a.sequence_indices()
+    a.free()
+    return lt, idx
+
+
+def _touch(path):
+    import os
+    import time
+
+    st = time.time_ns()
+    os.utime(path, ns=(st, st))
+
+
+@pytest.mark.parametrize("dtype,md,dedup", [(np.uint8, 255, True), (np.uint16, 65535, True),
+                                            (np.uint8, 7, False), (np.uint16, 300, False)])
+def test_streamed_equals_plain(ctx, big, dtype, md, dedup):
+    path, fa, rows = big
+    _touch(path)  # not on the device: the overlapped order runs
+    lt, aln = ctx.pairwise_lt_fasta_file(path, dtype=dtype, max_distance=md, remove_duplicates=dedup)
+    want, want_idx = _plain(ctx, path, dtype, md, dedup)
+    np.testing.assert_array_equal(lt, want)
+    np.testing.assert_array_equal(aln.sequence_indices(), want_idx)
+    assert aln.n_input == 3000
+    aln.free()
+
+
+def test_streamed_rows_against_oracle(ctx, big):
+    path, fa, rows = big
+    _touch(path)
+    lt, aln = ctx.pairwise_lt_fasta_file(path, remove_duplicates=True)
+    uniq = list(dict.fromkeys(r.tobytes() for r in rows))
+    assert aln.n_rows == len(uniq)
+    pick = np.array([0, 1, 2, len(uniq) // 3, len(uniq) // 2, len(uniq) - 2, len(uniq) - 1])
+    want = o.lt_dense([uniq[i] for i in pick])
+    got = [lt[pick[a] * (pick[a] - 1) // 2 + pick[b]] for a in range(len(pick)) for b in range(a)]
+    np.testing.assert_array_equal(np.array(got, dtype=np.uint8), want)
+    aln.free()
+
+
+def test_already_on_device_and_reference_after(ctx, big):
+    path, fa, rows = big
+    _touch(path)
+    lt1, a1 = ctx.pairwise_lt_fasta_file(path, remove_duplicates=True)
+    lt2, a2 = ctx.pairwise_lt_fasta_file(path, remove_duplicates=True)  # same file, on the device
+    np.testing.assert_array_equal(lt1, lt2)
+    ctx.trace(True)
+    try:
+        rd = ctx.reference_distances_file(rows[0].tobytes(), path)
+        assert "file already on the device" in ctx.trace_last()
+        assert "records already parsed" in ctx.trace_last()
+    finally:
+        ctx.trace(False)
+    np.testing.assert_array_equal(rd, o.reference_distances(rows[0].tobytes(), fa))
+    a1.free()
+    a2.free()
+
+
+def test_multiline_falls_back(ctx, tmp_path):
+    rows, _, _ = synth.alignment(2500, 29903, p=1e-3, seed=42, dup_frac=0.2)
+    out = bytearray()
+    for k, r in enumerate(rows):
+        out += b">s%d\n" % k
+        for i in range(0, len(r), 6000):
+            out += r[i:i + 6000].tobytes() + b"\n"
+    p = tmp_path / "multi.fasta"
+    p.write_bytes(bytes(out))
+    lt, aln = ctx.pairwise_lt_fasta_file(str(p), remove_duplicates=True)
+    want, want_idx = _plain(ctx, str(p), np.uint8, 255, True)
+    np.testing.assert_array_equal(lt, want)
+    np.testing.assert_array_equal(aln.sequence_indices(), want_idx)
+    aln.free()
+
+
+@pytest.mark.parametrize("bad", [b"ACGT", b""])
+def test_error_after_the_split(ctx, tmp_path, big, bad):
+    from hammingdist_gb300 import abi
+
+    path, fa, rows = big
+    p = tmp_path / "bad.fasta"
+    p.write_bytes(fa + b">late\n" + bad + b"\n" + fa[: 10 * 29916])
+    with pytest.raises(abi.HDError, match="same length"):
+        ctx.pairwise_lt_fasta_file(str(p), remove_duplicates=True)
+    # the context stays usable
+    _touch(path)
+    lt, aln = ctx.pairwise_lt_fasta_file(path, remove_duplicates=True)
+    aln.free()
+
+
+def test_module_from_fasta_uses_it(big):
+    import hammingdist_gb300 as hd
+    from hammingdist_gb300 import abi
+
+    path, fa, rows = big
+    _touch(path)
+    ds = hd.from_fasta(path, use_gpu=True, remove_duplicates=True)
+    big_ds = hd.from_fasta_large(path, use_gpu=True, remove_duplicates=True, max_distance=1000)
+    c = abi.Context(0)
+    try:
+        want, want_idx = _plain(c, path, np.uint8, 255, True)
+        want16, _ = _plain(c, path, np.uint16, 1000, True)
+    finally:
+        c.close()
+    np.testing.assert_array_equal(np.asarray(ds.lt_array), want)
+    np.testing.assert_array_equal(np.asarray(big_ds.lt_array), want16)
