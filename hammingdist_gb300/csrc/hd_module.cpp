@@ -370,6 +370,7 @@ py::list from_fasta_batch(const std::vector<std::string> &files, bool include_x,
     hd_last_pairwise_timing(c, &pair_ms, &tiles);
     say("batch of " + std::to_string(k) + " alignments: read, ingest and distances pipelined in " +
         std::to_string(ms_since(t1)) + " ms (" + std::to_string(tiles) + " tiles).");
+    say_trace();
   }
   py::list out;
   for (size_t i = 0; i < k; ++i) {

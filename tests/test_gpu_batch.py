@@ -151,6 +151,8 @@ def test_from_fasta_batch_matches_per_file_calls(tmp_path):
 def test_pipelined_file_batch_abi(ctx, tmp_path):
     # many files of uneven size, some tiny (0 or 1 row after dedupe), through
     # hd_pairwise_lt_files: every matrix and every sequence index vs the oracle
+    from hammingdist_gb300 import abi
+
     rng = np.random.default_rng(21)
     paths, dts, mds, fastas = [], [], [], []
     for k in range(40):
@@ -169,6 +171,15 @@ def test_pipelined_file_batch_abi(ctx, tmp_path):
         want, want_idx = o.from_fasta_dense(fa, remove_duplicates=True, max_distance=md, dtype=dt)
         np.testing.assert_array_equal(out, want)
         np.testing.assert_array_equal(ix, want_idx)
+    # an empty file among the others is reported, and the context stays usable
+    empty = write(tmp_path, "empty.fasta", b"")
+    with pytest.raises(abi.HDError, match="Empty sequence"):
+        ctx.pairwise_lt_files(paths[:3] + [empty] + paths[3:6])
+    outs, _ = ctx.pairwise_lt_files(paths[:2], dtypes=dts[:2], max_distances=mds[:2],
+                                    remove_duplicates=True)
+    for fa, out, dt, md in zip(fastas[:2], outs, dts[:2], mds[:2]):
+        np.testing.assert_array_equal(
+            out, o.from_fasta_dense(fa, remove_duplicates=True, max_distance=md, dtype=dt)[0])
 
 
 def test_pipelined_file_batch_errors(ctx, tmp_path):
@@ -207,3 +218,42 @@ def test_file_batch_cpu_semantics(tmp_path):
             seqs, _ = o.read_fasta(fa, remove_duplicates=True)
             want, _ = o.lt_cpu(seqs, include_x=incl_x)
             np.testing.assert_array_equal(np.asarray(ds.lt_array), want)
+
+
+def test_file_batch_read_modes(tmp_path, monkeypatch):
+    # the file batch's two read orders give the same matrices: the files'
+    # page-cache mappings copied into a device arena (where the device reads
+    # pageable memory through the host's page tables), and
+    # HAMMINGDIST_READ_MODE=pread (readers pread into pinned staging)
+    from hammingdist_gb300 import abi
+
+    rng = np.random.default_rng(33)
+    paths, fastas = [], []
+    for k in range(12):
+        n = int(rng.integers(2, 700))
+        L = int(rng.choice([7, 1000, 29903]))
+        rows, _, _ = synth.alignment(n, L, p=1e-3, seed=900 + k, dup_frac=0.2)
+        fa = synth.to_fasta(rows)
+        paths.append(write(tmp_path, f"m{k}.fasta", fa))
+        fastas.append(fa)
+    got = {}
+    for mode in ("map", "pread"):
+        if mode == "pread":
+            monkeypatch.setenv("HAMMINGDIST_READ_MODE", "pread")
+        else:
+            monkeypatch.delenv("HAMMINGDIST_READ_MODE", raising=False)
+        c = abi.Context(0)
+        try:
+            got[mode] = c.pairwise_lt_files(paths, remove_duplicates=True)
+            empty = write(tmp_path, "e.fasta", b"")
+            with pytest.raises(abi.HDError, match="Empty sequence"):
+                c.pairwise_lt_files(paths[:4] + [empty] + paths[4:])
+        finally:
+            c.close()
+    for fa, a, b, ia, ib in zip(fastas, got["map"][0], got["pread"][0], got["map"][1],
+                                got["pread"][1]):
+        want, want_idx = o.from_fasta_dense(fa, remove_duplicates=True)
+        np.testing.assert_array_equal(a, want)
+        np.testing.assert_array_equal(b, want)
+        np.testing.assert_array_equal(ia, want_idx)
+        np.testing.assert_array_equal(ib, want_idx)
