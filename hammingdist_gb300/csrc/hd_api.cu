@@ -687,6 +687,7 @@ int hd_ctx_create(int device, hd_ctx **out) {
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->up, cudaStreamNonBlocking));
+    HD_CUDA(cudaStreamCreateWithFlags(&ctx->side2, cudaStreamNonBlocking));
     // files are copied from their page-cache mapping where the device reads
     // pageable memory through the host's page tables (Grace: NVLink-C2C);
     // HAMMINGDIST_READ_MODE=pread keeps the pread + pinned staging order
@@ -753,6 +754,7 @@ void hd_ctx_destroy(hd_ctx *ctx) {
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->up) cudaStreamDestroy(ctx->up);
+  if (ctx->side2) cudaStreamDestroy(ctx->side2);
   delete ctx;
 }
 
@@ -883,129 +885,184 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       reader->finish();
       ctx->file_tag = tag;
     };
-    // split at the first record header at or after 40% of the file
-    uint64_t B = 0;
-    {
-      const uint64_t target = n / 10 * 4;
-      uint64_t pos = target;
-      while (!B) {
-        if (!reader->wait_bytes(std::min(n, pos + PartReader::kPart))) break;
+    // the first record header at or after pos (>= 1), 0 if none
+    auto header_at = [&](uint64_t pos) -> uint64_t {
+      for (;;) {
+        if (!reader->wait_bytes(std::min(n, pos + PartReader::kPart))) return 0;
         const uint64_t avail = reader->prefix_bytes();
         for (; pos < avail; ++pos)
-          if (text[pos] == '>' && text[pos - 1] == '\n') {
-            B = pos;
-            break;
-          }
-        if (avail >= n) break;
+          if (text[pos] == '>' && text[pos - 1] == '\n') return pos;
+        if (avail >= n) return 0;
       }
-    }
-    hd::trace_mark(ctx, "first part read");
-    hd::Records recA;
-    if (B && !reader->stream_wait_bytes(ctx->stream, B)) read_all();  // reports the error
-    if (B) recA = hd::parse_fasta(ctx, dev, B, 0);
-    if (!B || recA.gathered.p || recA.n == 0 || recA.len0 == 0 || !recA.all_equal) {
-      // multi-line records, no header past 40%, or an input the whole path
-      // reports on: the matrix after the whole file
-      recA = hd::Records();
+    };
+    // The file is ingested in parts that end at the first record headers
+    // after 20% and 50% of its bytes. After each part the whole prefix is
+    // deduplicated (first occurrences keep their order, so earlier unique
+    // rows keep their positions) and the new unique rows are packed; the tile
+    // rows that are complete then run on the side stream, with 16 SMs left
+    // for the next part's ingest. The last part's tile rows run as two
+    // launches on two streams (the second fills the first's tail), split at
+    // 90% of the rows, so that the copy of every finished range to the host
+    // overlaps the rest of the distances.
+    static constexpr double kEnds[] = {0.2, 0.5};
+    static const char *const kUp[] = {"part 1 uploaded", "part 2 uploaded", "part 3 uploaded"};
+    static const char *const kParsed[] = {"part 1 parsed", "part 2 parsed", "part 3 parsed"};
+    static const char *const kPacked[] = {"part 1 deduplicated + packed", "part 2 deduplicated + packed",
+                                          "part 3 deduplicated + packed"};
+    struct Band {
+      uint64_t row_lo = 0, row_hi = 0;  // rows whose entries it writes
+      cudaEvent_t done = nullptr;
+      hd_alignment view;
+      hd::PairLaunchPlan plan;
+    };
+    std::vector<std::unique_ptr<Band>> bands;
+    hd::Records all;
+    DevBuf uniq, iota, d_lt;
+    std::vector<uint64_t> seq;
+    std::unique_ptr<hd_alignment> owner;
+    // waits for every stream the call uses before any of the above is freed
+    struct Sync {
+      hd_ctx *c;
+      std::vector<cudaEvent_t> ev;
+      cudaEvent_t make() {
+        cudaEvent_t e;
+        HD_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ev.push_back(e);
+        return e;
+      }
+      ~Sync() {
+        for (cudaStream_t s : {c->stream, c->side, c->side2, c->up}) cudaStreamSynchronize(s);
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+      }
+    } sync{ctx, {}};
+    auto fallback = [&] {  // the whole matrix after the whole file
+      for (cudaStream_t s : {ctx->side, ctx->side2}) HD_CUDA(cudaStreamSynchronize(s));
       read_all();
       whole();
       hd::trace_end(ctx);
-      return;
-    }
-    hd::trace_mark(ctx, "first part uploaded + parsed");
-    const uint64_t L = recA.len0, words = words_for(L);
-    uint64_t KA = recA.n;
-    std::vector<uint64_t> seqA;
-    DevBuf uniqA;
-    if (remove_duplicates) uniqA = hd::dedupe(ctx, recA, &KA, seqA);
-    // rows that can still come: a record of L sites takes at least L + 2
-    // bytes (">\n" and the sites; the last one may lack its '\n')
-    const uint64_t R_max = recA.n + (n - B) / (L + 2) + 1;
-    auto owner = std::make_unique<hd_alignment>();
-    owner->ctx = ctx;
-    owner->device = ctx->device;
-    owner->length = L;
-    owner->words = words;
-    owner->rule = HD_RULE_AND;
-    owner->groups = 1;
-    owner->planes = 4;
-    owner->plane_buf[0] = DevBuf(R_max * words * 16, ctx->stream);
-    uint4 *g0 = owner->plane_buf[0].as<uint4>();
-    hd::pack_rows_and(ctx, recA, remove_duplicates ? uniqA.as<uint64_t>() : nullptr, KA, L, words, g0);
-    DevBuf d_lt((R_max < 2 ? 1 : tri(R_max)) * dtype_bytes, ctx->stream);
-    const hd::TileConfig cfg =
-        hd::tile_config_for(ctx, KA * (n / std::max<uint64_t>(B, 1)), L, dtype_bytes);
-    const uint32_t T = (uint32_t)cfg.tile;
-    // the first part's complete tile rows run on the side stream while the
-    // rest of the file is read; 16 SMs stay free for the second part's ingest
-    cudaEvent_t ev = nullptr;
-    HD_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    struct SideSync {  // waits for the side stream before any buffer is freed
-      hd_ctx *c;
-      cudaEvent_t e;
-      ~SideSync() {
-        cudaStreamSynchronize(c->side);
-        cudaEventDestroy(e);
-      }
-    } side_sync{ctx, ev};
-    hd::PairLaunchPlan planA, planB;
-    hd_alignment viewA;
-    viewA.base = owner.get();
-    viewA.n_rows = KA;
-    viewA.length = L;
-    viewA.words = words;
-    viewA.device = ctx->device;
-    const uint32_t tA = (uint32_t)(KA / T);
-    uint64_t tiles = 0;
-    if (tA > 0) {
-      HD_CUDA(cudaEventRecord(ev, ctx->stream));
-      HD_CUDA(cudaStreamWaitEvent(ctx->side, ev, 0));
+    };
+    uint64_t L = 0, words = 0, R_max = 0, K = 0, B_prev = 0, tiles = 0;
+    uint32_t T = 0, t_done = 0;
+    hd::TileConfig cfg;
+    uint4 *g0 = nullptr;
+    // tile rows [t_lo, t_hi) of the first `rows` unique rows on stream s
+    auto launch = [&](uint32_t t_lo, uint32_t t_hi, uint64_t rows, cudaStream_t s, int sm_limit,
+                      cudaEvent_t after) {
+      auto b = std::make_unique<Band>();
+      b->view.base = owner.get();
+      b->view.n_rows = rows;
+      b->view.length = L;
+      b->view.words = words;
+      b->view.device = ctx->device;
+      b->row_lo = (uint64_t)t_lo * T;
+      b->row_hi = std::min<uint64_t>((uint64_t)t_hi * T, rows);
+      if (after) HD_CUDA(cudaStreamWaitEvent(s, after, 0));
       std::vector<hd::PairJobSpec> specs(1);
-      specs[0].aln = &viewA;
+      specs[0].aln = &b->view;
       specs[0].dtype = dtype_bytes;
       specs[0].max_dist = md;
       specs[0].d_out = d_lt.p;
       specs[0].cfg = cfg;
-      specs[0].tile_lo = 0;
-      specs[0].tile_hi = tA;
-      hd::prepare_pairwise_jobs(ctx, specs, ctx->side, &planA, std::max(1, ctx->sm_count - 16));
-      hd::launch_pairwise_plan(ctx, planA, ctx->side);
+      specs[0].tile_lo = t_lo;
+      specs[0].tile_hi = t_hi;
+      hd::prepare_pairwise_jobs(ctx, specs, s, &b->plan, sm_limit);
+      hd::launch_pairwise_plan(ctx, b->plan, s);
       tiles += ctx->last_pair_tiles;
+      b->done = sync.make();
+      HD_CUDA(cudaEventRecord(b->done, s));
+      bands.push_back(std::move(b));
+    };
+    for (int c = 0;; ++c) {
+      uint64_t B = n;
+      if (c < 2) {
+        B = header_at(std::max<uint64_t>(B_prev + 1, (uint64_t)(kEnds[c] * (double)n)));
+        if (!B) {
+          // no header in the rest (or a read error): the first part is the
+          // whole file; later, the rest is the last part
+          if (c == 0) return fallback();
+          B = n;
+        }
+      }
+      const bool last = B == n;
+      if (last) read_all();  // throws on a read or copy error
+      else if (!reader->stream_wait_bytes(ctx->stream, B)) read_all();
+      hd::trace_mark(ctx, kUp[c]);
+      // parse_fasta reads 16-byte vectors from a 16-byte aligned start: a
+      // later part is parsed from B_prev rounded down. The bytes before B_prev
+      // end the previous part's last line; parsed as a FASTA's first line
+      // they are skipped and give an empty record 0, which is dropped.
+      const uint64_t C = B_prev & ~15ull;
+      hd::Records rec = hd::parse_fasta(ctx, dev + C, B - C, 0);
+      if (!rec.gathered.p && C < B_prev) rec = hd::drop_first_record(ctx, std::move(rec));
+      // multi-line records, or a first part the whole path reports on
+      if (rec.gathered.p || (c == 0 && (rec.n == 0 || rec.len0 == 0 || !rec.all_equal)))
+        return fallback();
+      if (c == 0) all = std::move(rec);
+      else all = hd::concat_records(ctx, all, rec, C, B);
+      if (!all.all_equal) fail(HD_ERR_LENGTH, kMsgLength);
+      hd::trace_mark(ctx, kParsed[c]);
+      if (c == 0) {
+        L = all.len0;
+        words = words_for(L);
+        // rows that can still come: a record of L sites takes at least L + 2
+        // bytes (">\n" and the sites; the last one may lack its '\n')
+        R_max = all.n + (n - B) / (L + 2) + 1;
+        owner = std::make_unique<hd_alignment>();
+        owner->ctx = ctx;
+        owner->device = ctx->device;
+        owner->length = L;
+        owner->words = words;
+        owner->rule = HD_RULE_AND;
+        owner->groups = 1;
+        owner->planes = 4;
+        owner->plane_buf[0] = DevBuf(R_max * words * 16, ctx->stream);
+        g0 = owner->plane_buf[0].as<uint4>();
+        d_lt = DevBuf((R_max < 2 ? 1 : tri(R_max)) * dtype_bytes, ctx->stream);
+        if (!remove_duplicates) {
+          std::vector<uint64_t> h(R_max);
+          for (uint64_t i = 0; i < R_max; ++i) h[i] = i;
+          iota = DevBuf(R_max * 8, ctx->stream);
+          HD_CUDA(cudaMemcpyAsync(iota.p, h.data(), R_max * 8, cudaMemcpyHostToDevice, ctx->stream));
+          HD_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+      }
+      uint64_t Kc = all.n;
+      if (remove_duplicates) uniq = hd::dedupe(ctx, all, &Kc, seq);
+      if (Kc > R_max || Kc < K) fail(HD_ERR_CUDA, "streamed ingest: inconsistent row counts");
+      if (c == 0) {
+        cfg = hd::tile_config_for(ctx, Kc * (n / std::max<uint64_t>(B, 1)), L, dtype_bytes);
+        T = (uint32_t)cfg.tile;
+      }
+      const uint64_t *rows = remove_duplicates ? uniq.as<uint64_t>() : iota.as<uint64_t>();
+      hd::pack_rows_and(ctx, all, rows + K, Kc - K, L, words, g0 + K * words);
+      hd::trace_mark(ctx, kPacked[c]);
+      K = Kc;
+      if (!last) {
+        const uint32_t t_end = (uint32_t)(K / T);
+        if (t_end > t_done) {
+          cudaEvent_t packed = sync.make();
+          HD_CUDA(cudaEventRecord(packed, ctx->stream));
+          launch(t_done, t_end, K, ctx->side, std::max(1, ctx->sm_count - 16), packed);
+          t_done = t_end;
+        }
+        B_prev = B;
+        continue;
+      }
+      const uint32_t t_end = K >= 2 ? (uint32_t)hd::ceil_div(K, T) : t_done;
+      if (t_end > t_done) {
+        const uint32_t t_split =
+            std::max(t_done + 1, (uint32_t)std::ceil(0.9 * (double)t_end));
+        cudaEvent_t packed = sync.make();
+        HD_CUDA(cudaEventRecord(packed, ctx->stream));
+        if (t_split < t_end) {
+          launch(t_done, t_split, K, ctx->side2, 0, packed);
+          launch(t_split, t_end, K, ctx->stream, 0, nullptr);
+        } else {
+          launch(t_done, t_end, K, ctx->side2, 0, packed);
+        }
+      }
+      break;
     }
-    hd::trace_mark(ctx, "first part ingested");
-    read_all();
-    // parse_fasta reads 16-byte vectors from a 16-byte aligned start: the
-    // second part is parsed from B rounded down. The bytes before B end the
-    // first part's last line; parsed as a FASTA's first line they are skipped
-    // and give an empty record 0, which is dropped.
-    const uint64_t B0 = B & ~15ull;
-    hd::Records recB = hd::parse_fasta(ctx, dev + B0, n - B0, 0);
-    if (!recB.gathered.p && B0 < B) recB = hd::drop_first_record(ctx, std::move(recB));
-    if (recB.gathered.p) {
-      // a multi-line record in the second part: the matrix after the whole file
-      cudaStreamSynchronize(ctx->side);
-      recB = hd::Records();
-      whole();
-      hd::trace_end(ctx);
-      return;
-    }
-    hd::Records all = hd::concat_records(ctx, recA, recB, B0, n);
-    if (!all.all_equal) fail(HD_ERR_LENGTH, kMsgLength);
-    uint64_t K = all.n;
-    DevBuf uniq;
-    std::vector<uint64_t> seq;
-    if (remove_duplicates) {
-      uniq = hd::dedupe(ctx, all, &K, seq);
-    } else {
-      std::vector<uint64_t> iota(all.n);
-      for (uint64_t i = 0; i < all.n; ++i) iota[i] = i;
-      uniq = DevBuf(all.n * 8, ctx->stream);
-      HD_CUDA(cudaMemcpyAsync(uniq.p, iota.data(), all.n * 8, cudaMemcpyHostToDevice, ctx->stream));
-      HD_CUDA(cudaStreamSynchronize(ctx->stream));
-    }
-    if (K > R_max || K < KA) fail(HD_ERR_CUDA, "streamed ingest: inconsistent row counts");
-    hd::pack_rows_and(ctx, all, uniq.as<uint64_t>() + KA, K - KA, L, words, g0 + KA * words);
-    hd::trace_mark(ctx, "second part ingested");
     owner->n_rows = K;
     owner->n_input = all.n;
     owner->seqidx = std::move(seq);
@@ -1014,32 +1071,26 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       HD_CUDA(cudaMemcpyAsync(owner->d_seqidx.p, owner->seqidx.data(), owner->seqidx.size() * 8,
                               cudaMemcpyHostToDevice, ctx->stream));
     }
-    const uint32_t tAll = (uint32_t)hd::ceil_div(K, T);
-    if (K >= 2 && tAll > tA) {
-      HD_CUDA(cudaEventRecord(ev, ctx->stream));
-      HD_CUDA(cudaStreamWaitEvent(ctx->side, ev, 0));
-      std::vector<hd::PairJobSpec> specs(1);
-      specs[0].aln = owner.get();
-      specs[0].dtype = dtype_bytes;
-      specs[0].max_dist = md;
-      specs[0].d_out = d_lt.p;
-      specs[0].cfg = cfg;
-      specs[0].tile_lo = tA;
-      specs[0].tile_hi = tAll;
-      hd::prepare_pairwise_jobs(ctx, specs, ctx->side, &planB);
-      hd::launch_pairwise_plan(ctx, planB, ctx->side);
-    }
+    ctx->last_pair_tiles = tiles;
+    // each finished range of rows is copied to the host on the upload stream
+    // once its launch is done, while the later ones compute
     const uint64_t entries = K < 2 ? 0 : tri(K);
     void *host = out_fn(user, 0, K, entries);
     if (!host && entries) fail(HD_ERR_ARG, "output callback returned no buffer");
     if (entries) {
       prefault_host(host, entries * dtype_bytes);  // while the kernels run
-      HD_CUDA(cudaMemcpyAsync(host, d_lt.p, entries * dtype_bytes, cudaMemcpyDeviceToHost,
-                              ctx->side));
+      for (const auto &b : bands) {
+        const uint64_t e0 = tri(b->row_lo), e1 = tri(b->row_hi);
+        if (e1 <= e0) continue;
+        HD_CUDA(cudaStreamWaitEvent(ctx->up, b->done, 0));
+        HD_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(host) + e0 * dtype_bytes,
+                                d_lt.as<uint8_t>() + e0 * dtype_bytes, (e1 - e0) * dtype_bytes,
+                                cudaMemcpyDeviceToHost, ctx->up));
+      }
     }
-    HD_CUDA(cudaStreamSynchronize(ctx->side));
-    HD_CUDA(cudaStreamSynchronize(ctx->stream));
-    hd::trace_mark(ctx, "pairwise + copy");
+    for (cudaStream_t s : {ctx->side2, ctx->side, ctx->up, ctx->stream})
+      HD_CUDA(cudaStreamSynchronize(s));
+    hd::trace_mark(ctx, "distances + copy");
     check_status(ctx);
     // the file and its records stay for later calls on the same file
     ctx->parsed = std::make_shared<hd::Records>(std::move(all));

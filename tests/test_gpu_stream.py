@@ -1,9 +1,10 @@
 """from_fasta with the distances overlapping the read (hd_pairwise_lt_fasta_file):
-for files of 64 MB or more the first ~40% is ingested and its distances run
-while the rest is read. Every result must equal the plain order (read,
-ingest, distances) bit for bit: duplicates that cross the split, dtypes,
-max_distance, no dedupe, the multi-line fallback, errors after the split, a
-file already on the device, and the module's from_fasta."""
+for files of 64 MB or more the file is ingested in parts that end after ~20%
+and ~50% of its bytes, and each part's complete tile rows run while the rest
+is read. Every result must equal the plain order (read, ingest, distances)
+bit for bit: duplicates that cross the parts, dtypes, max_distance, no
+dedupe, multi-line records (everywhere, or one in a later part), errors in a
+later part, a file already on the device, and the module's from_fasta."""
 import numpy as np
 import pytest
 
@@ -139,3 +140,42 @@ def test_module_from_fasta_uses_it(big):
         c.close()
     np.testing.assert_array_equal(np.asarray(ds.lt_array), want)
     np.testing.assert_array_equal(np.asarray(big_ds.lt_array), want16)
+
+
+@pytest.mark.parametrize("where", [0.35, 0.8])
+def test_multiline_record_in_a_later_part(ctx, tmp_path, where):
+    # the file is ingested in parts that end after 20% and 50% of its bytes:
+    # one multi-line record in the second or third part, found after earlier
+    # parts' distances have started, still gives the plain order's results
+    rows, _, _ = synth.alignment(2500, 29903, p=1e-3, seed=43, dup_frac=0.2)
+    k0 = int(where * len(rows))
+    out = bytearray()
+    for k, r in enumerate(rows):
+        out += b">s%d\n" % k
+        if k == k0:
+            out += r[:1000].tobytes() + b"\n" + r[1000:].tobytes() + b"\n"
+        else:
+            out += r.tobytes() + b"\n"
+    p = tmp_path / "late_multi.fasta"
+    p.write_bytes(bytes(out))
+    lt, aln = ctx.pairwise_lt_fasta_file(str(p), remove_duplicates=True)
+    want, want_idx = _plain(ctx, str(p), np.uint8, 255, True)
+    np.testing.assert_array_equal(lt, want)
+    np.testing.assert_array_equal(aln.sequence_indices(), want_idx)
+    aln.free()
+
+
+def test_error_in_the_second_part(ctx, tmp_path, big):
+    from hammingdist_gb300 import abi
+
+    path, fa, rows = big
+    cut = fa.index(b"\n>", int(0.35 * len(fa))) + 1  # a record header at ~35%
+    p = tmp_path / "bad2.fasta"
+    p.write_bytes(fa[:cut] + b">short\nACGT\n" + fa[cut:])
+    with pytest.raises(abi.HDError, match="same length"):
+        ctx.pairwise_lt_fasta_file(str(p), remove_duplicates=True)
+    _touch(path)
+    lt, aln = ctx.pairwise_lt_fasta_file(path, remove_duplicates=True)
+    want, _ = _plain(ctx, path, np.uint8, 255, True)
+    np.testing.assert_array_equal(lt, want)
+    aln.free()
