@@ -123,13 +123,14 @@ int hd_alignment_from_fasta_file(hd_ctx *ctx, const char *path, int remove_dupli
  * triangle (dtype_bytes, max_distance as in hd_pairwise_lt) is copied to the
  * buffer out_fn returns (index 0, n_rows, entries), and *aln_out receives the
  * alignment (sequence indices; free it with hd_alignment_free). For a file
- * of 64 MB or more the distances overlap the read: once the first ~40% of
- * the file (cut at a record header) is uploaded it is parsed, deduplicated
- * and packed, and the distances among its unique rows (which are the first
- * rows of the final result) run while the rest of the file is read; the
- * remaining rows follow. Multi-line records, or a file already on the
- * device, take the plain order: read, ingest, distances. Results and errors
- * are those of hd_alignment_from_fasta_file + hd_pairwise_lt. */
+ * of 64 MB or more the distances overlap the read: the file is ingested in
+ * three parts that end at record headers after ~20% and ~50% of its bytes;
+ * after each part the unique rows so far (the first rows of the final
+ * result) are packed and the tile rows that are complete run while the rest
+ * is read, and finished ranges of the result are copied while later ones
+ * compute. Multi-line records, or a file already on the device, take the
+ * plain order: read, ingest, distances. Results and errors are those of
+ * hd_alignment_from_fasta_file + hd_pairwise_lt. */
 int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicates,
                               int dtype_bytes, int64_t max_distance, hd_output_fn out_fn,
                               void *user, hd_alignment **aln_out);
