@@ -21,7 +21,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
-CU_SOURCES = ["hd_ingest.cu", "hd_pairwise.cu", "hd_format.cu", "hd_results.cu", "hd_peak.cu", "hd_tune.cu",
+CU_SOURCES = ["hd_ingest.cu", "hd_pairwise.cu", "hd_mma.cu", "hd_format.cu", "hd_results.cu", "hd_peak.cu", "hd_tune.cu",
               "hd_synth.cu", "hd_server.cu", "hd_api.cu"]
 GENCODE = "arch=compute_103a,code=sm_103a"
 LIBHD = os.path.join(PKG, "libhd.so")

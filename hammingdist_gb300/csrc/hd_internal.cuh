@@ -151,6 +151,11 @@ struct hd_alignment {
   hd::DevBuf plane_buf[2];
   std::vector<uint64_t> seqidx;  // host, n_input entries (empty = identity)
   hd::DevBuf d_seqidx;           // device copy (serving / reference queries)
+  // FP8 operand of the tensor-core engine (hd_mma.cu), rows [0, fp8_rows)
+  // expanded so far out of fp8_cap; built on first use, freed with the
+  // alignment
+  mutable hd::DevBuf fp8;
+  mutable uint64_t fp8_rows = 0, fp8_cap = 0;
   // Freed on the null stream: every API call has synchronised its own stream
   // before returning, so no queued work still reads these buffers, and the
   // creating context (and its streams) may already be gone.
@@ -161,7 +166,7 @@ struct hd_alignment {
   }
   ~hd_alignment() {
     cudaSetDevice(device);
-    for (auto *b : {&plane_buf[0], &plane_buf[1], &d_seqidx}) {
+    for (auto *b : {&plane_buf[0], &plane_buf[1], &d_seqidx, &fp8}) {
       b->s = nullptr;
       b->release();
     }
@@ -424,6 +429,20 @@ TileConfig default_tile_config(uint64_t n_rows, uint64_t length, int dtype_bytes
 bool tile_config_valid(int tile, int stages);
 // tune.cu: the autotuned table (or the default) for (n, L, dtype)
 TileConfig tile_config_for(hd_ctx *ctx, uint64_t n_rows, uint64_t length, int dtype_bytes);
+
+// mma.cu: the tensor-core engine for the dense AND rule (4 planes, one
+// group, no row offset, L <= 4,000,000; HAMMINGDIST_KERNEL=lop3 turns it off).
+bool mma_eligible(const hd_alignment *aln);
+// expands rows [fp8_rows, rows) of the alignment's planes into its FP8
+// operand on `stream`; false if the operand cannot be allocated
+bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream);
+// tile rows [tile_lo, tile_hi) (128 rows each) x all earlier columns into
+// d_out (lt index out_base at d_out[0]) on `stream`; sm_limit > 0 caps the
+// persistent grid. False when the alignment is not eligible (the caller
+// runs the bit-plane engine).
+bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
+                  void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi,
+                  cudaStream_t stream, int sm_limit);
 
 // format.cu: text of rows [i_lo, i_hi) of a lower triangle held on the
 // device (lt index lt_base at d_lt[0]). Returns bytes written to d_text

@@ -1,0 +1,441 @@
+// Tensor-core lower-triangle distances for the dense AND rule (tcgen05, FP8).
+//
+// Replaces the reference's Dist<T> kernel (src/distance_cuda.cu:9-202) for
+// the rule it implements: a site pair matches when the two 4-bit codes share
+// a bit (src/distance_cuda.cu:57-65; codes of src/hamming_impl.cc:23-44:
+// A, C, G, T one-hot, '-' all four bits, every other byte 0).
+//
+// For those codes the match indicator is a bilinear form. With e(x) the
+// code's 4 plane bits and d(x) = [x = '-'],
+//   match(a, b) = <e(a), e(b)> - 3 d(a) d(b):
+// the plane dot product is 1 for equal bases and for a base against '-', 4
+// for '-' against '-' (hence the -3), and 0 otherwise. Summed over the sites
+// of two rows, matches = D1 - 3 D2 with D1 the dot product of the rows'
+// plane vectors (4 values per site) and D2 of their dash vectors (1 per
+// site). Both are products of 0/1 matrices: exact in FP8 (E4M3, 1.0 = 0x38)
+// with FP32 accumulation while 4 L < 2^24. mismatches = L - matches.
+//
+// Operand (one copy serves as A and B): each row's bit planes are expanded
+// to 160 bytes per 32-site word, K-major: for every 128 sites, four 128-byte
+// blocks (planes 0-3) then one 128-byte dash block; sites past L are 0.
+//
+// Persistent CTAs (192 threads, one per SM) walk a list of 128 x 256 tiles
+// (128 rows I x 256 columns J of the lower triangle), in bands of 16 tile
+// rows, column-major within a band, so resident CTAs share operands in L2:
+//  * warp 0 (one thread) issues TMA loads (128-byte swizzle) of one 128-byte
+//    K block of the 128 A rows and 256 B rows per stage, 4 stages, with
+//    full/empty mbarriers; it also allocates and frees the TMEM;
+//  * warp 1 (one thread) issues tcgen05.mma.cta_group::1.kind::f8f6f4 (M=128, N=256,
+//    K=32), four per stage, into TMEM: plane blocks into D1 (columns 0-255),
+//    dash blocks into D2 (256-511); each stage's MMAs are committed to its
+//    empty barrier, a tile's last ones to the `done` barrier;
+//  * warps 2-5 read their 32 rows each of D1 and D2 (tcgen05.ld), form
+//    min(L - (D1 - 3 D2), max_dist) (safe_int_cast,
+//    include/hamming/hamming_impl.hh:37-45) and store each row's part of the
+//    lower triangle in the output dtype from registers; they then release
+//    the accumulators (`tmem_free`) for the MMAs of the next tile, whose
+//    first stages the producer has already loaded.
+// Every wait is bounded; on a timeout the CTA records it in the status word,
+// waits (bounded) for its own copies and MMAs, frees its TMEM and returns.
+#include <algorithm>
+#include <cstdlib>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "hd_internal.cuh"
+
+namespace hd {
+namespace {
+
+constexpr int kMmaThreads = 192;   // warp 0: TMA, warp 1: MMA, warps 2-5: epilogue
+constexpr int kEpiThreads = 128;
+constexpr int kMmaStages = 4;
+constexpr int kTM = 128, kTN = 256;                   // tile rows x columns
+constexpr uint32_t kABytes = kTM * 128;               // one 128-byte K block of the A rows
+constexpr uint32_t kBBytes = kTN * 128;
+constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 48 KB
+constexpr int kMmaSmem = kMmaStages * kStageBytes + 1024;
+constexpr uint32_t kTmemCols = 512;                   // D1: 0-255, D2: 256-511
+constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
+constexpr uint32_t kMmaBand = 16;                     // tile rows per L2 band
+// instruction descriptor: D F32 (bits 4-5 = 1), A and B E4M3 (0), both
+// K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(kTN >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+
+struct MmaTile {
+  uint32_t I, J;  // rows [128 I, 128 I + 128), columns [256 J, 256 J + 256)
+};
+
+// 4 bits -> 4 bytes of E4M3 1.0 (0x38) or 0
+__device__ __forceinline__ uint32_t spread4(uint32_t nib) {
+  return ((nib * 0x00204081u) & 0x01010101u) * 0x38u;
+}
+
+// Rows [row_lo, row_hi) of the AND-rule bit planes -> FP8 operand rows.
+// One thread per (row, 32-site word): 16 bytes read, 160 bytes written.
+__global__ void k_expand_fp8(const uint4 *__restrict__ planes, uint64_t words, uint64_t row_lo,
+                             uint64_t row_hi, uint64_t L, uint8_t *__restrict__ x) {
+  const uint64_t total = (row_hi - row_lo) * words;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = row_lo + t / words, w = t % words;
+    const uint4 p = planes[r * words + w];
+    const uint64_t s0 = w * 32;
+    const uint32_t valid = s0 >= L ? 0u : (L - s0 >= 32 ? 0xffffffffu : ((1u << (L - s0)) - 1u));
+    const uint32_t pl[5] = {p.x & valid, p.y & valid, p.z & valid, p.w & valid,
+                            p.x & p.y & p.z & p.w & valid};
+    uint8_t *row = x + r * (words * 160);
+    const uint64_t c = w / 4, o = (w % 4) * 32;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      const uint32_t b = pl[q];
+      uint4 *dst = reinterpret_cast<uint4 *>(row + (c * 5 + q) * 128 + o);
+      dst[0] = make_uint4(spread4(b & 15u), spread4((b >> 4) & 15u), spread4((b >> 8) & 15u),
+                          spread4((b >> 12) & 15u));
+      dst[1] = make_uint4(spread4((b >> 16) & 15u), spread4((b >> 20) & 15u),
+                          spread4((b >> 24) & 15u), spread4(b >> 28));
+    }
+  }
+}
+
+// ------------------------------------------------------- tcgen05 helpers
+// Shared-memory matrix descriptor, K-major, 128-byte swizzle: start address
+// >> 4 (bits 0-13), leading byte offset 16 B (unused for this layout, bits
+// 16-29), stride byte offset 1024 B between 8-row groups (bits 32-45),
+// descriptor version 1 (bits 46-47), layout SWIZZLE_128B = 2 (bits 61-63).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+// arrives on `bar` once every earlier tcgen05.mma of this thread has completed
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// 32 lanes x 32 consecutive 32-bit columns: thread t gets row (lane base + t)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kMmaThreads, 1)
+    k_pairwise_mma(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
+                   const MmaTile *__restrict__ tiles, uint32_t n_tiles, uint32_t n, uint32_t nkb,
+                   uint32_t sites, uint32_t max_dist, T *__restrict__ out,
+                   unsigned long long out_base, int *status) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full[kMmaStages], empty[kMmaStages], done, tmem_free, fin;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_abort;
+  uint8_t *smem =
+      reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int s = 0; s < kMmaStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    mbar_init(&tmem_free, kEpiThreads);
+    mbar_init(&fin, 1);
+    fence_mbar_init();
+    s_abort = 0;
+    prefetch_tmap(&tm_a);
+    prefetch_tmap(&tm_b);
+  }
+  if (warp == 0) {
+    tmem_alloc(&s_tmem, kTmemCols);
+    tmem_relinquish();
+  }
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+  const uint32_t tmem = s_tmem;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer: every K block of every tile of this CTA, in order
+      uint32_t g = 0;  // K blocks issued (stage g % S, phase g / S)
+      bool ok = true;
+      for (uint32_t t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
+        const MmaTile tl = tiles[t];
+        const int32_t ya = (int32_t)(tl.I * kTM), yb = (int32_t)(tl.J * kTN);
+        for (uint32_t kb = 0; kb < nkb; ++kb) {
+          const uint32_t s = g % kMmaStages;
+          if ((g >= (uint32_t)kMmaStages &&
+               !mbar_wait_bounded(&empty[s], ((g / kMmaStages) - 1) & 1u, kMmaWaitNs)) ||
+              *(volatile int *)&s_abort) {
+            ok = false;
+            break;
+          }
+          uint8_t *st = smem + s * kStageBytes;
+          mbar_expect_tx(&full[s], kStageBytes);
+          tma_load_2d(st, &tm_a, (int32_t)(kb * 128), ya, &full[s]);
+          tma_load_2d(st + kABytes, &tm_b, (int32_t)(kb * 128), yb, &full[s]);
+          ++g;
+        }
+      }
+      if (!ok) {
+        atomicExch(&s_abort, 1);
+        atomicExch(status, kStatusTmaTimeout);
+      }
+      // the copies still in flight land before the CTA may leave
+      for (uint32_t q = g > (uint32_t)kMmaStages ? g - kMmaStages : 0; q < g; ++q)
+        mbar_wait_bounded(&full[q % kMmaStages], (q / kMmaStages) & 1u, kMmaWaitNs);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      uint32_t g = 0, it = 0;
+      bool ok = true;
+      for (uint32_t t = blockIdx.x; ok && t < n_tiles; t += gridDim.x, ++it) {
+        // the epilogue has read the previous tile's accumulators
+        if (it > 0 && !mbar_wait_bounded(&tmem_free, (it - 1) & 1u, kMmaWaitNs)) {
+          ok = false;
+          break;
+        }
+        tc_after_sync();
+        for (uint32_t kb = 0; kb < nkb; ++kb) {
+          const uint32_t s = g % kMmaStages;
+          if (!mbar_wait_bounded(&full[s], (g / kMmaStages) & 1u, kMmaWaitNs) ||
+              *(volatile int *)&s_abort) {
+            ok = false;
+            break;
+          }
+          tc_after_sync();
+          const uint32_t a0 = smem_u32(smem + s * kStageBytes);
+          const uint64_t ad = sw128_desc(a0), bd = sw128_desc(a0 + kABytes);
+          const uint32_t d = tmem + (kb % 5 == 4 ? 256u : 0u);
+          const bool first = kb == 0 || kb == 4;  // first block of D1, of D2
+#pragma unroll
+          for (uint32_t k = 0; k < 4; ++k)  // 32 bytes of K per MMA: +2 in 16-byte units
+            mma_f8(d, ad + 2 * k, bd + 2 * k, (first && k == 0) ? 0u : 1u);
+          mma_commit(&empty[s]);
+          ++g;
+        }
+        if (!ok) break;
+        mma_commit(&done);
+      }
+      if (!ok) {
+        atomicExch(&s_abort, 1);
+        atomicExch(status, kStatusTmaTimeout);
+        mma_commit(&done);  // releases an epilogue waiting for this tile
+      }
+      // every MMA of this thread has completed before TMEM is freed
+      mma_commit(&fin);
+      mbar_wait_bounded(&fin, 0, 4 * kMmaWaitNs);
+    }
+  } else {
+    // epilogue warps 2-5: warp w reads TMEM lanes 32 (w % 4) .. + 31, which
+    // are tile rows 32 (w % 4) + lane
+    const uint32_t sub = warp & 3u;
+    const uint32_t r_tile = sub * 32 + lane;
+    const uint32_t t_lane = tmem + ((sub * 32) << 16);
+    uint32_t it = 0;
+    for (uint32_t t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
+      const bool got = mbar_wait_bounded(&done, it & 1u, 4 * kMmaWaitNs);
+      if (!got) {
+        atomicExch(&s_abort, 1);
+        atomicExch(status, kStatusTmaTimeout);
+      }
+      // one decision per warp: tcgen05.ld needs the whole warp
+      if (__any_sync(0xffffffffu, !got || *(volatile int *)&s_abort)) break;
+      tc_after_sync();
+      const MmaTile tl = tiles[t];
+      const uint32_t i = tl.I * kTM + r_tile;  // output row
+#pragma unroll 1
+      for (uint32_t c = 0; c < (uint32_t)kTN; c += 32) {
+        uint32_t d1[32], d2[32];
+        __syncwarp();
+        tmem_ld32(t_lane + c, d1);
+        tmem_ld32(t_lane + 256u + c, d2);
+        tmem_ld_wait();
+        const uint32_t j0 = tl.J * kTN + c;  // first column of this chunk
+        if (i < n && j0 < i) {
+          const uint32_t ncols = i - j0 < 32u ? i - j0 : 32u;
+          T *dst = out + ((unsigned long long)i * (i - 1) / 2 + j0 - out_base);
+#pragma unroll
+          for (uint32_t j = 0; j < 32; ++j) {
+            if (j < ncols) {
+              const uint32_t m1 = (uint32_t)__uint_as_float(d1[j]);
+              const uint32_t m2 = (uint32_t)__uint_as_float(d2[j]);
+              const uint32_t mism = sites - (m1 - 3u * m2);
+              dst[j] = (T)(mism < max_dist ? mism : max_dist);
+            }
+          }
+        }
+      }
+      // the accumulators may be overwritten
+      tc_before_sync();
+      mbar_arrive(&tmem_free);
+    }
+  }
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+  if (warp == 0) {
+    __syncwarp();
+    tmem_dealloc(tmem, kTmemCols);
+  }
+}
+
+template <typename T>
+void set_smem_once(void (*fn)(CUtensorMap, CUtensorMap, const MmaTile *, uint32_t, uint32_t,
+                              uint32_t, uint32_t, uint32_t, T *, unsigned long long, int *)) {
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [&] {
+    err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kMmaSmem);
+  });
+  HD_CUDA(err);
+}
+
+void make_tmap_u8(hd_ctx *ctx, CUtensorMap *tm, const void *base, uint64_t row_bytes,
+                  uint64_t rows, uint32_t box_rows) {
+  cuuint64_t dims[2] = {row_bytes, rows};
+  cuuint64_t strides[1] = {row_bytes};
+  cuuint32_t box[2] = {128, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = ctx->encode_tiled(tm, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void *>(base),
+                                 dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                 CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    fail(HD_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+}
+
+}  // namespace
+
+bool mma_eligible(const hd_alignment *aln) {
+  if (const char *e = std::getenv("HAMMINGDIST_KERNEL"))
+    if (std::string(e) == "lop3") return false;
+  // FP32 sums of up to 4 L are exact below 2^24
+  return aln->rule == HD_RULE_AND && aln->planes == 4 && aln->groups == 1 && aln->row0 == 0 &&
+         aln->length >= 1 && aln->length <= 4000000 && aln->n_rows >= 2 &&
+         aln->n_rows < (1ull << 31);
+}
+
+bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream) {
+  const hd_alignment *o = aln->base ? aln->base : aln;
+  if (o->fp8_rows >= rows) return true;
+  const uint64_t words = o->words, rb = words * 160;
+  if (!o->fp8.p) {
+    // room for every row the planes can hold (a streamed alignment grows)
+    const uint64_t cap = std::max<uint64_t>(o->plane_buf[0].bytes / (words * 16), rows);
+    try {
+      o->fp8 = DevBuf(cap * rb, stream);
+    } catch (const Error &e) {
+      if (e.code != HD_ERR_OOM) throw;
+      cudaGetLastError();
+      return false;  // the bit-plane engine needs no extra memory
+    }
+    o->fp8_cap = cap;
+  }
+  if (rows > o->fp8_cap) fail(HD_ERR_ARG, "FP8 operand smaller than the rows asked for");
+  const uint64_t total = (rows - o->fp8_rows) * words;
+  const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
+  k_expand_fp8<<<(unsigned)grid, 256, 0, stream>>>(o->plane_buf[0].as<uint4>(), words, o->fp8_rows,
+                                                   rows, o->length, o->fp8.as<uint8_t>());
+  HD_LAUNCHED(ctx);
+  o->fp8_rows = rows;
+  return true;
+}
+
+bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
+                  void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi,
+                  cudaStream_t stream, int sm_limit) {
+  if (!mma_eligible(aln)) return false;
+  const uint64_t n = aln->n_rows;
+  const uint32_t t_hi = std::min<uint32_t>(tile_hi, (uint32_t)ceil_div(n, kTM));
+  if (t_hi <= tile_lo) return true;
+  if (!ensure_fp8(ctx, aln, n, stream)) return false;
+  const hd_alignment *o = aln->base ? aln->base : aln;
+  // tiles in bands of kMmaBand tile rows, column-major within a band
+  std::vector<MmaTile> list;
+  for (uint32_t b = tile_lo; b < t_hi; b += kMmaBand) {
+    const uint32_t e = std::min(b + kMmaBand, t_hi);
+    for (uint32_t J = 0; J <= (e - 1) / 2; ++J)
+      for (uint32_t I = b; I < e; ++I)
+        if (J <= I / 2) list.push_back({I, J});
+  }
+  DevBuf d_list(list.size() * sizeof(MmaTile), stream);
+  // from pageable memory: the call has consumed `list` when it returns
+  HD_CUDA(cudaMemcpyAsync(d_list.p, list.data(), list.size() * sizeof(MmaTile),
+                          cudaMemcpyHostToDevice, stream));
+  const uint64_t rb = o->words * 160;
+  CUtensorMap tm_a, tm_b;
+  make_tmap_u8(ctx, &tm_a, o->fp8.p, rb, n, kTM);
+  make_tmap_u8(ctx, &tm_b, o->fp8.p, rb, n, kTN);
+  const int sms = sm_limit > 0 && sm_limit < ctx->sm_count ? sm_limit : ctx->sm_count;
+  const unsigned grid = (unsigned)std::min<uint64_t>(list.size(), (uint64_t)sms);
+  const uint32_t n_tiles = (uint32_t)list.size(), n32 = (uint32_t)n;
+  const uint32_t nkb = (uint32_t)(o->words * 5 / 4), sites = (uint32_t)aln->length;
+  const auto *tl = d_list.as<MmaTile>();
+  if (dtype_bytes == 1) {
+    set_smem_once(k_pairwise_mma<uint8_t>);
+    k_pairwise_mma<uint8_t><<<grid, kMmaThreads, kMmaSmem, stream>>>(
+        tm_a, tm_b, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint8_t *>(d_out),
+        out_base, ctx->d_status);
+  } else if (dtype_bytes == 2) {
+    set_smem_once(k_pairwise_mma<uint16_t>);
+    k_pairwise_mma<uint16_t><<<grid, kMmaThreads, kMmaSmem, stream>>>(
+        tm_a, tm_b, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint16_t *>(d_out),
+        out_base, ctx->d_status);
+  } else {
+    set_smem_once(k_pairwise_mma<uint32_t>);
+    k_pairwise_mma<uint32_t><<<grid, kMmaThreads, kMmaSmem, stream>>>(
+        tm_a, tm_b, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint32_t *>(d_out),
+        out_base, ctx->d_status);
+  }
+  HD_LAUNCHED(ctx);
+  ctx->last_pair_tiles += n_tiles;
+  return true;  // d_list is freed in stream order, after the kernel
+}
+
+}  // namespace hd

@@ -463,6 +463,10 @@ void run_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStream_
 void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
                     void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi) {
   if (aln->n_rows < 2 || tile_hi <= tile_lo) return;
+  // the dense AND rule runs on the tensor cores (hd_mma.cu)
+  if (pairwise_mma(ctx, aln, dtype_bytes, max_dist, d_out, out_base, tile_lo, tile_hi, ctx->stream,
+                   0))
+    return;
   std::vector<PairJobSpec> specs(1);
   PairJobSpec &s = specs[0];
   s.aln = aln;

@@ -1,0 +1,83 @@
+"""The tensor-core engine (hd_mma.cu: FP8 tcgen05 MMAs, matches = D1 - 3 D2)
+against the bit-plane engine (HAMMINGDIST_KERNEL=lop3) and the oracle, bit
+for bit: lengths at and around the 32/128-site blocks, row counts around the
+128 x 256 tiles, every dtype and saturation, '-' against '-', N and other
+bytes, the row ranges of the text writer and views."""
+import os
+
+import numpy as np
+import pytest
+
+from hammingdist_gb300 import synth
+from oracle import hd_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from hammingdist_gb300 import abi
+
+    c = abi.Context(0)
+    yield c
+    c.close()
+
+
+def _both(ctx, aln, **kw):
+    os.environ["HAMMINGDIST_KERNEL"] = "lop3"
+    try:
+        want = ctx.pairwise_lt(aln, **kw)
+    finally:
+        del os.environ["HAMMINGDIST_KERNEL"]
+    got = ctx.pairwise_lt(aln, **kw)
+    return got, want
+
+
+@pytest.mark.parametrize("n,L", [(2, 1), (3, 33), (5, 127), (17, 128), (129, 129), (255, 257),
+                                 (256, 1000), (257, 513), (300, 5000), (130, 29903)])
+def test_mma_equals_lop3_and_oracle(ctx, n, L):
+    seqs = synth.random_strings(n, L, b"ACGT-N", seed=n * 7 + L)
+    aln = ctx.alignment_from_sequences(seqs)
+    got, want = _both(ctx, aln)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got, o.lt_dense(seqs))
+    aln.free()
+
+
+@pytest.mark.parametrize("dtype,md", [(np.uint8, 255), (np.uint8, 3), (np.uint16, 65535),
+                                      (np.uint16, 200), (np.uint32, 2**32 - 1)])
+def test_mma_dtypes_and_saturation(ctx, dtype, md):
+    rows, _, _ = synth.alignment(700, 3001, p=5e-2, seed=5, dup_frac=0.0, dash_max=300)
+    seqs = [r.tobytes() for r in rows]
+    aln = ctx.alignment_from_sequences(seqs)
+    got, want = _both(ctx, aln, dtype=dtype, max_distance=md)
+    np.testing.assert_array_equal(got, want)
+    aln.free()
+
+
+def test_mma_dashes_and_other_bytes(ctx):
+    # '-' against '-' (plane dot 4, minus 3), N, X, lowercase and other
+    # bytes (code 0: never match), long dash runs
+    rng = np.random.default_rng(9)
+    alphabet = np.frombuffer(b"ACGT-NXacgt*?-----", dtype=np.uint8)
+    seqs = [alphabet[rng.integers(0, len(alphabet), 2000)].tobytes() for _ in range(300)]
+    seqs.append(b"-" * 2000)
+    seqs.append(b"N" * 2000)
+    aln = ctx.alignment_from_sequences(seqs)
+    got, want = _both(ctx, aln)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got, o.lt_dense(seqs))
+    aln.free()
+
+
+def test_mma_larger(ctx):
+    rows, _, _ = synth.alignment(3000, 29903, p=1e-3, seed=11, dup_frac=0.0)
+    seqs = [r.tobytes() for r in rows]
+    aln = ctx.alignment_from_sequences(seqs)
+    got, want = _both(ctx, aln)
+    np.testing.assert_array_equal(got, want)
+    pick = np.array([0, 1, 2, 127, 128, 255, 256, 257, 1500, 2998, 2999])
+    sub = o.lt_dense([seqs[i] for i in pick])
+    g = [got[pick[a] * (pick[a] - 1) // 2 + pick[b]] for a in range(len(pick)) for b in range(a)]
+    np.testing.assert_array_equal(np.array(g, dtype=np.uint8), sub)
+    aln.free()

@@ -151,6 +151,21 @@ def test_launches_and_device_output(ctx):
     ctx.pairwise_lt(aln, dtype=np.uint8, max_distance=255, out=out.data_ptr(), out_on_device=True)
     assert ctx.kernel_launches > before
     np.testing.assert_array_equal(out.cpu().numpy(), o.lt_dense(seqs))
+    # the tensor-core engine: 128-row x 256-column tiles, I // 2 + 1 per tile row
+    ms, tiles = ctx.last_pairwise_timing()
+    nb = -(-n // 128)
+    assert ms > 0 and tiles == sum(i // 2 + 1 for i in range(nb))
+    # the bit-plane engine: square tiles of the autotuned edge
+    import os
+
+    os.environ["HAMMINGDIST_KERNEL"] = "lop3"
+    try:
+        out.zero_()
+        ctx.pairwise_lt(aln, dtype=np.uint8, max_distance=255, out=out.data_ptr(),
+                        out_on_device=True)
+    finally:
+        del os.environ["HAMMINGDIST_KERNEL"]
+    np.testing.assert_array_equal(out.cpu().numpy(), o.lt_dense(seqs))
     ms, tiles = ctx.last_pairwise_timing()
     tile, _ = ctx.tune_lookup(n, 300, np.uint8)
     nb = -(-n // tile)
