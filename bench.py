@@ -145,9 +145,18 @@ def make_workload(tmpdir):
     return fa, root.tobytes(), path, rows
 
 
+def measured_peaks():
+    """The generated peaks of this machine's GPUs, if present."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return json.load(open(p))
+    except (OSError, ValueError):
+        return {}
+
+
 def profile_traffic():
     """DRAM bytes per pairwise launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "pairwise_n20000_L29903.md")
+    p = os.path.join(ROOT, "profiles", "pairwise_mma_n14000_L29903.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -340,13 +349,16 @@ def run_ours(args):
         e2e_mean = sum(e2e_times) / len(e2e_times)
         e2e_value = ws * pairs * L / e2e_mean / 1e9
 
-        # roofline of the dominant kernel: 4 LOP3 per 32 pair-sites
+        # roofline of the dominant kernel, the tensor-core engine: 5 multiply-adds
+        # (10 FLOP) per pair-site, matches = <planes, planes'> - 3 <dash, dash'>
         peaks = ctx.measure_int_peaks()
+        fp8_peak = ctx.measure_mma_peak()
         kern_s = statistics.mean(pair_ms) / 1e3
-        lop3_per_launch = pairs * L / 8.0
-        achieved = lop3_per_launch / kern_s / 1e12
-        peak = peaks["lop3_per_s"] / 1e12
+        flop_per_launch = 10.0 * pairs * L
+        achieved = flop_per_launch / kern_s / 1e12
+        peak = fp8_peak / 1e12
         traffic = profile_traffic()
+        bf16 = measured_peaks().get("bf16_tflops")
 
         if rank == 0:
             line = {
@@ -360,18 +372,19 @@ def run_ours(args):
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
                 "parity": "bit-exact (sampled rows + all reference distances vs oracle)"
                 if parity else "MISMATCH",
-                "roofline": {"bound": "int_lop3", "achieved": achieved, "peak": peak,
-                             "unit": "TLOP3/s", "frac": achieved / peak, "traffic": traffic,
+                "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                              "kernel_ms": kern_s * 1e3,
-                             "peak_source": "in-run LOP3 microbenchmark (hd_measure_int_peaks); "
-                                            "MEASURED_PEAKS.json has no integer-pipe figure",
-                             "popc_peak_T": peaks["popc_per_s"] / 1e12,
-                             "pair_sites_bound_T": min(8 * peaks["lop3_per_s"],
-                                                       32 * peaks["popc_per_s"]) / 1e12,
-                             "mix_ceiling_T": peaks["mix_pair_sites_per_s"] / 1e12,
-                             "frac_of_mix_ceiling": pairs * L / kern_s / peaks["mix_pair_sites_per_s"],
+                             "peak_source": "in-run FP8 tcgen05 MMA microbenchmark "
+                                            "(hd_measure_mma_peak); MEASURED_PEAKS.json has "
+                                            "bf16 only",
+                             "bf16_measured_TF": bf16,
+                             "flop_per_pair_site": 10,
                              "kernel_pair_sites_T": pairs * L / kern_s / 1e12,
-                             "hbm_write_GBs": pairs / kern_s / 1e9},
+                             "hbm_write_GBs": pairs / kern_s / 1e9,
+                             "lop3_engine_bound_T": min(8 * peaks["lop3_per_s"],
+                                                        32 * peaks["popc_per_s"]) / 1e12,
+                             "lop3_mix_ceiling_T": peaks["mix_pair_sites_per_s"] / 1e12},
                 "e2e": {"value": e2e_value, "unit": "Gpair-sites/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "ms_per_step": e2e_mean * 1e3},
                 "gpu_launches": launches,

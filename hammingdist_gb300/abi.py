@@ -82,6 +82,7 @@ SIGNATURES = {
     "hd_trace_enable": (ci, [vp, ctypes.c_int]),
     "hd_trace_last": (ctypes.c_char_p, [vp]),
     "hd_measure_int_peaks": (ci, [vp, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
+    "hd_measure_mma_peak": (ci, [vp, P(ctypes.c_double)]),
     "hd_last_pairwise_timing": (ci, [vp, P(ctypes.c_double), P(u64)]),
 }
 
@@ -473,6 +474,12 @@ class Context:
         self._check(lib().hd_measure_int_peaks(self.h, ctypes.byref(a), ctypes.byref(b),
                                                ctypes.byref(c)))
         return {"lop3_per_s": a.value, "popc_per_s": b.value, "mix_pair_sites_per_s": c.value}
+
+    def measure_mma_peak(self):
+        """Dense FP8 tensor-core FLOP/s (hd_measure_mma_peak)."""
+        f = ctypes.c_double()
+        self._check(lib().hd_measure_mma_peak(self.h, ctypes.byref(f)))
+        return f.value
 
     def last_pairwise_timing(self):
         ms, tiles = ctypes.c_double(), u64()

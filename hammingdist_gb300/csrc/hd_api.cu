@@ -943,6 +943,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     };
     uint64_t L = 0, words = 0, R_max = 0, K = 0, B_prev = 0, tiles = 0;
     uint32_t T = 0, t_done = 0;
+    bool use_mma = false;  // tensor-core engine: 128-row tiles
     hd::TileConfig cfg;
     uint4 *g0 = nullptr;
     // tile rows [t_lo, t_hi) of the first `rows` unique rows on stream s
@@ -957,16 +958,22 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       b->row_lo = (uint64_t)t_lo * T;
       b->row_hi = std::min<uint64_t>((uint64_t)t_hi * T, rows);
       if (after) HD_CUDA(cudaStreamWaitEvent(s, after, 0));
-      std::vector<hd::PairJobSpec> specs(1);
-      specs[0].aln = &b->view;
-      specs[0].dtype = dtype_bytes;
-      specs[0].max_dist = md;
-      specs[0].d_out = d_lt.p;
-      specs[0].cfg = cfg;
-      specs[0].tile_lo = t_lo;
-      specs[0].tile_hi = t_hi;
-      hd::prepare_pairwise_jobs(ctx, specs, s, &b->plan, sm_limit);
-      hd::launch_pairwise_plan(ctx, b->plan, s);
+      ctx->last_pair_tiles = 0;
+      // the tensor-core engine (its operand rows were expanded after the
+      // pack, on ctx->stream), else the bit-plane engine
+      if (!use_mma || !hd::pairwise_mma(ctx, &b->view, dtype_bytes, md, d_lt.p, 0, t_lo, t_hi, s,
+                                        sm_limit)) {
+        std::vector<hd::PairJobSpec> specs(1);
+        specs[0].aln = &b->view;
+        specs[0].dtype = dtype_bytes;
+        specs[0].max_dist = md;
+        specs[0].d_out = d_lt.p;
+        specs[0].cfg = cfg;
+        specs[0].tile_lo = t_lo;
+        specs[0].tile_hi = t_hi;
+        hd::prepare_pairwise_jobs(ctx, specs, s, &b->plan, sm_limit);
+        hd::launch_pairwise_plan(ctx, b->plan, s);
+      }
       tiles += ctx->last_pair_tiles;
       b->done = sync.make();
       HD_CUDA(cudaEventRecord(b->done, s));
@@ -1032,9 +1039,19 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       if (c == 0) {
         cfg = hd::tile_config_for(ctx, Kc * (n / std::max<uint64_t>(B, 1)), L, dtype_bytes);
         T = (uint32_t)cfg.tile;
+        owner->n_rows = R_max;  // the eligibility test looks at the shape only
+        use_mma = hd::mma_eligible(owner.get());
+        owner->n_rows = 0;
+        if (use_mma) T = hd::kTile;
       }
       const uint64_t *rows = remove_duplicates ? uniq.as<uint64_t>() : iota.as<uint64_t>();
       hd::pack_rows_and(ctx, all, rows + K, Kc - K, L, words, g0 + K * words);
+      // the new rows' FP8 operand, before the launches of any stream read it
+      if (use_mma && Kc >= 2 && !hd::ensure_fp8(ctx, owner.get(), Kc, ctx->stream)) {
+        use_mma = false;
+        T = (uint32_t)cfg.tile;
+        if (t_done) fail(HD_ERR_OOM, "no memory for the FP8 operand of a streamed call");
+      }
       hd::trace_mark(ctx, kPacked[c]);
       K = Kc;
       if (!last) {
@@ -1153,6 +1170,10 @@ int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, int64_
     }
     const uint32_t nb = (uint32_t)hd::ceil_div(n, hd::kTile);
     hd::trace_begin(ctx, "hd_pairwise_lt");
+    // the tensor-core engine's operand first, so that the timing below is the
+    // distance kernel's alone
+    if (hd::mma_eligible(aln) && hd::ensure_fp8(ctx, aln, n, ctx->stream))
+      hd::trace_mark(ctx, "FP8 operand");
     HD_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
     hd::pairwise_tiles(ctx, aln, dtype_bytes, md, d_out, 0, 0, nb);
     HD_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
@@ -1432,6 +1453,14 @@ int hd_distance(hd_ctx *ctx, const char *s0, uint64_t l0, const char *s1, uint64
     hd::reference_distances_device(ctx, rec, d.as<uint8_t>(), include_x, d_out.as<uint32_t>());
     HD_CUDA(cudaMemcpyAsync(out, d_out.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
     HD_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int hd_measure_mma_peak(hd_ctx *ctx, double *fp8_flop_per_s) {
+  if (!ctx || !fp8_flop_per_s) return HD_ERR_ARG;
+  return guard(ctx, [&] {
+    *fp8_flop_per_s = hd::measure_mma_peak(ctx);
+    check_status(ctx);
   });
 }
 

@@ -443,6 +443,8 @@ bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_
 bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
                   void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi,
                   cudaStream_t stream, int sm_limit);
+// FP8 dense MMA rate (FLOP/s) of this device from shared-memory operands
+double measure_mma_peak(hd_ctx *ctx);
 
 // format.cu: text of rows [i_lo, i_hi) of a lower triangle held on the
 // device (lt index lt_base at d_lt[0]). Returns bytes written to d_text

@@ -325,6 +325,49 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   }
 }
 
+// FP8 MMA rate from shared memory alone (no loads): one CTA per SM (the
+// shared-memory request keeps it alone) issues `rounds` x 4 MMAs of M=128,
+// N=256, K=32 on a zeroed stage (the values do not change the rate).
+__global__ void __launch_bounds__(128, 1) k_peak_mma(uint32_t rounds, int *status) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  uint8_t *smem =
+      reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  for (uint32_t k = threadIdx.x; k < kStageBytes / 16; k += blockDim.x)
+    reinterpret_cast<uint4 *>(smem)[k] = make_uint4(0, 0, 0, 0);
+  // the generic-proxy writes above, before the tensor cores read them
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  if (threadIdx.x < 32) {
+    tmem_alloc(&s_tmem, kTmemCols);
+    tmem_relinquish();
+  }
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+  const uint32_t tmem = s_tmem;
+  if (threadIdx.x == 0) {
+    const uint32_t a0 = smem_u32(smem);
+    const uint64_t ad = sw128_desc(a0), bd = sw128_desc(a0 + kABytes);
+    for (uint32_t r = 0; r < rounds; ++r)
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k) mma_f8(tmem, ad + 2 * k, bd + 2 * k, (r | k) ? 1u : 0u);
+    mma_commit(&bar);
+    if (!mbar_wait_bounded(&bar, 0, 4 * kMmaWaitNs)) atomicExch(status, kStatusTmaTimeout);
+  }
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
+  if (threadIdx.x < 32) {
+    __syncwarp();
+    tmem_dealloc(tmem, kTmemCols);
+  }
+}
+
 template <typename T>
 void set_smem_once(void (*fn)(CUtensorMap, CUtensorMap, const MmaTile *, uint32_t, uint32_t,
                               uint32_t, uint32_t, uint32_t, T *, unsigned long long, int *)) {
@@ -385,6 +428,27 @@ bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_
   HD_LAUNCHED(ctx);
   o->fp8_rows = rows;
   return true;
+}
+
+double measure_mma_peak(hd_ctx *ctx) {
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [&] {
+    err = cudaFuncSetAttribute(k_peak_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, kMmaSmem);
+  });
+  HD_CUDA(err);
+  const uint32_t rounds = 4096;
+  k_peak_mma<<<ctx->sm_count, 128, kMmaSmem, ctx->stream>>>(256, ctx->d_status);  // warm-up
+  HD_LAUNCHED(ctx);
+  HD_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
+  k_peak_mma<<<ctx->sm_count, 128, kMmaSmem, ctx->stream>>>(rounds, ctx->d_status);
+  HD_LAUNCHED(ctx);
+  HD_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
+  HD_CUDA(cudaStreamSynchronize(ctx->stream));
+  float ms = 0;
+  HD_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+  const double flop = (double)ctx->sm_count * rounds * 4 * 2.0 * kTM * kTN * 32;
+  return flop / (ms / 1e3);
 }
 
 bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
