@@ -10,30 +10,35 @@
 //   match(a, b) = <e(a), e(b)> - 3 d(a) d(b):
 // the plane dot product is 1 for equal bases and for a base against '-', 4
 // for '-' against '-' (hence the -3), and 0 otherwise. Summed over the sites
-// of two rows, matches = D1 - 3 D2 with D1 the dot product of the rows'
-// plane vectors (4 values per site) and D2 of their dash vectors (1 per
-// site). Both are products of 0/1 matrices: exact in FP8 (E4M3, 1.0 = 0x38)
-// with FP32 accumulation while 4 L < 2^24. mismatches = L - matches.
+// of two rows this is one dot product of 5 values per site, the dash value
+// being 1 on the row side and -3 on the column side. All values are 0, 1 or
+// -3: exact in FP8 (E4M3: 1.0 = 0x38, -3.0 = 0xC4) with FP32 accumulation
+// while 4 L < 2^24. mismatches = L - matches.
 //
-// Operand (one copy serves as A and B): each row's bit planes are expanded
-// to 160 bytes per 32-site word, K-major: for every 128 sites, four 128-byte
-// blocks (planes 0-3) then one 128-byte dash block; sites past L are 0.
+// Operand (one buffer serves rows and columns): each row's bit planes are
+// expanded to 192 bytes per 32-site word, K-major: for every 128 sites, six
+// 128-byte blocks, the four planes, the dash as 1 (read for rows) and the dash
+// as -3 (read for columns); sites past L are 0.
 //
-// Persistent CTAs (192 threads, one per SM) walk a list of 128 x 256 tiles
-// (128 rows I x 256 columns J of the lower triangle), in bands of 16 tile
-// rows, column-major within a band, so resident CTAs share operands in L2:
-//  * warp 0 (one thread) issues TMA loads (128-byte swizzle) of one 128-byte
-//    K block of the 128 A rows and 256 B rows per stage, 4 stages, with
-//    full/empty mbarriers; it also allocates and frees the TMEM;
-//  * warp 1 (one thread) issues tcgen05.mma.cta_group::1.kind::f8f6f4 (M=128, N=256,
-//    K=32), four per stage, into TMEM: plane blocks into D1 (columns 0-255),
-//    dash blocks into D2 (256-511); each stage's MMAs are committed to its
-//    empty barrier, a tile's last ones to the `done` barrier;
-//  * warps 2-5 read their 32 rows each of D1 and D2 (tcgen05.ld), form
-//    min(L - (D1 - 3 D2), max_dist) (safe_int_cast,
+// Persistent CTAs (192 threads, one per SM) walk a list of items: 256 columns
+// J x one or two 128-row tiles I (rows [128 I, 128 I + 128 k)), in bands of
+// 16 tile rows, column-major within a band, so resident CTAs share operands
+// in L2; the list ends with single-row-tile items so that every CTA gets the
+// same work to within a row tile.
+//  * warp 0 (one thread) issues TMA loads (128-byte swizzle) per stage of
+//    one 128-byte K block of the item's 128 or 256 rows and 256 columns,
+//    3 stages of 64 KB with full/empty mbarriers; warp 0 also allocates and
+//    frees the TMEM;
+//  * warp 1 (one thread) issues tcgen05.mma.cta_group::1.kind::f8f6f4
+//    (M=128, N=256, K=32), four per row tile per stage, into TMEM (row tile
+//    h of the item at columns 256 h), so each column stage feeds up to eight
+//    MMAs; each stage's MMAs are committed to its empty barrier, an item's
+//    last ones to the `done` barrier;
+//  * warps 2-5 read their 32 rows of each accumulator (tcgen05.ld), form
+//    min(L - matches, max_dist) (safe_int_cast,
 //    include/hamming/hamming_impl.hh:37-45) and store each row's part of the
 //    lower triangle in the output dtype from registers; they then release
-//    the accumulators (`tmem_free`) for the MMAs of the next tile, whose
+//    the accumulators (`tmem_free`) for the MMAs of the next item, whose
 //    first stages the producer has already loaded.
 // Every wait is bounded; on a timeout the CTA records it in the status word,
 // waits (bounded) for its own copies and MMAs, frees its TMEM and returns.
@@ -50,30 +55,41 @@ namespace {
 
 constexpr int kMmaThreads = 192;   // warp 0: TMA, warp 1: MMA, warps 2-5: epilogue
 constexpr int kEpiThreads = 128;
-constexpr int kMmaStages = 4;
-constexpr int kTM = 128, kTN = 256;                   // tile rows x columns
-constexpr uint32_t kABytes = kTM * 128;               // one 128-byte K block of the A rows
+constexpr int kMmaStages = 3;
+constexpr int kTM = 128, kTN = 256;                   // MMA tile: rows x columns
+constexpr uint32_t kHalfBytes = kTM * 128;            // one 128-byte K block of 128 rows
+constexpr uint32_t kABytes = 2 * kHalfBytes;          // up to two row tiles
 constexpr uint32_t kBBytes = kTN * 128;
-constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 48 KB
+constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 64 KB
 constexpr int kMmaSmem = kMmaStages * kStageBytes + 1024;
-constexpr uint32_t kTmemCols = 512;                   // D1: 0-255, D2: 256-511
+constexpr uint32_t kTmemCols = 512;                   // row tile h at columns 256 h
 constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
 constexpr uint32_t kMmaBand = 16;                     // tile rows per L2 band
+constexpr uint64_t kRowBytesPerWord = 192;            // operand bytes per 32-site word
 // instruction descriptor: D F32 (bits 4-5 = 1), A and B E4M3 (0), both
 // K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
 constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(kTN >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
 
 struct MmaTile {
-  uint32_t I, J;  // rows [128 I, 128 I + 128), columns [256 J, 256 J + 256)
+  uint32_t I;       // first 128-row tile
+  uint32_t J;       // 256-column tile
+  uint32_t halves;  // row tiles in the item: 1 or 2
 };
 
-// 4 bits -> 4 bytes of E4M3 1.0 (0x38) or 0
-__device__ __forceinline__ uint32_t spread4(uint32_t nib) {
-  return ((nib * 0x00204081u) & 0x01010101u) * 0x38u;
+// 4 bits -> 4 bytes, each `one` (an FP8 value) or 0
+__device__ __forceinline__ uint32_t spread4(uint32_t nib, uint32_t one) {
+  return ((nib * 0x00204081u) & 0x01010101u) * one;
+}
+__device__ __forceinline__ void put32(uint8_t *dst, uint32_t b, uint32_t one) {
+  uint4 *d = reinterpret_cast<uint4 *>(dst);
+  d[0] = make_uint4(spread4(b & 15u, one), spread4((b >> 4) & 15u, one),
+                    spread4((b >> 8) & 15u, one), spread4((b >> 12) & 15u, one));
+  d[1] = make_uint4(spread4((b >> 16) & 15u, one), spread4((b >> 20) & 15u, one),
+                    spread4((b >> 24) & 15u, one), spread4(b >> 28, one));
 }
 
 // Rows [row_lo, row_hi) of the AND-rule bit planes -> FP8 operand rows.
-// One thread per (row, 32-site word): 16 bytes read, 160 bytes written.
+// One thread per (row, 32-site word): 16 bytes read, 192 bytes written.
 __global__ void k_expand_fp8(const uint4 *__restrict__ planes, uint64_t words, uint64_t row_lo,
                              uint64_t row_hi, uint64_t L, uint8_t *__restrict__ x) {
   const uint64_t total = (row_hi - row_lo) * words;
@@ -83,19 +99,14 @@ __global__ void k_expand_fp8(const uint4 *__restrict__ planes, uint64_t words, u
     const uint4 p = planes[r * words + w];
     const uint64_t s0 = w * 32;
     const uint32_t valid = s0 >= L ? 0u : (L - s0 >= 32 ? 0xffffffffu : ((1u << (L - s0)) - 1u));
-    const uint32_t pl[5] = {p.x & valid, p.y & valid, p.z & valid, p.w & valid,
-                            p.x & p.y & p.z & p.w & valid};
-    uint8_t *row = x + r * (words * 160);
-    const uint64_t c = w / 4, o = (w % 4) * 32;
-#pragma unroll
-    for (int q = 0; q < 5; ++q) {
-      const uint32_t b = pl[q];
-      uint4 *dst = reinterpret_cast<uint4 *>(row + (c * 5 + q) * 128 + o);
-      dst[0] = make_uint4(spread4(b & 15u), spread4((b >> 4) & 15u), spread4((b >> 8) & 15u),
-                          spread4((b >> 12) & 15u));
-      dst[1] = make_uint4(spread4((b >> 16) & 15u), spread4((b >> 20) & 15u),
-                          spread4((b >> 24) & 15u), spread4(b >> 28));
-    }
+    const uint32_t dash = p.x & p.y & p.z & p.w & valid;
+    uint8_t *blk = x + r * (words * kRowBytesPerWord) + (w / 4) * 768 + (w % 4) * 32;
+    put32(blk, p.x & valid, 0x38u);
+    put32(blk + 128, p.y & valid, 0x38u);
+    put32(blk + 256, p.z & valid, 0x38u);
+    put32(blk + 384, p.w & valid, 0x38u);
+    put32(blk + 512, dash, 0x38u);  // 1.0: the row side
+    put32(blk + 640, dash, 0xC4u);  // -3.0: the column side
   }
 }
 
@@ -165,7 +176,7 @@ __device__ __forceinline__ void tmem_ld_wait() {
 
 template <typename T>
 __global__ void __launch_bounds__(kMmaThreads, 1)
-    k_pairwise_mma(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
+    k_pairwise_mma(const __grid_constant__ CUtensorMap tm256, const __grid_constant__ CUtensorMap tm128,
                    const MmaTile *__restrict__ tiles, uint32_t n_tiles, uint32_t n, uint32_t nkb,
                    uint32_t sites, uint32_t max_dist, T *__restrict__ out,
                    unsigned long long out_base, int *status) {
@@ -186,8 +197,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     mbar_init(&fin, 1);
     fence_mbar_init();
     s_abort = 0;
-    prefetch_tmap(&tm_a);
-    prefetch_tmap(&tm_b);
+    prefetch_tmap(&tm256);
+    prefetch_tmap(&tm128);
   }
   if (warp == 0) {
     tmem_alloc(&s_tmem, kTmemCols);
@@ -200,12 +211,13 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      // producer: every K block of every tile of this CTA, in order
+      // producer: every K block of every item of this CTA, in order
       uint32_t g = 0;  // K blocks issued (stage g % S, phase g / S)
       bool ok = true;
       for (uint32_t t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
         const MmaTile tl = tiles[t];
         const int32_t ya = (int32_t)(tl.I * kTM), yb = (int32_t)(tl.J * kTN);
+        const uint32_t bytes = kBBytes + tl.halves * kHalfBytes;
         for (uint32_t kb = 0; kb < nkb; ++kb) {
           const uint32_t s = g % kMmaStages;
           if ((g >= (uint32_t)kMmaStages &&
@@ -214,10 +226,15 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
             ok = false;
             break;
           }
+          // K block kb: 128 sites of chunk kb / 5, block kb % 5 (planes 0-3,
+          // then the dash: +1 for the rows, the -3 block for the columns)
+          const uint32_t c = kb / 5, q = kb % 5;
+          const int32_t xa = (int32_t)((6 * c + q) * 128);
+          const int32_t xb = (int32_t)((6 * c + (q == 4 ? 5 : q)) * 128);
           uint8_t *st = smem + s * kStageBytes;
-          mbar_expect_tx(&full[s], kStageBytes);
-          tma_load_2d(st, &tm_a, (int32_t)(kb * 128), ya, &full[s]);
-          tma_load_2d(st + kABytes, &tm_b, (int32_t)(kb * 128), yb, &full[s]);
+          mbar_expect_tx(&full[s], bytes);
+          tma_load_2d(st, tl.halves == 2 ? &tm256 : &tm128, xa, ya, &full[s]);
+          tma_load_2d(st + kABytes, &tm256, xb, yb, &full[s]);
           ++g;
         }
       }
@@ -235,7 +252,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       uint32_t g = 0, it = 0;
       bool ok = true;
       for (uint32_t t = blockIdx.x; ok && t < n_tiles; t += gridDim.x, ++it) {
-        // the epilogue has read the previous tile's accumulators
+        const uint32_t halves = tiles[t].halves;
+        // the epilogue has read the previous item's accumulators
         if (it > 0 && !mbar_wait_bounded(&tmem_free, (it - 1) & 1u, kMmaWaitNs)) {
           ok = false;
           break;
@@ -250,12 +268,13 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
           }
           tc_after_sync();
           const uint32_t a0 = smem_u32(smem + s * kStageBytes);
-          const uint64_t ad = sw128_desc(a0), bd = sw128_desc(a0 + kABytes);
-          const uint32_t d = tmem + (kb % 5 == 4 ? 256u : 0u);
-          const bool first = kb == 0 || kb == 4;  // first block of D1, of D2
+          const uint64_t bd = sw128_desc(a0 + kABytes);
+          for (uint32_t h = 0; h < halves; ++h) {
+            const uint64_t ad = sw128_desc(a0 + h * kHalfBytes);
 #pragma unroll
-          for (uint32_t k = 0; k < 4; ++k)  // 32 bytes of K per MMA: +2 in 16-byte units
-            mma_f8(d, ad + 2 * k, bd + 2 * k, (first && k == 0) ? 0u : 1u);
+            for (uint32_t k = 0; k < 4; ++k)  // 32 bytes of K per MMA: +2 in 16-byte units
+              mma_f8(tmem + 256u * h, ad + 2 * k, bd + 2 * k, (kb | k) ? 1u : 0u);
+          }
           mma_commit(&empty[s]);
           ++g;
         }
@@ -265,7 +284,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       if (!ok) {
         atomicExch(&s_abort, 1);
         atomicExch(status, kStatusTmaTimeout);
-        mma_commit(&done);  // releases an epilogue waiting for this tile
+        mma_commit(&done);  // releases an epilogue waiting for this item
       }
       // every MMA of this thread has completed before TMEM is freed
       mma_commit(&fin);
@@ -273,9 +292,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     }
   } else {
     // epilogue warps 2-5: warp w reads TMEM lanes 32 (w % 4) .. + 31, which
-    // are tile rows 32 (w % 4) + lane
+    // are rows 32 (w % 4) + lane of each row tile of the item
     const uint32_t sub = warp & 3u;
-    const uint32_t r_tile = sub * 32 + lane;
     const uint32_t t_lane = tmem + ((sub * 32) << 16);
     uint32_t it = 0;
     for (uint32_t t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
@@ -288,25 +306,24 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       if (__any_sync(0xffffffffu, !got || *(volatile int *)&s_abort)) break;
       tc_after_sync();
       const MmaTile tl = tiles[t];
-      const uint32_t i = tl.I * kTM + r_tile;  // output row
+      for (uint32_t h = 0; h < tl.halves; ++h) {
+        const uint32_t i = (tl.I + h) * kTM + sub * 32 + lane;  // output row
 #pragma unroll 1
-      for (uint32_t c = 0; c < (uint32_t)kTN; c += 32) {
-        uint32_t d1[32], d2[32];
-        __syncwarp();
-        tmem_ld32(t_lane + c, d1);
-        tmem_ld32(t_lane + 256u + c, d2);
-        tmem_ld_wait();
-        const uint32_t j0 = tl.J * kTN + c;  // first column of this chunk
-        if (i < n && j0 < i) {
-          const uint32_t ncols = i - j0 < 32u ? i - j0 : 32u;
-          T *dst = out + ((unsigned long long)i * (i - 1) / 2 + j0 - out_base);
+        for (uint32_t c = 0; c < (uint32_t)kTN; c += 32) {
+          uint32_t d[32];
+          __syncwarp();
+          tmem_ld32(t_lane + 256u * h + c, d);
+          tmem_ld_wait();
+          const uint32_t j0 = tl.J * kTN + c;  // first column of this chunk
+          if (i < n && j0 < i) {
+            const uint32_t ncols = i - j0 < 32u ? i - j0 : 32u;
+            T *dst = out + ((unsigned long long)i * (i - 1) / 2 + j0 - out_base);
 #pragma unroll
-          for (uint32_t j = 0; j < 32; ++j) {
-            if (j < ncols) {
-              const uint32_t m1 = (uint32_t)__uint_as_float(d1[j]);
-              const uint32_t m2 = (uint32_t)__uint_as_float(d2[j]);
-              const uint32_t mism = sites - (m1 - 3u * m2);
-              dst[j] = (T)(mism < max_dist ? mism : max_dist);
+            for (uint32_t j = 0; j < 32; ++j) {
+              if (j < ncols) {
+                const uint32_t mism = sites - (uint32_t)__uint_as_float(d[j]);
+                dst[j] = (T)(mism < max_dist ? mism : max_dist);
+              }
             }
           }
         }
@@ -407,7 +424,7 @@ bool mma_eligible(const hd_alignment *aln) {
 bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream) {
   const hd_alignment *o = aln->base ? aln->base : aln;
   if (o->fp8_rows >= rows) return true;
-  const uint64_t words = o->words, rb = words * 160;
+  const uint64_t words = o->words, rb = words * kRowBytesPerWord;
   if (!o->fp8.p) {
     // room for every row the planes can hold (a streamed alignment grows)
     const uint64_t cap = std::max<uint64_t>(o->plane_buf[0].bytes / (words * 16), rows);
@@ -460,41 +477,64 @@ bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_
   if (t_hi <= tile_lo) return true;
   if (!ensure_fp8(ctx, aln, n, stream)) return false;
   const hd_alignment *o = aln->base ? aln->base : aln;
-  // tiles in bands of kMmaBand tile rows, column-major within a band
+  // Items: pairs of 128-row tiles (a single one where the range is odd) x
+  // 256-column tiles J up to the last column any of their rows needs, in
+  // bands of kMmaBand tile rows, column-major within a band.
   std::vector<MmaTile> list;
   for (uint32_t b = tile_lo; b < t_hi; b += kMmaBand) {
     const uint32_t e = std::min(b + kMmaBand, t_hi);
-    for (uint32_t J = 0; J <= (e - 1) / 2; ++J)
-      for (uint32_t I = b; I < e; ++I)
-        if (J <= I / 2) list.push_back({I, J});
+    const uint32_t j_end = (uint32_t)ceil_div((uint64_t)e * kTM - 1, kTN);  // columns < last row
+    for (uint32_t J = 0; J < j_end; ++J)
+      for (uint32_t I = b; I < e; I += 2) {
+        const uint32_t h = std::min(2u, e - I);
+        // rows [128 I, 128 (I + h)) need columns < 128 (I + h) - 1
+        if ((uint64_t)J * kTN < (uint64_t)(I + h) * kTM - 1) list.push_back({I, J, h});
+      }
   }
+  // Persistent CTAs take items round-robin: split the last pairs into single
+  // row tiles until the item count is a multiple of the grid, so that every
+  // CTA ends within one row tile of the others (a short list splits them all
+  // to fill more SMs).
+  const int sms = sm_limit > 0 && sm_limit < ctx->sm_count ? sm_limit : ctx->sm_count;
+  uint64_t pairs = 0;
+  for (const MmaTile &m : list) pairs += m.halves == 2;
+  const uint64_t grid_n = std::min<uint64_t>(list.size() + pairs, (uint64_t)sms);
+  uint64_t split = list.size() < grid_n ? grid_n - list.size()
+                                        : (grid_n - list.size() % grid_n) % grid_n;
+  std::vector<MmaTile> tail;
+  for (size_t k = list.size(); k-- > 0 && split > 0;) {
+    if (list[k].halves != 2) continue;
+    tail.push_back({list[k].I + 1, list[k].J, 1});
+    list[k].halves = 1;
+    --split;
+  }
+  list.insert(list.end(), tail.rbegin(), tail.rend());
   DevBuf d_list(list.size() * sizeof(MmaTile), stream);
   // from pageable memory: the call has consumed `list` when it returns
   HD_CUDA(cudaMemcpyAsync(d_list.p, list.data(), list.size() * sizeof(MmaTile),
                           cudaMemcpyHostToDevice, stream));
-  const uint64_t rb = o->words * 160;
-  CUtensorMap tm_a, tm_b;
-  make_tmap_u8(ctx, &tm_a, o->fp8.p, rb, n, kTM);
-  make_tmap_u8(ctx, &tm_b, o->fp8.p, rb, n, kTN);
-  const int sms = sm_limit > 0 && sm_limit < ctx->sm_count ? sm_limit : ctx->sm_count;
-  const unsigned grid = (unsigned)std::min<uint64_t>(list.size(), (uint64_t)sms);
+  const uint64_t rb = o->words * kRowBytesPerWord;
+  CUtensorMap tm256, tm128;
+  make_tmap_u8(ctx, &tm256, o->fp8.p, rb, n, kTN);
+  make_tmap_u8(ctx, &tm128, o->fp8.p, rb, n, kTM);
+  const unsigned grid = (unsigned)grid_n;
   const uint32_t n_tiles = (uint32_t)list.size(), n32 = (uint32_t)n;
   const uint32_t nkb = (uint32_t)(o->words * 5 / 4), sites = (uint32_t)aln->length;
   const auto *tl = d_list.as<MmaTile>();
   if (dtype_bytes == 1) {
     set_smem_once(k_pairwise_mma<uint8_t>);
     k_pairwise_mma<uint8_t><<<grid, kMmaThreads, kMmaSmem, stream>>>(
-        tm_a, tm_b, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint8_t *>(d_out),
+        tm256, tm128, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint8_t *>(d_out),
         out_base, ctx->d_status);
   } else if (dtype_bytes == 2) {
     set_smem_once(k_pairwise_mma<uint16_t>);
     k_pairwise_mma<uint16_t><<<grid, kMmaThreads, kMmaSmem, stream>>>(
-        tm_a, tm_b, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint16_t *>(d_out),
+        tm256, tm128, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint16_t *>(d_out),
         out_base, ctx->d_status);
   } else {
     set_smem_once(k_pairwise_mma<uint32_t>);
     k_pairwise_mma<uint32_t><<<grid, kMmaThreads, kMmaSmem, stream>>>(
-        tm_a, tm_b, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint32_t *>(d_out),
+        tm256, tm128, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint32_t *>(d_out),
         out_base, ctx->d_status);
   }
   HD_LAUNCHED(ctx);
