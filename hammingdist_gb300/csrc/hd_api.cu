@@ -896,7 +896,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       }
     };
     // The file is ingested in parts that end at the first record headers
-    // after 20% and 50% of its bytes. After each part the whole prefix is
+    // after the given fractions of its bytes. After each part the whole prefix is
     // deduplicated (first occurrences keep their order, so earlier unique
     // rows keep their positions) and the new unique rows are packed; the tile
     // rows that are complete then run on the side stream, with 16 SMs left
@@ -904,11 +904,28 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     // launches on two streams (the second fills the first's tail), split at
     // 90% of the rows, so that the copy of every finished range to the host
     // overlaps the rest of the distances.
-    static constexpr double kEnds[] = {0.2, 0.5};
-    static const char *const kUp[] = {"part 1 uploaded", "part 2 uploaded", "part 3 uploaded"};
-    static const char *const kParsed[] = {"part 1 parsed", "part 2 parsed", "part 3 parsed"};
+    // part ends as fractions of the file (HAMMINGDIST_STREAM_SPLITS="f1,f2,...",
+    // increasing, at most 3). At n=20,000 x L=29,903 splits at 20% and 50%
+    // and a single split at 50% are within noise of each other (the former
+    // steadier: 17.9-18.0 against 18.0-18.8 ms per bench step); no split takes
+    // 16.1 ms for the call against 14.2-14.5.
+    std::vector<double> ends = {0.2, 0.5};
+    if (const char *e = std::getenv("HAMMINGDIST_STREAM_SPLITS")) {
+      ends.clear();
+      for (const char *q = e; *q && ends.size() < 3;) {
+        char *endp = nullptr;
+        const double f = std::strtod(q, &endp);
+        if (endp == q) break;
+        if (f > 0 && f < 1 && (ends.empty() || f > ends.back())) ends.push_back(f);
+        q = *endp == ',' ? endp + 1 : endp;
+      }
+    }
+    static const char *const kUp[] = {"part 1 uploaded", "part 2 uploaded", "part 3 uploaded",
+                                      "part 4 uploaded"};
+    static const char *const kParsed[] = {"part 1 parsed", "part 2 parsed", "part 3 parsed",
+                                          "part 4 parsed"};
     static const char *const kPacked[] = {"part 1 deduplicated + packed", "part 2 deduplicated + packed",
-                                          "part 3 deduplicated + packed"};
+                                          "part 3 deduplicated + packed", "part 4 deduplicated + packed"};
     struct Band {
       uint64_t row_lo = 0, row_hi = 0;  // rows whose entries it writes
       cudaEvent_t done = nullptr;
@@ -981,8 +998,8 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     };
     for (int c = 0;; ++c) {
       uint64_t B = n;
-      if (c < 2) {
-        B = header_at(std::max<uint64_t>(B_prev + 1, (uint64_t)(kEnds[c] * (double)n)));
+      if (c < (int)ends.size()) {
+        B = header_at(std::max<uint64_t>(B_prev + 1, (uint64_t)(ends[c] * (double)n)));
         if (!B) {
           // no header in the rest (or a read error): the first part is the
           // whole file; later, the rest is the last part

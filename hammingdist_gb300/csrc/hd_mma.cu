@@ -64,7 +64,7 @@ constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 64 KB
 constexpr int kMmaSmem = kMmaStages * kStageBytes + 1024;
 constexpr uint32_t kTmemCols = 512;                   // row tile h at columns 256 h
 constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
-constexpr uint32_t kMmaBand = 16;                     // tile rows per L2 band
+constexpr uint32_t kMmaBand = 16;  // tile rows per L2 band (HAMMINGDIST_MMA_BAND overrides)
 constexpr uint64_t kRowBytesPerWord = 192;            // operand bytes per 32-site word
 // instruction descriptor: D F32 (bits 4-5 = 1), A and B E4M3 (0), both
 // K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
@@ -480,9 +480,11 @@ bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_
   // Items: pairs of 128-row tiles (a single one where the range is odd) x
   // 256-column tiles J up to the last column any of their rows needs, in
   // bands of kMmaBand tile rows, column-major within a band.
+  uint32_t band = kMmaBand;
+  if (const char *e = std::getenv("HAMMINGDIST_MMA_BAND")) band = (uint32_t)std::max(2, std::atoi(e)) & ~1u;
   std::vector<MmaTile> list;
-  for (uint32_t b = tile_lo; b < t_hi; b += kMmaBand) {
-    const uint32_t e = std::min(b + kMmaBand, t_hi);
+  for (uint32_t b = tile_lo; b < t_hi; b += band) {
+    const uint32_t e = std::min(b + band, t_hi);
     const uint32_t j_end = (uint32_t)ceil_div((uint64_t)e * kTM - 1, kTN);  // columns < last row
     for (uint32_t J = 0; J < j_end; ++J)
       for (uint32_t I = b; I < e; I += 2) {

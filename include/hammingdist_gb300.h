@@ -124,11 +124,11 @@ int hd_alignment_from_fasta_file(hd_ctx *ctx, const char *path, int remove_dupli
  * buffer out_fn returns (index 0, n_rows, entries), and *aln_out receives the
  * alignment (sequence indices; free it with hd_alignment_free). For a file
  * of 64 MB or more the distances overlap the read: the file is ingested in
- * three parts that end at record headers after ~20% and ~50% of its bytes;
- * after each part the unique rows so far (the first rows of the final
- * result) are packed and the tile rows that are complete run while the rest
- * is read, and finished ranges of the result are copied while later ones
- * compute. Multi-line records, or a file already on the device, take the
+ * parts that end at record headers (by default after ~20% and ~50% of its
+ * bytes; HAMMINGDIST_STREAM_SPLITS sets up to three splits); after each part the
+ * unique rows so far (the first rows of the final result) are packed and the
+ * tile rows that are complete run while the rest is read, and finished
+ * ranges of the result are copied while later ones compute. Multi-line records, or a file already on the device, take the
  * plain order: read, ingest, distances. Results and errors are those of
  * hd_alignment_from_fasta_file + hd_pairwise_lt. */
 int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicates,

@@ -1,10 +1,11 @@
 """from_fasta with the distances overlapping the read (hd_pairwise_lt_fasta_file):
-for files of 64 MB or more the file is ingested in parts that end after ~20%
-and ~50% of its bytes, and each part's complete tile rows run while the rest
-is read. Every result must equal the plain order (read, ingest, distances)
-bit for bit: duplicates that cross the parts, dtypes, max_distance, no
-dedupe, multi-line records (everywhere, or one in a later part), errors in a
-later part, a file already on the device, and the module's from_fasta."""
+for files of 64 MB or more the file is ingested in parts (by default split
+after ~20% and ~50% of its bytes; HAMMINGDIST_STREAM_SPLITS sets up to three),
+and each part's complete tile rows run while the rest is read. Every result
+must equal the plain order (read, ingest, distances) bit for bit: duplicates
+that cross the parts, dtypes, max_distance, no dedupe, every split setting,
+multi-line records (everywhere, or one in a later part), errors in a later
+part, a file already on the device, and the module's from_fasta."""
 import numpy as np
 import pytest
 
@@ -165,11 +166,13 @@ def test_multiline_record_in_a_later_part(ctx, tmp_path, where):
     aln.free()
 
 
-def test_error_in_the_second_part(ctx, tmp_path, big):
+@pytest.mark.parametrize("where", [0.35, 0.7])
+def test_error_in_a_part(ctx, tmp_path, big, where):
+    # a short record in the second or the third part (default splits at 20%, 50%)
     from hammingdist_gb300 import abi
 
     path, fa, rows = big
-    cut = fa.index(b"\n>", int(0.35 * len(fa))) + 1  # a record header at ~35%
+    cut = fa.index(b"\n>", int(where * len(fa))) + 1  # a record header
     p = tmp_path / "bad2.fasta"
     p.write_bytes(fa[:cut] + b">short\nACGT\n" + fa[cut:])
     with pytest.raises(abi.HDError, match="same length"):
@@ -178,4 +181,40 @@ def test_error_in_the_second_part(ctx, tmp_path, big):
     lt, aln = ctx.pairwise_lt_fasta_file(path, remove_duplicates=True)
     want, _ = _plain(ctx, path, np.uint8, 255, True)
     np.testing.assert_array_equal(lt, want)
+    aln.free()
+
+
+@pytest.mark.parametrize("splits", ["", "0.5", "0.2,0.5", "0.25,0.5,0.75", "0.9"])
+def test_every_split_setting(ctx, big, monkeypatch, splits):
+    # no split (one part), one, two (the default) and three splits: the same
+    # matrix and sequence indices as the plain order
+    path, fa, rows = big
+    monkeypatch.setenv("HAMMINGDIST_STREAM_SPLITS", splits)
+    _touch(path)
+    lt, aln = ctx.pairwise_lt_fasta_file(path, remove_duplicates=True)
+    want, want_idx = _plain(ctx, path, np.uint8, 255, True)
+    np.testing.assert_array_equal(lt, want)
+    np.testing.assert_array_equal(aln.sequence_indices(), want_idx)
+    aln.free()
+
+
+@pytest.mark.parametrize("where", [0.3, 0.6])
+def test_multiline_record_with_three_splits(ctx, tmp_path, monkeypatch, where):
+    # one multi-line record in the second or third of four parts
+    monkeypatch.setenv("HAMMINGDIST_STREAM_SPLITS", "0.25,0.5,0.75")
+    rows, _, _ = synth.alignment(2500, 29903, p=1e-3, seed=44, dup_frac=0.2)
+    k0 = int(where * len(rows))
+    out = bytearray()
+    for k, r in enumerate(rows):
+        out += b">s%d\n" % k
+        if k == k0:
+            out += r[:1000].tobytes() + b"\n" + r[1000:].tobytes() + b"\n"
+        else:
+            out += r.tobytes() + b"\n"
+    p = tmp_path / "late_multi3.fasta"
+    p.write_bytes(bytes(out))
+    lt, aln = ctx.pairwise_lt_fasta_file(str(p), remove_duplicates=True)
+    want, want_idx = _plain(ctx, str(p), np.uint8, 255, True)
+    np.testing.assert_array_equal(lt, want)
+    np.testing.assert_array_equal(aln.sequence_indices(), want_idx)
     aln.free()
