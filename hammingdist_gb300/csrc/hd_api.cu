@@ -1064,7 +1064,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       const uint64_t *rows = remove_duplicates ? uniq.as<uint64_t>() : iota.as<uint64_t>();
       hd::pack_rows_and(ctx, all, rows + K, Kc - K, L, words, g0 + K * words);
       // the new rows' FP8 operand, before the launches of any stream read it
-      if (use_mma && Kc >= 2 && !hd::ensure_fp8(ctx, owner.get(), Kc, ctx->stream)) {
+      if (use_mma && Kc >= 2 && !hd::ensure_fp8(ctx, owner.get(), Kc, ctx->stream, R_max)) {
         use_mma = false;
         T = (uint32_t)cfg.tile;
         if (t_done) fail(HD_ERR_OOM, "no memory for the FP8 operand of a streamed call");

@@ -413,6 +413,8 @@ struct PairLaunchPlan {
     uint64_t grid = 0, tiles = 0, jobs = 0;
     const void *d_jobs = nullptr;
     unsigned long long *d_counter = nullptr;
+    bool mma = false;              // the tensor-core engine (hd_mma.cu): d_items holds
+    const void *d_items = nullptr; // its work items, `tiles` of them
   };
   std::vector<Launch> launches;
   std::vector<DevBuf> blocks;  // job tables + tensor maps + tile counters
@@ -434,8 +436,10 @@ TileConfig tile_config_for(hd_ctx *ctx, uint64_t n_rows, uint64_t length, int dt
 // group, no row offset, L <= 4,000,000; HAMMINGDIST_KERNEL=lop3 turns it off).
 bool mma_eligible(const hd_alignment *aln);
 // expands rows [fp8_rows, rows) of the alignment's planes into its FP8
-// operand on `stream`; false if the operand cannot be allocated
-bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream);
+// operand on `stream` (room for cap_hint rows if it must grow); false if the
+// operand cannot be allocated
+bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream,
+                uint64_t cap_hint = 0);
 // tile rows [tile_lo, tile_hi) (128 rows each) x all earlier columns into
 // d_out (lt index out_base at d_out[0]) on `stream`; sm_limit > 0 caps the
 // persistent grid. False when the alignment is not eligible (the caller
@@ -445,6 +449,12 @@ bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_
                   cudaStream_t stream, int sm_limit);
 // FP8 dense MMA rate (FLOP/s) of this device from shared-memory operands
 double measure_mma_peak(hd_ctx *ctx);
+// One tensor-core launch for the specs it can take (dense AND rule, row
+// range starting on a 128-row tile, operand memory available); taken[k] marks
+// them. The plan keeps the launch's device block.
+void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaStream_t stream,
+                      PairLaunchPlan *plan, int sm_limit, std::vector<char> &taken);
+void launch_mma(hd_ctx *ctx, const PairLaunchPlan::Launch &L, cudaStream_t stream);
 
 // format.cu: text of rows [i_lo, i_hi) of a lower triangle held on the
 // device (lt index lt_base at d_lt[0]). Returns bytes written to d_text

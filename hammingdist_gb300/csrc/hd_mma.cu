@@ -70,11 +70,27 @@ constexpr uint64_t kRowBytesPerWord = 192;            // operand bytes per 32-si
 // K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
 constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(kTN >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
 
-struct MmaTile {
+}  // namespace
+
+// One matrix of a launch (device copy): its operand's tensor maps (boxes of
+// 256 and 128 rows) and its output.
+struct MmaJob {
+  const CUtensorMap *tm256;
+  const CUtensorMap *tm128;
+  void *out;                     // lt index out_base at out[0]
+  unsigned long long out_base;
+  uint32_t n, nkb, sites, max_dist, dtype;  // rows, K blocks per side, L, cap, 1/2/4 bytes
+};
+
+// One work item: 256 columns J x row tiles [I, I + halves) of job `job`.
+struct MmaItem {
+  uint32_t job;
   uint32_t I;       // first 128-row tile
   uint32_t J;       // 256-column tile
   uint32_t halves;  // row tiles in the item: 1 or 2
 };
+
+namespace {
 
 // 4 bits -> 4 bytes, each `one` (an FP8 value) or 0
 __device__ __forceinline__ uint32_t spread4(uint32_t nib, uint32_t one) {
@@ -174,12 +190,23 @@ __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// min(sites - matches, max_dist) of up to 32 accumulator columns (FP32
+// integers) into dst[0 .. ncols)
 template <typename T>
+__device__ __forceinline__ void store_row(T *dst, const uint32_t (&d)[32], uint32_t ncols,
+                                          uint32_t sites, uint32_t max_dist) {
+#pragma unroll
+  for (uint32_t j = 0; j < 32; ++j) {
+    if (j < ncols) {
+      const uint32_t mism = sites - (uint32_t)__uint_as_float(d[j]);
+      dst[j] = (T)(mism < max_dist ? mism : max_dist);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kMmaThreads, 1)
-    k_pairwise_mma(const __grid_constant__ CUtensorMap tm256, const __grid_constant__ CUtensorMap tm128,
-                   const MmaTile *__restrict__ tiles, uint32_t n_tiles, uint32_t n, uint32_t nkb,
-                   uint32_t sites, uint32_t max_dist, T *__restrict__ out,
-                   unsigned long long out_base, int *status) {
+    k_pairwise_mma(const MmaJob *__restrict__ jobs, const MmaItem *__restrict__ items,
+                   uint32_t n_items, int *status) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full[kMmaStages], empty[kMmaStages], done, tmem_free, fin;
   __shared__ uint32_t s_tmem;
@@ -197,8 +224,6 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     mbar_init(&fin, 1);
     fence_mbar_init();
     s_abort = 0;
-    prefetch_tmap(&tm256);
-    prefetch_tmap(&tm128);
   }
   if (warp == 0) {
     tmem_alloc(&s_tmem, kTmemCols);
@@ -214,10 +239,14 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       // producer: every K block of every item of this CTA, in order
       uint32_t g = 0;  // K blocks issued (stage g % S, phase g / S)
       bool ok = true;
-      for (uint32_t t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
-        const MmaTile tl = tiles[t];
+      for (uint32_t t = blockIdx.x; ok && t < n_items; t += gridDim.x) {
+        const MmaItem tl = items[t];
+        const MmaJob &job = jobs[tl.job];
+        const CUtensorMap *ta = tl.halves == 2 ? job.tm256 : job.tm128;
+        prefetch_tmap(ta);
+        prefetch_tmap(job.tm256);
         const int32_t ya = (int32_t)(tl.I * kTM), yb = (int32_t)(tl.J * kTN);
-        const uint32_t bytes = kBBytes + tl.halves * kHalfBytes;
+        const uint32_t bytes = kBBytes + tl.halves * kHalfBytes, nkb = job.nkb;
         for (uint32_t kb = 0; kb < nkb; ++kb) {
           const uint32_t s = g % kMmaStages;
           if ((g >= (uint32_t)kMmaStages &&
@@ -233,8 +262,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
           const int32_t xb = (int32_t)((6 * c + (q == 4 ? 5 : q)) * 128);
           uint8_t *st = smem + s * kStageBytes;
           mbar_expect_tx(&full[s], bytes);
-          tma_load_2d(st, tl.halves == 2 ? &tm256 : &tm128, xa, ya, &full[s]);
-          tma_load_2d(st + kABytes, &tm256, xb, yb, &full[s]);
+          tma_load_2d(st, ta, xa, ya, &full[s]);
+          tma_load_2d(st + kABytes, job.tm256, xb, yb, &full[s]);
           ++g;
         }
       }
@@ -251,8 +280,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       // MMA issuer
       uint32_t g = 0, it = 0;
       bool ok = true;
-      for (uint32_t t = blockIdx.x; ok && t < n_tiles; t += gridDim.x, ++it) {
-        const uint32_t halves = tiles[t].halves;
+      for (uint32_t t = blockIdx.x; ok && t < n_items; t += gridDim.x, ++it) {
+        const uint32_t halves = items[t].halves, nkb = jobs[items[t].job].nkb;
         // the epilogue has read the previous item's accumulators
         if (it > 0 && !mbar_wait_bounded(&tmem_free, (it - 1) & 1u, kMmaWaitNs)) {
           ok = false;
@@ -296,7 +325,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     const uint32_t sub = warp & 3u;
     const uint32_t t_lane = tmem + ((sub * 32) << 16);
     uint32_t it = 0;
-    for (uint32_t t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
+    for (uint32_t t = blockIdx.x; t < n_items; t += gridDim.x, ++it) {
       const bool got = mbar_wait_bounded(&done, it & 1u, 4 * kMmaWaitNs);
       if (!got) {
         atomicExch(&s_abort, 1);
@@ -305,7 +334,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       // one decision per warp: tcgen05.ld needs the whole warp
       if (__any_sync(0xffffffffu, !got || *(volatile int *)&s_abort)) break;
       tc_after_sync();
-      const MmaTile tl = tiles[t];
+      const MmaItem tl = items[t];
+      const MmaJob &job = jobs[tl.job];
+      const uint32_t n = job.n, sites = job.sites, max_dist = job.max_dist, dtype = job.dtype;
       for (uint32_t h = 0; h < tl.halves; ++h) {
         const uint32_t i = (tl.I + h) * kTM + sub * 32 + lane;  // output row
 #pragma unroll 1
@@ -317,14 +348,13 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
           const uint32_t j0 = tl.J * kTN + c;  // first column of this chunk
           if (i < n && j0 < i) {
             const uint32_t ncols = i - j0 < 32u ? i - j0 : 32u;
-            T *dst = out + ((unsigned long long)i * (i - 1) / 2 + j0 - out_base);
-#pragma unroll
-            for (uint32_t j = 0; j < 32; ++j) {
-              if (j < ncols) {
-                const uint32_t mism = sites - (uint32_t)__uint_as_float(d[j]);
-                dst[j] = (T)(mism < max_dist ? mism : max_dist);
-              }
-            }
+            const unsigned long long e0 = (unsigned long long)i * (i - 1) / 2 + j0 - job.out_base;
+            if (dtype == 1)
+              store_row<uint8_t>(static_cast<uint8_t *>(job.out) + e0, d, ncols, sites, max_dist);
+            else if (dtype == 2)
+              store_row<uint16_t>(static_cast<uint16_t *>(job.out) + e0, d, ncols, sites, max_dist);
+            else
+              store_row<uint32_t>(static_cast<uint32_t *>(job.out) + e0, d, ncols, sites, max_dist);
           }
         }
       }
@@ -385,13 +415,12 @@ __global__ void __launch_bounds__(128, 1) k_peak_mma(uint32_t rounds, int *statu
   }
 }
 
-template <typename T>
-void set_smem_once(void (*fn)(CUtensorMap, CUtensorMap, const MmaTile *, uint32_t, uint32_t,
-                              uint32_t, uint32_t, uint32_t, T *, unsigned long long, int *)) {
+void set_smem_once() {
   static std::once_flag once;
   static cudaError_t err = cudaSuccess;
   std::call_once(once, [&] {
-    err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kMmaSmem);
+    err = cudaFuncSetAttribute(k_pairwise_mma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               kMmaSmem);
   });
   HD_CUDA(err);
 }
@@ -416,28 +445,39 @@ bool mma_eligible(const hd_alignment *aln) {
   if (const char *e = std::getenv("HAMMINGDIST_KERNEL"))
     if (std::string(e) == "lop3") return false;
   // FP32 sums of up to 4 L are exact below 2^24
+  // a view qualifies when its base already holds an operand (the streamed
+  // from_fasta prepares one; a serving window should not expand a large base)
   return aln->rule == HD_RULE_AND && aln->planes == 4 && aln->groups == 1 && aln->row0 == 0 &&
-         aln->length >= 1 && aln->length <= 4000000 && aln->n_rows >= 2 &&
-         aln->n_rows < (1ull << 31);
+         (!aln->base || aln->base->fp8.p) && aln->length >= 1 && aln->length <= 4000000 &&
+         aln->n_rows >= 2 && aln->n_rows < (1ull << 31);
 }
 
-bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream) {
+bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream,
+                uint64_t cap_hint) {
   const hd_alignment *o = aln->base ? aln->base : aln;
   if (o->fp8_rows >= rows) return true;
   const uint64_t words = o->words, rb = words * kRowBytesPerWord;
-  if (!o->fp8.p) {
-    // room for every row the planes can hold (a streamed alignment grows)
-    const uint64_t cap = std::max<uint64_t>(o->plane_buf[0].bytes / (words * 16), rows);
+  if (rows > o->fp8_cap) {
+    // room for the rows asked for, or for what the caller says will come
+    const uint64_t plane_rows = o->plane_buf[0].bytes / (words * 16);
+    const uint64_t cap = std::max(rows, std::min(cap_hint, plane_rows));
+    DevBuf grown;
     try {
-      o->fp8 = DevBuf(cap * rb, stream);
+      grown = DevBuf(cap * rb, stream);
     } catch (const Error &e) {
       if (e.code != HD_ERR_OOM) throw;
       cudaGetLastError();
       return false;  // the bit-plane engine needs no extra memory
     }
+    if (o->fp8_rows) {
+      HD_CUDA(cudaMemcpyAsync(grown.p, o->fp8.p, o->fp8_rows * rb, cudaMemcpyDeviceToDevice, stream));
+      // launches on the context's other streams may still read the old
+      // operand: they finish before it is freed
+      for (cudaStream_t st : {ctx->side, ctx->side2, ctx->stream}) HD_CUDA(cudaStreamSynchronize(st));
+    }
+    o->fp8 = std::move(grown);
     o->fp8_cap = cap;
   }
-  if (rows > o->fp8_cap) fail(HD_ERR_ARG, "FP8 operand smaller than the rows asked for");
   const uint64_t total = (rows - o->fp8_rows) * words;
   const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
   k_expand_fp8<<<(unsigned)grid, 256, 0, stream>>>(o->plane_buf[0].as<uint4>(), words, o->fp8_rows,
@@ -468,80 +508,140 @@ double measure_mma_peak(hd_ctx *ctx) {
   return flop / (ms / 1e3);
 }
 
-bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
-                  void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi,
-                  cudaStream_t stream, int sm_limit) {
-  if (!mma_eligible(aln)) return false;
-  const uint64_t n = aln->n_rows;
-  const uint32_t t_hi = std::min<uint32_t>(tile_hi, (uint32_t)ceil_div(n, kTM));
-  if (t_hi <= tile_lo) return true;
-  if (!ensure_fp8(ctx, aln, n, stream)) return false;
-  const hd_alignment *o = aln->base ? aln->base : aln;
-  // Items: pairs of 128-row tiles (a single one where the range is odd) x
-  // 256-column tiles J up to the last column any of their rows needs, in
-  // bands of kMmaBand tile rows, column-major within a band.
+void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaStream_t stream,
+                      PairLaunchPlan *plan, int sm_limit, std::vector<char> &taken) {
+  taken.assign(specs.size(), 0);
+  struct Job {
+    size_t k;
+    uint32_t t_lo, t_hi;
+    double cost;
+  };
+  std::vector<Job> js;
+  for (size_t k = 0; k < specs.size(); ++k) {
+    const PairJobSpec &sp = specs[k];
+    const hd_alignment *a = sp.aln;
+    if (!mma_eligible(a) || sp.tile_hi <= sp.tile_lo) continue;
+    // the caller's tile rows are in units of its configuration's tile edge
+    const uint64_t edge = sp.cfg.tile > 0 ? (uint64_t)sp.cfg.tile : kTile;
+    const uint64_t row_lo = sp.tile_lo * edge, row_hi = std::min<uint64_t>(sp.tile_hi * edge, a->n_rows);
+    if (row_lo % kTM || row_hi <= row_lo) continue;
+    if (!ensure_fp8(ctx, a, a->n_rows, stream)) continue;
+    const uint32_t lo = (uint32_t)(row_lo / kTM), hi = (uint32_t)ceil_div(row_hi, kTM);
+    js.push_back({k, lo, hi, (double)a->words * ((double)hi * hi - (double)lo * lo)});
+    taken[k] = 1;
+  }
+  if (js.empty()) return;
+  // biggest jobs first: their items start early, small ones fill the tail
+  std::stable_sort(js.begin(), js.end(), [](const Job &a, const Job &b) { return a.cost > b.cost; });
   uint32_t band = kMmaBand;
   if (const char *e = std::getenv("HAMMINGDIST_MMA_BAND")) band = (uint32_t)std::max(2, std::atoi(e)) & ~1u;
-  std::vector<MmaTile> list;
-  for (uint32_t b = tile_lo; b < t_hi; b += band) {
-    const uint32_t e = std::min(b + band, t_hi);
-    const uint32_t j_end = (uint32_t)ceil_div((uint64_t)e * kTM - 1, kTN);  // columns < last row
-    for (uint32_t J = 0; J < j_end; ++J)
-      for (uint32_t I = b; I < e; I += 2) {
-        const uint32_t h = std::min(2u, e - I);
-        // rows [128 I, 128 (I + h)) need columns < 128 (I + h) - 1
-        if ((uint64_t)J * kTN < (uint64_t)(I + h) * kTM - 1) list.push_back({I, J, h});
-      }
-  }
+  // Items of each job: pairs of 128-row tiles (a single one where a range is
+  // odd) x 256-column tiles up to the last column any of their rows needs, in
+  // bands of `band` tile rows, column-major within a band.
+  std::vector<MmaItem> list;
+  for (uint32_t q = 0; q < (uint32_t)js.size(); ++q)
+    for (uint32_t b = js[q].t_lo; b < js[q].t_hi; b += band) {
+      const uint32_t e = std::min(b + band, js[q].t_hi);
+      const uint32_t j_end = (uint32_t)ceil_div((uint64_t)e * kTM - 1, kTN);
+      for (uint32_t J = 0; J < j_end; ++J)
+        for (uint32_t I = b; I < e; I += 2) {
+          const uint32_t h = std::min(2u, e - I);
+          // rows [128 I, 128 (I + h)) need columns < 128 (I + h) - 1
+          if ((uint64_t)J * kTN < (uint64_t)(I + h) * kTM - 1) list.push_back({q, I, J, h});
+        }
+    }
   // Persistent CTAs take items round-robin: split the last pairs into single
   // row tiles until the item count is a multiple of the grid, so that every
   // CTA ends within one row tile of the others (a short list splits them all
   // to fill more SMs).
   const int sms = sm_limit > 0 && sm_limit < ctx->sm_count ? sm_limit : ctx->sm_count;
   uint64_t pairs = 0;
-  for (const MmaTile &m : list) pairs += m.halves == 2;
+  for (const MmaItem &m : list) pairs += m.halves == 2;
   const uint64_t grid_n = std::min<uint64_t>(list.size() + pairs, (uint64_t)sms);
   uint64_t split = list.size() < grid_n ? grid_n - list.size()
                                         : (grid_n - list.size() % grid_n) % grid_n;
-  std::vector<MmaTile> tail;
+  std::vector<MmaItem> tail;
   for (size_t k = list.size(); k-- > 0 && split > 0;) {
     if (list[k].halves != 2) continue;
-    tail.push_back({list[k].I + 1, list[k].J, 1});
+    tail.push_back({list[k].job, list[k].I + 1, list[k].J, 1});
     list[k].halves = 1;
     --split;
   }
   list.insert(list.end(), tail.rbegin(), tail.rend());
-  DevBuf d_list(list.size() * sizeof(MmaTile), stream);
-  // from pageable memory: the call has consumed `list` when it returns
-  HD_CUDA(cudaMemcpyAsync(d_list.p, list.data(), list.size() * sizeof(MmaTile),
-                          cudaMemcpyHostToDevice, stream));
-  const uint64_t rb = o->words * kRowBytesPerWord;
-  CUtensorMap tm256, tm128;
-  make_tmap_u8(ctx, &tm256, o->fp8.p, rb, n, kTN);
-  make_tmap_u8(ctx, &tm128, o->fp8.p, rb, n, kTM);
-  const unsigned grid = (unsigned)grid_n;
-  const uint32_t n_tiles = (uint32_t)list.size(), n32 = (uint32_t)n;
-  const uint32_t nkb = (uint32_t)(o->words * 5 / 4), sites = (uint32_t)aln->length;
-  const auto *tl = d_list.as<MmaTile>();
-  if (dtype_bytes == 1) {
-    set_smem_once(k_pairwise_mma<uint8_t>);
-    k_pairwise_mma<uint8_t><<<grid, kMmaThreads, kMmaSmem, stream>>>(
-        tm256, tm128, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint8_t *>(d_out),
-        out_base, ctx->d_status);
-  } else if (dtype_bytes == 2) {
-    set_smem_once(k_pairwise_mma<uint16_t>);
-    k_pairwise_mma<uint16_t><<<grid, kMmaThreads, kMmaSmem, stream>>>(
-        tm256, tm128, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint16_t *>(d_out),
-        out_base, ctx->d_status);
-  } else {
-    set_smem_once(k_pairwise_mma<uint32_t>);
-    k_pairwise_mma<uint32_t><<<grid, kMmaThreads, kMmaSmem, stream>>>(
-        tm256, tm128, tl, n_tiles, n32, nkb, sites, max_dist, static_cast<uint32_t *>(d_out),
-        out_base, ctx->d_status);
+  // one device block: [tensor maps (2 per job)][jobs][items]
+  const size_t nj = js.size();
+  const size_t tm_bytes = nj * 2 * sizeof(CUtensorMap);
+  const size_t job_bytes = round_up(nj * sizeof(MmaJob), 64);
+  std::vector<uint8_t> host(tm_bytes + job_bytes + list.size() * sizeof(MmaItem), 0);
+  DevBuf dev(host.size(), stream);
+  auto *tms = reinterpret_cast<CUtensorMap *>(host.data());
+  auto *jobs = reinterpret_cast<MmaJob *>(host.data() + tm_bytes);
+  const auto *d_tms = reinterpret_cast<const CUtensorMap *>(dev.p);
+  for (size_t q = 0; q < nj; ++q) {
+    const PairJobSpec &sp = specs[js[q].k];
+    const hd_alignment *a = sp.aln;
+    const hd_alignment *o = a->base ? a->base : a;
+    const uint64_t rb = o->words * kRowBytesPerWord;
+    make_tmap_u8(ctx, &tms[2 * q], o->fp8.p, rb, a->n_rows, kTN);
+    make_tmap_u8(ctx, &tms[2 * q + 1], o->fp8.p, rb, a->n_rows, kTM);
+    MmaJob &m = jobs[q];
+    m.tm256 = d_tms + 2 * q;
+    m.tm128 = d_tms + 2 * q + 1;
+    m.out = sp.d_out;
+    m.out_base = sp.out_base;
+    m.n = (uint32_t)a->n_rows;
+    m.nkb = (uint32_t)(o->words * 5 / 4);
+    m.sites = (uint32_t)a->length;
+    m.max_dist = sp.max_dist;
+    m.dtype = (uint32_t)sp.dtype;
   }
+  std::memcpy(host.data() + tm_bytes + job_bytes, list.data(), list.size() * sizeof(MmaItem));
+  // from pageable memory: the call has consumed `host` when it returns
+  HD_CUDA(cudaMemcpyAsync(dev.p, host.data(), host.size(), cudaMemcpyHostToDevice, stream));
+  PairLaunchPlan::Launch L;
+  L.mma = true;
+  L.fn = reinterpret_cast<const void *>(k_pairwise_mma);
+  L.smem = kMmaSmem;
+  L.tile = kTM;
+  L.jobs = nj;
+  L.tiles = list.size();
+  L.grid = grid_n;
+  L.d_jobs = dev.as<uint8_t>() + tm_bytes;
+  L.d_items = dev.as<uint8_t>() + tm_bytes + job_bytes;
+  plan->launches.push_back(L);
+  plan->blocks.push_back(std::move(dev));
+}
+
+void launch_mma(hd_ctx *ctx, const PairLaunchPlan::Launch &L, cudaStream_t stream) {
+  set_smem_once();
+  k_pairwise_mma<<<(unsigned)L.grid, kMmaThreads, kMmaSmem, stream>>>(
+      static_cast<const MmaJob *>(L.d_jobs), static_cast<const MmaItem *>(L.d_items),
+      (uint32_t)L.tiles, ctx->d_status);
   HD_LAUNCHED(ctx);
-  ctx->last_pair_tiles += n_tiles;
-  return true;  // d_list is freed in stream order, after the kernel
+  ctx->last_pair_tiles += L.tiles;
+}
+
+bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
+                  void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi,
+                  cudaStream_t stream, int sm_limit) {
+  if (!mma_eligible(aln)) return false;
+  std::vector<PairJobSpec> specs(1);
+  PairJobSpec &sp = specs[0];
+  sp.aln = aln;
+  sp.dtype = dtype_bytes;
+  sp.max_dist = max_dist;
+  sp.d_out = d_out;
+  sp.out_base = out_base;
+  sp.cfg.tile = kTM;
+  sp.tile_lo = tile_lo;
+  sp.tile_hi = std::min<uint32_t>(tile_hi, (uint32_t)ceil_div(aln->n_rows, kTM));
+  if (sp.tile_hi <= sp.tile_lo) return true;
+  PairLaunchPlan plan;
+  std::vector<char> taken;
+  prepare_mma_jobs(ctx, specs, stream, &plan, sm_limit, taken);
+  if (!taken[0]) return false;
+  for (const auto &L : plan.launches) launch_mma(ctx, L, stream);
+  return true;  // the plan's device block is freed in stream order, after the kernel
 }
 
 }  // namespace hd

@@ -358,6 +358,9 @@ bool tile_config_valid(int tile, int stages) {
 // a batch captures only the launch step and replays it.
 void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStream_t stream,
                            PairLaunchPlan *plan, int sm_limit) {
+  // the dense AND rule goes to the tensor-core engine, one launch for all of it
+  std::vector<char> taken;
+  prepare_mma_jobs(ctx, specs, stream, plan, sm_limit, taken);
   struct Group {
     const Variant *v;
     std::vector<size_t> idx;
@@ -365,7 +368,7 @@ void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStr
   std::vector<Group> groups;
   for (size_t k = 0; k < specs.size(); ++k) {
     PairJobSpec &s = specs[k];
-    if (s.aln->n_rows < 2 || s.tile_hi <= s.tile_lo) continue;
+    if (taken[k] || s.aln->n_rows < 2 || s.tile_hi <= s.tile_lo) continue;
     if (s.aln->n_rows > 0xffffffffull) fail(HD_ERR_ARG, "too many rows");
     const Variant *v = &find_variant(s.cfg.tile, s.cfg.stages, s.aln->planes);
     s.cfg = {v->tile, v->stages};
@@ -436,6 +439,10 @@ void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStr
 
 void launch_pairwise_plan(hd_ctx *ctx, PairLaunchPlan &plan, cudaStream_t stream) {
   for (auto &L : plan.launches) {
+    if (L.mma) {
+      launch_mma(ctx, L, stream);
+      continue;
+    }
     HD_CUDA(cudaMemsetAsync(L.d_counter, 0, sizeof(unsigned long long), stream));
     const void *jobs = L.d_jobs;
     uint32_t nj = (uint32_t)L.jobs;
