@@ -107,6 +107,8 @@ def lib():
 # void *(*hd_output_fn)(void *user, uint64_t index, uint64_t n_rows, uint64_t entries)
 OUTPUT_FN = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
                              ctypes.c_uint64)
+# hd_pairwise_lt_fasta_file's request for a second copy of its result
+OUTPUT_MIRROR = 2**64 - 1
 
 
 class HDError(RuntimeError):
@@ -219,17 +221,24 @@ class Context:
         return Alignment(self, a)
 
     def pairwise_lt_fasta_file(self, path, dtype=np.uint8, max_distance=None,
-                               remove_duplicates=False):
+                               remove_duplicates=False, mirror=False):
         """from_fasta(use_gpu=True) of a file in one call (distances overlap
-        the read for large files): (lower triangle, Alignment)."""
+        the read for large files): (lower triangle, Alignment), and with
+        mirror=True also the second copy the library writes on request
+        (HD_OUTPUT_MIRROR)."""
         dt = np.dtype(dtype)
         md = np.iinfo(dt).max if max_distance is None else max_distance
         box = {}
 
         @OUTPUT_FN
         def alloc(user, index, n_rows, entries):
+            key = "lt"
+            if index == OUTPUT_MIRROR:
+                if not mirror:
+                    return None
+                key = "mirror"
             arr = np.empty(max(int(entries), 1), dtype=dt)
-            box["lt"] = arr[: int(entries)]
+            box[key] = arr[: int(entries)]
             return arr.ctypes.data
 
         a = vp()
@@ -237,6 +246,8 @@ class Context:
                                                     int(remove_duplicates), dt.itemsize, int(md),
                                                     ctypes.cast(alloc, vp), None,
                                                     ctypes.byref(a)))
+        if mirror:
+            return box["lt"], Alignment(self, a), box.get("mirror")
         return box["lt"], Alignment(self, a)
 
     def alignment_from_sequences(self, seqs, include_x=False, semantics=SEM_GPU) -> Alignment:
@@ -404,6 +415,8 @@ class Context:
 
         @OUTPUT_FN
         def alloc(user, index, n_rows, entries):
+            if index == OUTPUT_MIRROR:
+                return None
             arr = np.empty(max(int(entries), 1), dtype=dtypes[index])
             outs[index] = arr[: int(entries)]
             return arr.ctypes.data

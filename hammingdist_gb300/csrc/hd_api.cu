@@ -851,6 +851,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       const uint64_t entries = a->n_rows < 2 ? 0 : tri(a->n_rows);
       void *host = out_fn(user, 0, a->n_rows, entries);
       if (!host && entries) fail(HD_ERR_ARG, "output callback returned no buffer");
+      void *mirror = entries ? out_fn(user, HD_OUTPUT_MIRROR, a->n_rows, entries) : nullptr;
       if (entries) {
         DevBuf d_out(entries * dtype_bytes, ctx->stream);
         hd::pairwise_tiles(ctx, a, dtype_bytes, md, d_out.p, 0, 0,
@@ -859,6 +860,11 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         prefault_host(host, entries * dtype_bytes);
         HD_CUDA(cudaMemcpyAsync(host, d_out.p, entries * dtype_bytes, cudaMemcpyDeviceToHost,
                                 ctx->stream));
+        if (mirror) {
+          prefault_host(mirror, entries * dtype_bytes);
+          HD_CUDA(cudaMemcpyAsync(mirror, d_out.p, entries * dtype_bytes, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+        }
         HD_CUDA(cudaStreamSynchronize(ctx->stream));
         check_status(ctx);
       }
@@ -1111,15 +1117,19 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     const uint64_t entries = K < 2 ? 0 : tri(K);
     void *host = out_fn(user, 0, K, entries);
     if (!host && entries) fail(HD_ERR_ARG, "output callback returned no buffer");
+    void *mirror = entries ? out_fn(user, HD_OUTPUT_MIRROR, K, entries) : nullptr;
     if (entries) {
       prefault_host(host, entries * dtype_bytes);  // while the kernels run
+      if (mirror) prefault_host(mirror, entries * dtype_bytes);
       for (const auto &b : bands) {
         const uint64_t e0 = tri(b->row_lo), e1 = tri(b->row_hi);
         if (e1 <= e0) continue;
         HD_CUDA(cudaStreamWaitEvent(ctx->up, b->done, 0));
-        HD_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(host) + e0 * dtype_bytes,
-                                d_lt.as<uint8_t>() + e0 * dtype_bytes, (e1 - e0) * dtype_bytes,
-                                cudaMemcpyDeviceToHost, ctx->up));
+        for (void *dst : {host, mirror})
+          if (dst)
+            HD_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(dst) + e0 * dtype_bytes,
+                                    d_lt.as<uint8_t>() + e0 * dtype_bytes, (e1 - e0) * dtype_bytes,
+                                    cudaMemcpyDeviceToHost, ctx->up));
       }
     }
     for (cudaStream_t s : {ctx->side2, ctx->side, ctx->up, ctx->stream})

@@ -151,6 +151,15 @@ struct DataSet {
   uint64_t nsamples = 0;
   HostVec<T> result;
   std::vector<uint64_t> sequence_indices;
+  // A second copy of the result that the library wrote while the distances
+  // ran (HD_OUTPUT_MIRROR). The first lt_array access hands it out as its
+  // fresh array, and later accesses copy; shared by copies of the DataSet, so
+  // only one of them can hand it out.
+  struct FirstCopy {
+    std::mutex mu;
+    std::unique_ptr<HostVec<T>> buf;
+  };
+  std::shared_ptr<FirstCopy> first_copy;
 
   int at(const std::array<size_t, 2> &ij) const {
     size_t i = ij[0], j = ij[1];
@@ -234,8 +243,17 @@ DataSet<T> from_fasta(const std::string &filename, bool include_x, bool remove_d
   if (use_gpu && !include_x && n == 0) {
     // one call: for large files the distances overlap the read
     DataSet<T> ds;
-    hd_output_fn alloc = [](void *user, uint64_t, uint64_t rows, uint64_t entries) -> void * {
+    hd_output_fn alloc = [](void *user, uint64_t index, uint64_t rows, uint64_t entries) -> void * {
       auto *d = static_cast<DataSet<T> *>(user);
+      if (index == HD_OUTPUT_MIRROR) {
+        // the first lt_array's copy, made while the distances run; not for
+        // results above 2 GB, which would double the host memory held
+        if (entries * sizeof(T) > (2ull << 30)) return nullptr;
+        d->first_copy = std::make_shared<typename DataSet<T>::FirstCopy>();
+        d->first_copy->buf = std::make_unique<HostVec<T>>();
+        d->first_copy->buf->resize(entries);
+        return d->first_copy->buf->data();
+      }
       d->nsamples = rows;
       d->result.resize(entries);  // its pages are first touched while the kernels run
       return d->result.data();
@@ -495,7 +513,21 @@ void bind_dataset(py::module_ &m, const char *name, int default_threshold) {
       .def("__getitem__", &DataSet<T>::at)
       .def_readonly("_distances", &DataSet<T>::result)
       .def_property_readonly("lt_array", [](const DataSet<T> &self) {
-        // a fresh copy on every access, as the reference's py::array(size, ptr)
+        // a fresh copy on every access, as the reference's py::array(size, ptr);
+        // the first access takes the copy written while the distances ran
+        if (self.first_copy) {
+          std::unique_ptr<HostVec<T>> b;
+          {
+            std::lock_guard<std::mutex> lk(self.first_copy->mu);
+            b = std::move(self.first_copy->buf);
+          }
+          if (b && b->size() == self.result.size()) {
+            HostVec<T> *raw = b.release();
+            py::capsule owner(raw, [](void *p) { delete static_cast<HostVec<T> *>(p); });
+            say_host("lt_array copy", 0.0);
+            return py::array_t<T>((py::ssize_t)raw->size(), raw->data(), owner);
+          }
+        }
         py::array_t<T> a((py::ssize_t)self.result.size());
         const auto tc = std::chrono::steady_clock::now();
         copy_parallel(a.mutable_data(), self.result.data(), self.result.size() * sizeof(T));

@@ -48,6 +48,12 @@ extern "C" {
  * dtype. It need not be touched yet. NULL with entries > 0 fails the call
  * with HD_ERR_ARG. Calls for different indices may run concurrently. */
 typedef void *(*hd_output_fn)(void *user, uint64_t index, uint64_t n_rows, uint64_t entries);
+/* hd_pairwise_lt_fasta_file asks once more, after index 0, with this index:
+ * a non-NULL buffer of the same size receives a second copy of the result,
+ * written while the distances run (a binding can hand it out as the first of
+ * the fresh copies the reference's lt_array returns,
+ * python/hammingdist.cc:47-49,65-67). NULL: no second copy. */
+#define HD_OUTPUT_MIRROR UINT64_MAX
 
 /* ---- semantics of a pairwise matrix ------------------------------------- */
 /* HD_SEM_GPU: the reference's use_gpu=True semantics — the dense AND rule of
@@ -122,14 +128,16 @@ int hd_alignment_from_fasta_file(hd_ctx *ctx, const char *path, int remove_dupli
  * (include/hamming/hamming.hh:169-177 with the dense AND rule): the lower
  * triangle (dtype_bytes, max_distance as in hd_pairwise_lt) is copied to the
  * buffer out_fn returns (index 0, n_rows, entries), and *aln_out receives the
- * alignment (sequence indices; free it with hd_alignment_free). For a file
- * of 64 MB or more the distances overlap the read: the file is ingested in
- * parts that end at record headers (by default after ~20% and ~50% of its
- * bytes; HAMMINGDIST_STREAM_SPLITS sets up to three splits); after each part the
+ * alignment (sequence indices; free it with hd_alignment_free). out_fn is
+ * then asked for HD_OUTPUT_MIRROR (see there). For a file of 64 MB or more
+ * the distances overlap the read: the file is ingested in parts that end at
+ * record headers (by default after ~20% and ~50% of its bytes;
+ * HAMMINGDIST_STREAM_SPLITS sets up to three splits); after each part the
  * unique rows so far (the first rows of the final result) are packed and the
  * tile rows that are complete run while the rest is read, and finished
- * ranges of the result are copied while later ones compute. Multi-line records, or a file already on the device, take the
- * plain order: read, ingest, distances. Results and errors are those of
+ * ranges of the result are copied while later ones compute. Multi-line
+ * records, or a file already on the device, take the plain order: read,
+ * ingest, distances. Results and errors are those of
  * hd_alignment_from_fasta_file + hd_pairwise_lt. */
 int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicates,
                               int dtype_bytes, int64_t max_distance, hd_output_fn out_fn,

@@ -218,3 +218,37 @@ def test_multiline_record_with_three_splits(ctx, tmp_path, monkeypatch, where):
     np.testing.assert_array_equal(lt, want)
     np.testing.assert_array_equal(aln.sequence_indices(), want_idx)
     aln.free()
+
+
+def test_mirror_copy(ctx, big, tmp_path):
+    # HD_OUTPUT_MIRROR: a second copy of the result written while the
+    # distances run, on the streamed path and on a small file's plain order
+    path, fa, rows = big
+    _touch(path)
+    lt, aln, mirror = ctx.pairwise_lt_fasta_file(path, remove_duplicates=True, mirror=True)
+    np.testing.assert_array_equal(mirror, lt)
+    assert mirror.ctypes.data != lt.ctypes.data
+    aln.free()
+    small = tmp_path / "small.fasta"
+    small.write_bytes(synth.to_fasta(rows[:300]))
+    lt, aln, mirror = ctx.pairwise_lt_fasta_file(str(small), dtype=np.uint16, mirror=True)
+    np.testing.assert_array_equal(mirror, lt)
+    aln.free()
+
+
+def test_module_first_lt_array_is_a_fresh_copy(big):
+    # the first lt_array access hands out the copy written during the call;
+    # every access is still a fresh array that aliases neither the DataSet
+    # nor another access
+    import hammingdist_gb300 as hd
+
+    path, fa, rows = big
+    _touch(path)
+    ds = hd.from_fasta(path, use_gpu=True, remove_duplicates=True)
+    a = np.asarray(ds.lt_array)
+    b = np.asarray(ds.lt_array)
+    np.testing.assert_array_equal(a, b)
+    a[:] = 7
+    c = np.asarray(ds.lt_array)
+    np.testing.assert_array_equal(b, c)
+    assert ds[1, 0] == int(b[0])
