@@ -967,6 +967,11 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     uint64_t L = 0, words = 0, R_max = 0, K = 0, B_prev = 0, tiles = 0;
     uint32_t T = 0, t_done = 0;
     bool use_mma = false;  // tensor-core engine: 128-row tiles
+    // SMs left to the next part's ingest while a band runs
+    // (HAMMINGDIST_STREAM_FREE_SMS, default 16)
+    int free_sms = 16;
+    if (const char *e = std::getenv("HAMMINGDIST_STREAM_FREE_SMS"))
+      free_sms = std::min(std::max(0, std::atoi(e)), ctx->sm_count - 1);
     hd::TileConfig cfg;
     uint4 *g0 = nullptr;
     // tile rows [t_lo, t_hi) of the first `rows` unique rows on stream s
@@ -1082,7 +1087,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         if (t_end > t_done) {
           cudaEvent_t packed = sync.make();
           HD_CUDA(cudaEventRecord(packed, ctx->stream));
-          launch(t_done, t_end, K, ctx->side, std::max(1, ctx->sm_count - 16), packed);
+          launch(t_done, t_end, K, ctx->side, std::max(1, ctx->sm_count - free_sms), packed);
           t_done = t_end;
         }
         B_prev = B;
