@@ -65,7 +65,14 @@ constexpr int kMmaSmem = kMmaStages * kStageBytes + 1024;
 constexpr uint32_t kTmemCols = 512;                   // row tile h at columns 256 h
 constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
 constexpr uint32_t kMmaBand = 16;  // tile rows per L2 band (HAMMINGDIST_MMA_BAND overrides)
-constexpr uint64_t kRowBytesPerWord = 192;            // operand bytes per 32-site word
+// operand bytes per 32-site word: P planes + the two dash blocks, 32 B each
+__host__ __device__ constexpr uint64_t row_bytes_per_word(uint32_t planes) {
+  return (uint64_t)(planes + 2) * 32;
+}
+// the column side's dash value -(P - 1) in E4M3: -3 (0xC4), -4 (0xC8), -5 (0xCA)
+__device__ __forceinline__ uint32_t dash_neg(uint32_t planes) {
+  return planes == 4 ? 0xC4u : planes == 5 ? 0xC8u : 0xCAu;
+}
 // instruction descriptor: D F32 (bits 4-5 = 1), A and B E4M3 (0), both
 // K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
 constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(kTN >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
@@ -80,6 +87,7 @@ struct MmaJob {
   void *out;                     // lt index out_base at out[0]
   unsigned long long out_base;
   uint32_t n, nkb, sites, max_dist, dtype;  // rows, K blocks per side, L, cap, 1/2/4 bytes
+  uint32_t planes;                          // P: P + 1 K blocks per 128 sites and side
 };
 
 // One work item: 256 columns J x row tiles [I, I + halves) of job `job`.
@@ -104,25 +112,34 @@ __device__ __forceinline__ void put32(uint8_t *dst, uint32_t b, uint32_t one) {
                     spread4((b >> 24) & 15u, one), spread4(b >> 28, one));
 }
 
-// Rows [row_lo, row_hi) of the AND-rule bit planes -> FP8 operand rows.
-// One thread per (row, 32-site word): 16 bytes read, 192 bytes written.
-__global__ void k_expand_fp8(const uint4 *__restrict__ planes, uint64_t words, uint64_t row_lo,
-                             uint64_t row_hi, uint64_t L, uint8_t *__restrict__ x) {
+// Rows [row_lo, row_hi) of a P-plane alignment (P = 4: the AND rule; 5, 6:
+// the sparse rules, planes 4-5 in the second group) -> FP8 operand rows.
+// One thread per (row, 32-site word): 16 or 32 bytes read, (P + 2) x 32
+// bytes written. The dash is the AND of the P planes ('-' has every plane).
+__global__ void k_expand_fp8(const uint4 *__restrict__ g0, const uint4 *__restrict__ g1,
+                             uint32_t planes, uint64_t words, uint64_t row_lo, uint64_t row_hi,
+                             uint64_t L, uint8_t *__restrict__ x) {
   const uint64_t total = (row_hi - row_lo) * words;
+  const uint32_t nb = planes + 2;  // 128-byte blocks per 128 sites
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
        t += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t r = row_lo + t / words, w = t % words;
-    const uint4 p = planes[r * words + w];
+    const uint4 p = g0[r * words + w];
+    const uint4 p1 = planes > 4 ? g1[r * words + w] : make_uint4(0u, 0u, 0u, 0u);
     const uint64_t s0 = w * 32;
     const uint32_t valid = s0 >= L ? 0u : (L - s0 >= 32 ? 0xffffffffu : ((1u << (L - s0)) - 1u));
-    const uint32_t dash = p.x & p.y & p.z & p.w & valid;
-    uint8_t *blk = x + r * (words * kRowBytesPerWord) + (w / 4) * 768 + (w % 4) * 32;
+    uint32_t dash = p.x & p.y & p.z & p.w & valid;
+    if (planes > 4) dash &= p1.x;
+    if (planes > 5) dash &= p1.y;
+    uint8_t *blk = x + r * (words * row_bytes_per_word(planes)) + (w / 4) * (nb * 128) + (w % 4) * 32;
     put32(blk, p.x & valid, 0x38u);
     put32(blk + 128, p.y & valid, 0x38u);
     put32(blk + 256, p.z & valid, 0x38u);
     put32(blk + 384, p.w & valid, 0x38u);
-    put32(blk + 512, dash, 0x38u);  // 1.0: the row side
-    put32(blk + 640, dash, 0xC4u);  // -3.0: the column side
+    if (planes > 4) put32(blk + 512, p1.x & valid, 0x38u);
+    if (planes > 5) put32(blk + 640, p1.y & valid, 0x38u);
+    put32(blk + planes * 128, dash, 0x38u);               // 1.0: the row side
+    put32(blk + (planes + 1) * 128, dash, dash_neg(planes));  // -(P - 1): the column side
   }
 }
 
@@ -246,7 +263,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
         prefetch_tmap(ta);
         prefetch_tmap(job.tm256);
         const int32_t ya = (int32_t)(tl.I * kTM), yb = (int32_t)(tl.J * kTN);
-        const uint32_t bytes = kBBytes + tl.halves * kHalfBytes, nkb = job.nkb;
+        const uint32_t bytes = kBBytes + tl.halves * kHalfBytes, nkb = job.nkb, P = job.planes;
         for (uint32_t kb = 0; kb < nkb; ++kb) {
           const uint32_t s = g % kMmaStages;
           if ((g >= (uint32_t)kMmaStages &&
@@ -255,11 +272,12 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
             ok = false;
             break;
           }
-          // K block kb: 128 sites of chunk kb / 5, block kb % 5 (planes 0-3,
-          // then the dash: +1 for the rows, the -3 block for the columns)
-          const uint32_t c = kb / 5, q = kb % 5;
-          const int32_t xa = (int32_t)((6 * c + q) * 128);
-          const int32_t xb = (int32_t)((6 * c + (q == 4 ? 5 : q)) * 128);
+          // K block kb: 128 sites of chunk kb / (P + 1), block kb % (P + 1)
+          // (planes 0 .. P-1, then the dash: the +1 block for the rows, the
+          // -(P - 1) block for the columns)
+          const uint32_t c = kb / (P + 1), q = kb % (P + 1);
+          const int32_t xa = (int32_t)(((P + 2) * c + q) * 128);
+          const int32_t xb = (int32_t)(((P + 2) * c + (q == P ? P + 1 : q)) * 128);
           uint8_t *st = smem + s * kStageBytes;
           mbar_expect_tx(&full[s], bytes);
           tma_load_2d(st, ta, xa, ya, &full[s]);
@@ -445,18 +463,22 @@ bool mma_eligible(const hd_alignment *aln) {
   if (const char *e = std::getenv("HAMMINGDIST_KERNEL"))
     if (std::string(e) == "lop3") return false;
   // FP32 sums of up to 4 L are exact below 2^24
-  // a view qualifies when its base already holds an operand (the streamed
-  // from_fasta prepares one; a serving window should not expand a large base)
-  return aln->rule == HD_RULE_AND && aln->planes == 4 && aln->groups == 1 && aln->row0 == 0 &&
-         (!aln->base || aln->base->fp8.p) && aln->length >= 1 && aln->length <= 4000000 &&
-         aln->n_rows >= 2 && aln->n_rows < (1ull << 31);
+  // the AND rule (4 planes) or a sparse rule (5, 6 planes); FP32 sums of up
+  // to P L are exact below 2^24. A view qualifies when its base already holds
+  // an operand (the streamed from_fasta prepares one; a serving window should
+  // not expand a large base).
+  const uint64_t P = (uint64_t)aln->planes;
+  const bool shape = (P == 4 && aln->groups == 1) || ((P == 5 || P == 6) && aln->groups == 2);
+  return shape && aln->row0 == 0 && (!aln->base || aln->base->fp8.p) && aln->length >= 1 &&
+         aln->length * P < (1ull << 24) && aln->n_rows >= 2 && aln->n_rows < (1ull << 31);
 }
 
 bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream,
                 uint64_t cap_hint) {
   const hd_alignment *o = aln->base ? aln->base : aln;
   if (o->fp8_rows >= rows) return true;
-  const uint64_t words = o->words, rb = words * kRowBytesPerWord;
+  const uint32_t P = (uint32_t)o->planes;
+  const uint64_t words = o->words, rb = words * row_bytes_per_word(P);
   if (rows > o->fp8_cap) {
     // room for the rows asked for, or for what the caller says will come
     const uint64_t plane_rows = o->plane_buf[0].bytes / (words * 16);
@@ -480,8 +502,9 @@ bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_
   }
   const uint64_t total = (rows - o->fp8_rows) * words;
   const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
-  k_expand_fp8<<<(unsigned)grid, 256, 0, stream>>>(o->plane_buf[0].as<uint4>(), words, o->fp8_rows,
-                                                   rows, o->length, o->fp8.as<uint8_t>());
+  k_expand_fp8<<<(unsigned)grid, 256, 0, stream>>>(
+      o->plane_buf[0].as<uint4>(), P > 4 ? o->plane_buf[1].as<uint4>() : nullptr, P, words,
+      o->fp8_rows, rows, o->length, o->fp8.as<uint8_t>());
   HD_LAUNCHED(ctx);
   o->fp8_rows = rows;
   return true;
@@ -581,7 +604,7 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     const PairJobSpec &sp = specs[js[q].k];
     const hd_alignment *a = sp.aln;
     const hd_alignment *o = a->base ? a->base : a;
-    const uint64_t rb = o->words * kRowBytesPerWord;
+    const uint64_t rb = o->words * row_bytes_per_word((uint32_t)o->planes);
     make_tmap_u8(ctx, &tms[2 * q], o->fp8.p, rb, a->n_rows, kTN);
     make_tmap_u8(ctx, &tms[2 * q + 1], o->fp8.p, rb, a->n_rows, kTM);
     MmaJob &m = jobs[q];
@@ -590,7 +613,8 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     m.out = sp.d_out;
     m.out_base = sp.out_base;
     m.n = (uint32_t)a->n_rows;
-    m.nkb = (uint32_t)(o->words * 5 / 4);
+    m.nkb = (uint32_t)(o->words / 4 * (o->planes + 1));
+    m.planes = (uint32_t)o->planes;
     m.sites = (uint32_t)a->length;
     m.max_dist = sp.max_dist;
     m.dtype = (uint32_t)sp.dtype;

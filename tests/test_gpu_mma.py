@@ -81,3 +81,28 @@ def test_mma_larger(ctx):
     g = [got[pick[a] * (pick[a] - 1) // 2 + pick[b]] for a in range(len(pick)) for b in range(a)]
     np.testing.assert_array_equal(np.array(g, dtype=np.uint8), sub)
     aln.free()
+
+
+@pytest.mark.parametrize("include_x", [False, True])
+@pytest.mark.parametrize("n,L", [(3, 100), (129, 1000), (300, 2999), (700, 29903)])
+def test_mma_sparse_rules(ctx, include_x, n, L):
+    # use_gpu=False semantics on low-diversity rows: the reference CPU takes
+    # the sparse rule (5 planes, or 6 with include_x); on the tensor cores
+    # match = <planes> - (P - 1) [dash][dash]
+    from hammingdist_gb300 import abi
+
+    rows, _, _ = synth.alignment(n, L, p=1e-4, seed=n + L, dash_max=min(10, L // 20),
+                                 n_rate=0.0)
+    rows[::50, ::101] = ord("X")
+    seqs = [r.tobytes() for r in rows]
+    aln = ctx.alignment_from_sequences(seqs, include_x=include_x, semantics=abi.SEM_CPU)
+    want_lt, used_sparse = o.lt_cpu(seqs, include_x=include_x)
+    # the heuristic's choice is the reference's; with include_x it is always sparse
+    assert (aln.rule != "and") == used_sparse and (used_sparse or not include_x)
+    if used_sparse:
+        assert aln.rule == ("sparse_x" if include_x else "sparse")
+    for dtype, md in ((np.uint8, 255), (np.uint16, 65535), (np.uint8, 2)):
+        got, want = _both(ctx, aln, dtype=dtype, max_distance=md)
+        np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(_both(ctx, aln)[0], want_lt)
+    aln.free()
