@@ -1070,7 +1070,14 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         owner->n_rows = R_max;  // the eligibility test looks at the shape only
         use_mma = hd::mma_eligible(owner.get());
         owner->n_rows = 0;
-        if (use_mma) T = hd::kTile;
+        if (use_mma) {
+          // bands count tile rows of 128; a band the tensor-core engine
+          // declines (too few items) runs on the bit-plane engine with the
+          // same 128-row tiles
+          T = hd::kTile;
+          cfg.tile = (int)hd::kTile;
+          if (!hd::tile_config_valid(cfg.tile, cfg.stages)) cfg.stages = 3;
+        }
       }
       const uint64_t *rows = remove_duplicates ? uniq.as<uint64_t>() : iota.as<uint64_t>();
       hd::pack_rows_and(ctx, all, rows + K, Kc - K, L, words, g0 + K * words);
@@ -1204,7 +1211,7 @@ int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, int64_
     hd::trace_begin(ctx, "hd_pairwise_lt");
     // the tensor-core engine's operand first, so that the timing below is the
     // distance kernel's alone
-    if (hd::mma_eligible(aln) && hd::ensure_fp8(ctx, aln, n, ctx->stream))
+    if (!aln->base && hd::mma_eligible(aln) && hd::ensure_fp8(ctx, aln, n, ctx->stream))
       hd::trace_mark(ctx, "FP8 operand");
     HD_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
     hd::pairwise_tiles(ctx, aln, dtype_bytes, md, d_out, 0, 0, nb);

@@ -64,6 +64,7 @@ constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 64 KB
 constexpr int kMmaSmem = kMmaStages * kStageBytes + 1024;
 constexpr uint32_t kTmemCols = 512;                   // row tile h at columns 256 h
 constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
+constexpr uint64_t kMmaMinItems = 48;                 // HAMMINGDIST_MMA_MIN_ITEMS overrides
 constexpr uint32_t kMmaBand = 16;  // tile rows per L2 band (HAMMINGDIST_MMA_BAND overrides)
 // operand bytes per 32-site word: P planes + the two dash blocks, 32 B each
 __host__ __device__ constexpr uint64_t row_bytes_per_word(uint32_t planes) {
@@ -464,13 +465,11 @@ bool mma_eligible(const hd_alignment *aln) {
     if (std::string(e) == "lop3") return false;
   // FP32 sums of up to 4 L are exact below 2^24
   // the AND rule (4 planes) or a sparse rule (5, 6 planes); FP32 sums of up
-  // to P L are exact below 2^24. A view qualifies when its base already holds
-  // an operand (the streamed from_fasta prepares one; a serving window should
-  // not expand a large base).
+  // to P L are exact below 2^24
   const uint64_t P = (uint64_t)aln->planes;
   const bool shape = (P == 4 && aln->groups == 1) || ((P == 5 || P == 6) && aln->groups == 2);
-  return shape && aln->row0 == 0 && (!aln->base || aln->base->fp8.p) && aln->length >= 1 &&
-         aln->length * P < (1ull << 24) && aln->n_rows >= 2 && aln->n_rows < (1ull << 31);
+  return shape && aln->length >= 1 && aln->length * P < (1ull << 24) && aln->n_rows >= 2 &&
+         aln->n_rows < (1ull << 31);
 }
 
 bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream,
@@ -531,15 +530,71 @@ double measure_mma_peak(hd_ctx *ctx) {
   return flop / (ms / 1e3);
 }
 
+// The FP8 operand rows of a job: the alignment's own cache (an alignment, or
+// a view at row 0 of a base whose cache already holds its rows: the streamed
+// from_fasta), else the view's rows expanded into a buffer the plan keeps
+// until the kernel has run (a serving window must not expand a large base).
+// False if there is no memory for it.
+bool operand_for(hd_ctx *ctx, const hd_alignment *a, cudaStream_t stream, PairLaunchPlan *plan,
+                 const uint8_t *&op) {
+  const hd_alignment *o = a->base ? a->base : a;
+  if (!a->base) {
+    if (!ensure_fp8(ctx, a, a->n_rows, stream)) return false;
+    op = a->fp8.as<uint8_t>();
+    return true;
+  }
+  if (a->row0 == 0 && o->fp8.p && o->fp8_rows >= a->n_rows) {
+    op = o->fp8.as<uint8_t>();
+    return true;
+  }
+  const uint32_t P = (uint32_t)o->planes;
+  const uint64_t rb = o->words * row_bytes_per_word(P), bytes = a->n_rows * rb;
+  if (bytes > (8ull << 30)) return false;  // the bit-plane engine needs no extra memory
+  DevBuf tmp;
+  try {
+    tmp = DevBuf(bytes, stream);
+  } catch (const Error &e) {
+    if (e.code != HD_ERR_OOM) throw;
+    cudaGetLastError();
+    return false;
+  }
+  const uint64_t total = a->n_rows * o->words;
+  const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
+  k_expand_fp8<<<(unsigned)grid, 256, 0, stream>>>(
+      static_cast<const uint4 *>(a->planes_ptr(0)),
+      P > 4 ? static_cast<const uint4 *>(a->planes_ptr(1)) : nullptr, P, o->words, 0, a->n_rows,
+      o->length, tmp.as<uint8_t>());
+  HD_LAUNCHED(ctx);
+  op = tmp.as<uint8_t>();
+  plan->blocks.push_back(std::move(tmp));
+  return true;
+}
+
 void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaStream_t stream,
                       PairLaunchPlan *plan, int sm_limit, std::vector<char> &taken) {
   taken.assign(specs.size(), 0);
+  std::vector<const uint8_t *> ops(specs.size(), nullptr);  // each job's operand rows
   struct Job {
     size_t k;
     uint32_t t_lo, t_hi;
     double cost;
   };
   std::vector<Job> js;
+  // A launch with few items leaves SMs idle: below kMmaMinItems single row
+  // tiles (128 x 256) in all, the bit-plane engine's finer tiles finish first
+  // (its rate is a third, but it fills the SMs); a batch of small matrices
+  // still goes here when together they are enough.
+  uint64_t min_items = kMmaMinItems;
+  if (const char *e = std::getenv("HAMMINGDIST_MMA_MIN_ITEMS")) min_items = (uint64_t)std::max(0, std::atoi(e));
+  uint64_t items_total = 0;
+  for (const PairJobSpec &sp : specs) {
+    if (!mma_eligible(sp.aln) || sp.tile_hi <= sp.tile_lo) continue;
+    const uint64_t edge = sp.cfg.tile > 0 ? (uint64_t)sp.cfg.tile : kTile;
+    const uint64_t lo = sp.tile_lo * edge / kTM;
+    const uint64_t hi = ceil_div(std::min<uint64_t>(sp.tile_hi * edge, sp.aln->n_rows), kTM);
+    for (uint64_t I = lo; I < hi; ++I) items_total += ((I + 1) * kTM - 2) / kTN + 1;
+  }
+  if (items_total < min_items) return;
   for (size_t k = 0; k < specs.size(); ++k) {
     const PairJobSpec &sp = specs[k];
     const hd_alignment *a = sp.aln;
@@ -548,7 +603,7 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     const uint64_t edge = sp.cfg.tile > 0 ? (uint64_t)sp.cfg.tile : kTile;
     const uint64_t row_lo = sp.tile_lo * edge, row_hi = std::min<uint64_t>(sp.tile_hi * edge, a->n_rows);
     if (row_lo % kTM || row_hi <= row_lo) continue;
-    if (!ensure_fp8(ctx, a, a->n_rows, stream)) continue;
+    if (!operand_for(ctx, a, stream, plan, ops[k])) continue;
     const uint32_t lo = (uint32_t)(row_lo / kTM), hi = (uint32_t)ceil_div(row_hi, kTM);
     js.push_back({k, lo, hi, (double)a->words * ((double)hi * hi - (double)lo * lo)});
     taken[k] = 1;
@@ -605,8 +660,8 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     const hd_alignment *a = sp.aln;
     const hd_alignment *o = a->base ? a->base : a;
     const uint64_t rb = o->words * row_bytes_per_word((uint32_t)o->planes);
-    make_tmap_u8(ctx, &tms[2 * q], o->fp8.p, rb, a->n_rows, kTN);
-    make_tmap_u8(ctx, &tms[2 * q + 1], o->fp8.p, rb, a->n_rows, kTM);
+    make_tmap_u8(ctx, &tms[2 * q], ops[js[q].k], rb, a->n_rows, kTN);
+    make_tmap_u8(ctx, &tms[2 * q + 1], ops[js[q].k], rb, a->n_rows, kTM);
     MmaJob &m = jobs[q];
     m.tm256 = d_tms + 2 * q;
     m.tm128 = d_tms + 2 * q + 1;

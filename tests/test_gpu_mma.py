@@ -14,6 +14,13 @@ from oracle import hd_oracle as o
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def _every_size(monkeypatch):
+    # small matrices too: by default a launch with few items takes the
+    # bit-plane engine (HAMMINGDIST_MMA_MIN_ITEMS)
+    monkeypatch.setenv("HAMMINGDIST_MMA_MIN_ITEMS", "0")
+
+
 @pytest.fixture(scope="module")
 def ctx():
     from hammingdist_gb300 import abi
@@ -106,3 +113,27 @@ def test_mma_sparse_rules(ctx, include_x, n, L):
         np.testing.assert_array_equal(got, want)
     np.testing.assert_array_equal(_both(ctx, aln)[0], want_lt)
     aln.free()
+
+
+@pytest.mark.parametrize("row0,n", [(0, 300), (1, 257), (127, 129), (128, 400), (300, 2)])
+def test_mma_views(ctx, row0, n):
+    # windows of a resident alignment (serving): the window's rows are
+    # expanded into an operand of their own, at any row offset
+    from hammingdist_gb300 import abi
+
+    rows, _, _ = synth.alignment(800, 2999, p=1e-3, seed=31, dash_max=60)
+    seqs = [r.tobytes() for r in rows]
+    base = ctx.alignment_from_sequences(seqs)
+    v = base.view(row0, n)
+    got, want = _both(ctx, v)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got, o.lt_dense(seqs[row0:row0 + n]))
+    v.free()
+    base.free()
+    # a sparse-rule base
+    sp = ctx.alignment_from_sequences(seqs, include_x=True, semantics=abi.SEM_CPU)
+    v = sp.view(row0, n)
+    got, want = _both(ctx, v, dtype=np.uint16, max_distance=65535)
+    np.testing.assert_array_equal(got, want)
+    v.free()
+    sp.free()

@@ -139,9 +139,11 @@ def test_multiline_and_crlf_records(tmp_path):
                                       o.from_fasta_dense(fa, remove_duplicates=dedup)[0])
 
 
-def test_launches_and_device_output(ctx):
+def test_launches_and_device_output(ctx, monkeypatch):
     import torch
 
+    # 200 rows: the tensor-core engine only when its item threshold is off
+    monkeypatch.setenv("HAMMINGDIST_MMA_MIN_ITEMS", "0")
     seqs = synth.random_strings(200, 300, b"ACGT-", seed=9)
     aln = ctx.alignment_from_sequences(seqs)
     n = aln.n_rows
