@@ -943,6 +943,10 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     DevBuf uniq, iota, d_lt;
     std::vector<uint64_t> seq;
     std::unique_ptr<hd_alignment> owner;
+    // each part's new records only, while that resolves them (else the full
+    // dedupe of the prefix, from then on)
+    hd::IncDedupe inc;
+    bool inc_ok = true;
     // waits for every stream the call uses before any of the above is freed
     struct Sync {
       hd_ctx *c;
@@ -1062,7 +1066,18 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         }
       }
       uint64_t Kc = all.n;
-      if (remove_duplicates) uniq = hd::dedupe(ctx, all, &Kc, seq);
+      const uint64_t *rows = iota.as<uint64_t>();
+      if (remove_duplicates) {
+        if (c == 0) inc.init(ctx, R_max);
+        if (inc_ok && inc.add(ctx, all, seq)) {
+          Kc = inc.n_unique;
+          rows = inc.unique_rec.as<uint64_t>();
+        } else {
+          inc_ok = false;
+          uniq = hd::dedupe(ctx, all, &Kc, seq);
+          rows = uniq.as<uint64_t>();
+        }
+      }
       if (Kc > R_max || Kc < K) fail(HD_ERR_CUDA, "streamed ingest: inconsistent row counts");
       if (c == 0) {
         cfg = hd::tile_config_for(ctx, Kc * (n / std::max<uint64_t>(B, 1)), L, dtype_bytes);
@@ -1079,7 +1094,6 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
           if (!hd::tile_config_valid(cfg.tile, cfg.stages)) cfg.stages = 3;
         }
       }
-      const uint64_t *rows = remove_duplicates ? uniq.as<uint64_t>() : iota.as<uint64_t>();
       hd::pack_rows_and(ctx, all, rows + K, Kc - K, L, words, g0 + K * words);
       // the new rows' FP8 operand, before the launches of any stream read it
       if (use_mma && Kc >= 2 && !hd::ensure_fp8(ctx, owner.get(), Kc, ctx->stream, R_max)) {

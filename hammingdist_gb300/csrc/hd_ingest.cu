@@ -611,6 +611,97 @@ DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<u
   return unique_rec;
 }
 
+// ------------------------------------------- incremental duplicate removal
+__global__ void k_iota(uint64_t *out, uint64_t start, uint64_t n) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = start + i;
+}
+__global__ void k_inc_flags(const uint64_t *dup, uint64_t r0, uint64_t m, uint32_t *flag) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < m) flag[i] = dup[r0 + i] == r0 + i ? 1u : 0u;
+}
+// new unique record r0 + i gets row k0 + uidx[i]
+__global__ void k_inc_number(const uint64_t *dup, const uint64_t *uidx, uint64_t r0, uint64_t m,
+                             uint64_t k0, uint64_t *rowid, uint64_t *unique_rec) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= m || dup[r0 + i] != r0 + i) return;
+  rowid[r0 + i] = k0 + uidx[i];
+  unique_rec[k0 + uidx[i]] = r0 + i;
+}
+// a new duplicate gets the row of its first occurrence (earlier, or new and
+// numbered by k_inc_number)
+__global__ void k_inc_link(const uint64_t *dup, uint64_t r0, uint64_t m, uint64_t *rowid) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < m && dup[r0 + i] != r0 + i) rowid[r0 + i] = rowid[dup[r0 + i]];
+}
+
+void IncDedupe::init(hd_ctx *ctx, uint64_t capacity) {
+  cudaStream_t st = ctx->stream;
+  cap = capacity ? capacity : 1;
+  T = 64;
+  while (T < 2 * cap) T <<= 1;
+  hash = DevBuf(cap * 8, st);
+  dup = DevBuf(cap * 8, st);
+  rowid = DevBuf(cap * 8, st);
+  unique_rec = DevBuf(cap * 8, st);
+  list = DevBuf(cap * 8, st);
+  next = DevBuf(cap * 8, st);
+  flag = DevBuf(cap * 4, st);
+  uidx = DevBuf(cap * 8, st);
+  keys = DevBuf(T * 8, st);
+  mins = DevBuf(T * 8, st);
+  cnt = DevBuf(16, st);
+  HD_CUDA(cudaMemsetAsync(keys.p, 0xff, T * 8, st));
+  HD_CUDA(cudaMemsetAsync(mins.p, 0xff, T * 8, st));
+  seen = 0;
+  n_unique = 0;
+}
+
+bool IncDedupe::add(hd_ctx *ctx, const Records &rec, std::vector<uint64_t> &seqidx) {
+  cudaStream_t st = ctx->stream;
+  const uint64_t r0 = seen, m = rec.n - seen;
+  if (rec.n < seen || rec.n > cap) return false;
+  if (m == 0) return true;
+  uint64_t *hp = hash.as<uint64_t>(), *lp = list.as<uint64_t>();
+  k_hash<<<grid_for(m * 32, 256), 256, 0, st>>>(rec.base, rec.bytes, rec.rec_start.as<uint64_t>() + r0,
+                                                rec.rec_len.as<uint64_t>() + r0, m, hp + r0);
+  HD_LAUNCHED(ctx);
+  k_iota<<<grid_for(m, 256), 256, 0, st>>>(lp, r0, m);
+  HD_LAUNCHED(ctx);
+  // earlier records hold the smaller indices: they stay each hash's minimum
+  k_tab_insert<<<grid_for(m, 256), 256, 0, st>>>(hp, lp, m, keys.as<unsigned long long>(),
+                                                 mins.as<unsigned long long>(), T - 1);
+  HD_LAUNCHED(ctx);
+  HD_CUDA(cudaMemsetAsync(cnt.p, 0, 16, st));
+  k_tab_verify<<<grid_for(m * 32, 256), 256, 0, st>>>(
+      rec.base, rec.bytes, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(), hp, lp, m,
+      keys.as<unsigned long long>(), mins.as<unsigned long long>(), T - 1, dup.as<uint64_t>(),
+      next.as<uint64_t>(), cnt.as<unsigned long long>());
+  HD_LAUNCHED(ctx);
+  k_inc_flags<<<grid_for(m, 256), 256, 0, st>>>(dup.as<uint64_t>(), r0, m, flag.as<uint32_t>());
+  HD_LAUNCHED(ctx);
+  scan_exclusive<uint32_t>(ctx, flag.as<uint32_t>(), uidx.as<uint64_t>(), m,
+                           cnt.as<uint64_t>() + 1);
+  uint64_t h[2] = {0, 0};  // unresolved records, new unique rows
+  HD_CUDA(cudaMemcpyAsync(h, cnt.p, 16, cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  // a new record unlike the first record of its hash: the full dedupe decides
+  if (h[0]) return false;
+  k_inc_number<<<grid_for(m, 256), 256, 0, st>>>(dup.as<uint64_t>(), uidx.as<uint64_t>(), r0, m,
+                                                 n_unique, rowid.as<uint64_t>(),
+                                                 unique_rec.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+  k_inc_link<<<grid_for(m, 256), 256, 0, st>>>(dup.as<uint64_t>(), r0, m, rowid.as<uint64_t>());
+  HD_LAUNCHED(ctx);
+  seqidx.resize(rec.n);
+  HD_CUDA(cudaMemcpyAsync(seqidx.data() + r0, rowid.as<uint64_t>() + r0, m * 8,
+                          cudaMemcpyDeviceToHost, st));
+  HD_CUDA(cudaStreamSynchronize(st));
+  n_unique += h[1];
+  seen = rec.n;
+  return true;
+}
+
 // -------------------------------------------------------------- consensus
 constexpr int kColRows = 128;
 

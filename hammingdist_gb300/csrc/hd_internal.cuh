@@ -360,6 +360,20 @@ Records records_from_offsets(hd_ctx *ctx, const uint8_t *d_bytes, const uint64_t
 // Deduplicates: returns the unique records (first-occurrence order) as a list
 // of record indices on the device and fills seqidx (host, n entries).
 DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<uint64_t> &seqidx);
+// Duplicate removal over a growing record set (the parts of a streamed
+// FASTA file): records [0, seen) are resolved, and add() hashes, inserts and
+// verifies only the records after them. Earlier records hold the smaller
+// indices, so they stay the first occurrences and their rows keep their
+// numbers; unique_rec lists the unique rows' records (n_unique of them) and
+// seqidx receives each new record's row. A new record unlike the first
+// record of its hash (a 64-bit collision), or more records than the
+// capacity, makes add() return false: the caller runs the full dedupe.
+struct IncDedupe {
+  DevBuf hash, dup, rowid, unique_rec, list, next, flag, uidx, keys, mins, cnt;
+  uint64_t cap = 0, T = 0, seen = 0, n_unique = 0;
+  void init(hd_ctx *ctx, uint64_t capacity);
+  bool add(hd_ctx *ctx, const Records &rec, std::vector<uint64_t> &seqidx);
+};
 // Sum over sites of the most frequent of A/C/G/T among the given rows.
 uint64_t consensus_matches(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows,
                            uint64_t n_rows);
