@@ -446,8 +446,8 @@ bool tile_config_valid(int tile, int stages);
 // tune.cu: the autotuned table (or the default) for (n, L, dtype)
 TileConfig tile_config_for(hd_ctx *ctx, uint64_t n_rows, uint64_t length, int dtype_bytes);
 
-// mma.cu: the tensor-core engine for the dense AND rule (4 planes, one
-// group, no row offset, L <= 4,000,000; HAMMINGDIST_KERNEL=lop3 turns it off).
+// mma.cu: the tensor-core engine for every rule (4, 5 or 6 planes, with
+// P L < 2^24; HAMMINGDIST_KERNEL=lop3 turns it off).
 bool mma_eligible(const hd_alignment *aln);
 // expands rows [fp8_rows, rows) of the alignment's planes into its FP8
 // operand on `stream` (room for cap_hint rows if it must grow); false if the

@@ -1,30 +1,36 @@
-// Tensor-core lower-triangle distances for the dense AND rule (tcgen05, FP8).
+// Tensor-core lower-triangle distances (tcgen05, FP8) for the dense AND rule
+// and the sparse rules.
 //
-// Replaces the reference's Dist<T> kernel (src/distance_cuda.cu:9-202) for
-// the rule it implements: a site pair matches when the two 4-bit codes share
-// a bit (src/distance_cuda.cu:57-65; codes of src/hamming_impl.cc:23-44:
-// A, C, G, T one-hot, '-' all four bits, every other byte 0).
+// Replaces the reference's Dist<T> kernel (src/distance_cuda.cu:9-202) and,
+// for use_gpu=False, its CPU loops (include/hamming/hamming_impl.hh:120-175).
+// A site pair matches when the two codes share a bit: the dense rule's
+// 4-bit codes (src/distance_cuda.cu:57-65; src/hamming_impl.cc:23-44: A, C,
+// G, T one-hot, '-' all four bits, every other byte 0) or the sparse rules'
+// one-hot classes over P = 5 or 6 planes with '-' as all P bits
+// (src/hamming_impl.cc:93-129).
 //
-// For those codes the match indicator is a bilinear form. With e(x) the
-// code's 4 plane bits and d(x) = [x = '-'],
-//   match(a, b) = <e(a), e(b)> - 3 d(a) d(b):
-// the plane dot product is 1 for equal bases and for a base against '-', 4
-// for '-' against '-' (hence the -3), and 0 otherwise. Summed over the sites
-// of two rows this is one dot product of 5 values per site, the dash value
-// being 1 on the row side and -3 on the column side. All values are 0, 1 or
-// -3: exact in FP8 (E4M3: 1.0 = 0x38, -3.0 = 0xC4) with FP32 accumulation
-// while 4 L < 2^24. mismatches = L - matches.
+// For those codes the match indicator is a bilinear form. With e(x) the P
+// plane bits of x and d(x) = [x = '-'],
+//   match(a, b) = <e(a), e(b)> - (P - 1) d(a) d(b):
+// the plane dot product is 1 for equal symbols and for a symbol against '-',
+// P for '-' against '-' (hence the -(P - 1)), and 0 otherwise. Summed over
+// the sites of two rows this is one dot product of P + 1 values per site, the
+// dash value being 1 on the row side and -(P - 1) on the column side. All
+// values are 0, 1, -3, -4 or -5: exact in FP8 (E4M3) with FP32 accumulation
+// while P L < 2^24. mismatches = L - matches.
 //
 // Operand (one buffer serves rows and columns): each row's bit planes are
-// expanded to 192 bytes per 32-site word, K-major: for every 128 sites, six
-// 128-byte blocks, the four planes, the dash as 1 (read for rows) and the dash
-// as -3 (read for columns); sites past L are 0.
+// expanded to (P + 2) x 32 bytes per 32-site word, K-major: for every 128
+// sites, P + 2 blocks of 128 bytes, the P planes, the dash as 1 (read for
+// rows) and the dash as -(P - 1) (read for columns); sites past L are 0. An
+// alignment caches its operand; a view of a resident alignment (a serving
+// window) gets one of its own rows.
 //
-// Persistent CTAs (192 threads, one per SM) walk a list of items: 256 columns
-// J x one or two 128-row tiles I (rows [128 I, 128 I + 128 k)), in bands of
-// 16 tile rows, column-major within a band, so resident CTAs share operands
-// in L2; the list ends with single-row-tile items so that every CTA gets the
-// same work to within a row tile.
+// One launch serves a job table of matrices. Persistent CTAs (192 threads,
+// one per SM) walk a list of items: 256 columns J x one or two 128-row tiles
+// I of one job, in bands of 16 tile rows, column-major within a band, so
+// resident CTAs share operands in L2; the list ends with single-row-tile items
+// so that every CTA gets the same work to within a row tile.
 //  * warp 0 (one thread) issues TMA loads (128-byte swizzle) per stage of
 //    one 128-byte K block of the item's 128 or 256 rows and 256 columns,
 //    3 stages of 64 KB with full/empty mbarriers; warp 0 also allocates and
@@ -37,9 +43,9 @@
 //  * warps 2-5 read their 32 rows of each accumulator (tcgen05.ld), form
 //    min(L - matches, max_dist) (safe_int_cast,
 //    include/hamming/hamming_impl.hh:37-45) and store each row's part of the
-//    lower triangle in the output dtype from registers; they then release
-//    the accumulators (`tmem_free`) for the MMAs of the next item, whose
-//    first stages the producer has already loaded.
+//    lower triangle in the job's dtype from registers; they then release the
+//    accumulators (`tmem_free`) for the MMAs of the next item, whose first
+//    stages the producer has already loaded.
 // Every wait is bounded; on a timeout the CTA records it in the status word,
 // waits (bounded) for its own copies and MMAs, frees its TMEM and returns.
 #include <algorithm>
@@ -463,7 +469,6 @@ void make_tmap_u8(hd_ctx *ctx, CUtensorMap *tm, const void *base, uint64_t row_b
 bool mma_eligible(const hd_alignment *aln) {
   if (const char *e = std::getenv("HAMMINGDIST_KERNEL"))
     if (std::string(e) == "lop3") return false;
-  // FP32 sums of up to 4 L are exact below 2^24
   // the AND rule (4 planes) or a sparse rule (5, 6 planes); FP32 sums of up
   // to P L are exact below 2^24
   const uint64_t P = (uint64_t)aln->planes;
