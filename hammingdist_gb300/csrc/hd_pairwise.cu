@@ -1,9 +1,13 @@
-// The pairwise lower-triangle distance engine.
+// The bit-plane pairwise lower-triangle engine, and the job planner both
+// engines share.
 //
 // Replaces the reference's Dist<T> kernel and its chunked driver
 // (src/distance_cuda.cu:9-202), which computes one lower-triangle entry per
 // CTA from the nibble-packed rows with a shared-memory reduction and re-reads
-// both rows from memory for every pair.
+// both rows from memory for every pair. prepare_pairwise_jobs first gives
+// the tensor-core engine (hd_mma.cu) every job it can take; this engine
+// computes the rest: launches too small to fill the SMs with the tensor-core
+// engine's coarser items, and rows too long for its FP32 sums.
 //
 // One persistent kernel serves a single matrix and a batch of independent
 // matrices alike: CTAs draw tiles from a device counter over a table of jobs
