@@ -947,6 +947,8 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     // dedupe of the prefix, from then on)
     hd::IncDedupe inc;
     bool inc_ok = true;
+    if (const char *e = std::getenv("HAMMINGDIST_STREAM_DEDUPE"))  // "full": the full path only
+      inc_ok = std::string(e) != "full";
     // waits for every stream the call uses before any of the above is freed
     struct Sync {
       hd_ctx *c;

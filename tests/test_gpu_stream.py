@@ -252,3 +252,22 @@ def test_module_first_lt_array_is_a_fresh_copy(big):
     c = np.asarray(ds.lt_array)
     np.testing.assert_array_equal(b, c)
     assert ds[1, 0] == int(b[0])
+
+
+@pytest.mark.parametrize("splits", ["0.2,0.5", "0.25,0.5,0.75"])
+def test_incremental_and_full_dedupe_agree(ctx, big, monkeypatch, splits):
+    # each part's new records only (the default), and the full dedupe of the
+    # prefix that a hash collision falls back to (HAMMINGDIST_STREAM_DEDUPE=full)
+    path, fa, rows = big
+    monkeypatch.setenv("HAMMINGDIST_STREAM_SPLITS", splits)
+    got = {}
+    for mode in ("", "full"):
+        monkeypatch.setenv("HAMMINGDIST_STREAM_DEDUPE", mode)
+        _touch(path)
+        lt, aln = ctx.pairwise_lt_fasta_file(path, remove_duplicates=True)
+        got[mode] = (lt, aln.sequence_indices())
+        aln.free()
+    want, want_idx = _plain(ctx, path, np.uint8, 255, True)
+    for lt, idx in got.values():
+        np.testing.assert_array_equal(lt, want)
+        np.testing.assert_array_equal(idx, want_idx)
