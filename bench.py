@@ -84,6 +84,26 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_elapsed(elapsed, ws, device):
+    """Replicas: every rank timed its own steps; the job's time is the max
+    over ranks (all_reduce MAX on `device`: cuda under NCCL, cpu under gloo),
+    followed by a barrier."""
+    if ws <= 1:
+        return elapsed
+    import torch
+
+    t = torch.tensor([elapsed], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
+def replica_value(units_per_rank, ws, elapsed):
+    """Whole-job throughput: every rank processed the same units (weak
+    scaling), in the max time over ranks."""
+    return ws * units_per_rank / elapsed
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -299,14 +319,9 @@ def run_ours(args):
         torch.cuda.synchronize()
         clk = clocks.stop()
         launches = ctx.kernel_launches - launches0
-        elapsed = ev0.elapsed_time(ev1) / 1e3
-        if ws > 1:
-            t = torch.tensor([elapsed], device=f"cuda:{local}")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            elapsed = float(t.item())
-            torch.distributed.barrier()
+        elapsed = replica_elapsed(ev0.elapsed_time(ev1) / 1e3, ws, f"cuda:{local}")
         ms_step = elapsed / args.steps * 1e3
-        value = ws * pairs * L * args.steps / elapsed / 1e9
+        value = replica_value(pairs * L * args.steps, ws, elapsed) / 1e9
 
         # parity on the final step's device results: sampled rows vs the oracle
         from oracle import hd_oracle as o
