@@ -40,10 +40,11 @@
 //    h of the item at columns 256 h), so each column stage feeds up to eight
 //    MMAs; each stage's MMAs are committed to its empty barrier, an item's
 //    last ones to the `done` barrier;
-//  * warps 2-5 read their 32 rows of each accumulator (tcgen05.ld), form
-//    min(L - matches, max_dist) (safe_int_cast,
-//    include/hamming/hamming_impl.hh:37-45) and store each row's part of the
-//    lower triangle in the job's dtype from registers; they then release the
+//  * warps 2-5 read their 32 rows of each accumulator (tcgen05.ld) 32
+//    columns at a time, form min(L - matches, max_dist) (safe_int_cast,
+//    include/hamming/hamming_impl.hh:37-45), turn each 32 x 32 chunk around
+//    in a padded shared buffer and store it row by row, 32 consecutive
+//    entries of the job's dtype per store; they then release the
 //    accumulators (`tmem_free`) for the MMAs of the next item, whose first
 //    stages the producer has already loaded.
 // Every wait is bounded; on a timeout the CTA records it in the status word,
@@ -67,7 +68,9 @@ constexpr uint32_t kHalfBytes = kTM * 128;            // one 128-byte K block of
 constexpr uint32_t kABytes = 2 * kHalfBytes;          // up to two row tiles
 constexpr uint32_t kBBytes = kTN * 128;
 constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 64 KB
-constexpr int kMmaSmem = kMmaStages * kStageBytes + 1024;
+constexpr uint32_t kEpiPitch = 33;                    // words per row of an epilogue chunk
+constexpr uint32_t kEpiBytes = 4 * 32 * kEpiPitch * 4;  // 32 x 32 words per epilogue warp
+constexpr int kMmaSmem = kMmaStages * kStageBytes + kEpiBytes + 1024;
 constexpr uint32_t kTmemCols = 512;                   // row tile h at columns 256 h
 constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
 constexpr uint64_t kMmaMinItems = 48;                 // HAMMINGDIST_MMA_MIN_ITEMS overrides
@@ -214,18 +217,10 @@ __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// min(sites - matches, max_dist) of up to 32 accumulator columns (FP32
-// integers) into dst[0 .. ncols)
+// one entry of a lower-triangle row segment in the job's dtype
 template <typename T>
-__device__ __forceinline__ void store_row(T *dst, const uint32_t (&d)[32], uint32_t ncols,
-                                          uint32_t sites, uint32_t max_dist) {
-#pragma unroll
-  for (uint32_t j = 0; j < 32; ++j) {
-    if (j < ncols) {
-      const uint32_t mism = sites - (uint32_t)__uint_as_float(d[j]);
-      dst[j] = (T)(mism < max_dist ? mism : max_dist);
-    }
-  }
+__device__ __forceinline__ void store_entry(void *out, unsigned long long e, uint32_t v) {
+  static_cast<T *>(out)[e] = (T)v;
 }
 
 __global__ void __launch_bounds__(kMmaThreads, 1)
@@ -346,9 +341,14 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     }
   } else {
     // epilogue warps 2-5: warp w reads TMEM lanes 32 (w % 4) .. + 31, which
-    // are rows 32 (w % 4) + lane of each row tile of the item
+    // are rows 32 (w % 4) + lane of each row tile of the item. Each 32 x 32
+    // chunk goes through the warp's padded shared buffer (row r at words
+    // 33 r: conflict-free both ways), so that one store instruction writes
+    // 32 consecutive entries of one row rather than one entry of 32 rows.
     const uint32_t sub = warp & 3u;
     const uint32_t t_lane = tmem + ((sub * 32) << 16);
+    uint32_t *buf = reinterpret_cast<uint32_t *>(smem + kMmaStages * kStageBytes) +
+                    sub * 32 * kEpiPitch;
     uint32_t it = 0;
     for (uint32_t t = blockIdx.x; t < n_items; t += gridDim.x, ++it) {
       const bool got = mbar_wait_bounded(&done, it & 1u, 4 * kMmaWaitNs);
@@ -363,24 +363,42 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       const MmaJob &job = jobs[tl.job];
       const uint32_t n = job.n, sites = job.sites, max_dist = job.max_dist, dtype = job.dtype;
       for (uint32_t h = 0; h < tl.halves; ++h) {
-        const uint32_t i = (tl.I + h) * kTM + sub * 32 + lane;  // output row
+        const uint32_t i0 = (tl.I + h) * kTM + sub * 32;  // output row of lane 0
+        if (i0 >= n) continue;                           // warp-uniform
+        const uint32_t rows = n - i0 < 32u ? n - i0 : 32u;
 #pragma unroll 1
         for (uint32_t c = 0; c < (uint32_t)kTN; c += 32) {
+          const uint32_t j0 = tl.J * kTN + c;  // first column of this chunk
+          if (j0 + 1 >= i0 + rows) break;      // no row reaches column j0 (warp-uniform)
           uint32_t d[32];
           __syncwarp();
           tmem_ld32(t_lane + 256u * h + c, d);
           tmem_ld_wait();
-          const uint32_t j0 = tl.J * kTN + c;  // first column of this chunk
-          if (i < n && j0 < i) {
-            const uint32_t ncols = i - j0 < 32u ? i - j0 : 32u;
-            const unsigned long long e0 = (unsigned long long)i * (i - 1) / 2 + j0 - job.out_base;
-            if (dtype == 1)
-              store_row<uint8_t>(static_cast<uint8_t *>(job.out) + e0, d, ncols, sites, max_dist);
-            else if (dtype == 2)
-              store_row<uint16_t>(static_cast<uint16_t *>(job.out) + e0, d, ncols, sites, max_dist);
-            else
-              store_row<uint32_t>(static_cast<uint32_t *>(job.out) + e0, d, ncols, sites, max_dist);
+          // min(sites - matches, max_dist) (FP32 integers)
+#pragma unroll
+          for (uint32_t j = 0; j < 32; ++j) {
+            const uint32_t mism = sites - (uint32_t)__uint_as_float(d[j]);
+            buf[lane * kEpiPitch + j] = mism < max_dist ? mism : max_dist;
           }
+          __syncwarp();
+          // row i = i0 + r holds entries tri(i) + j0 .. + min(i - j0, 32) - 1
+          unsigned long long e =
+              (unsigned long long)i0 * (i0 - 1) / 2 + j0 - job.out_base + lane;
+#pragma unroll 1
+          for (uint32_t r = 0; r < rows; ++r) {
+            const uint32_t i = i0 + r;
+            if (j0 < i && lane < i - j0) {
+              const uint32_t v = buf[r * kEpiPitch + lane];
+              if (dtype == 1)
+                store_entry<uint8_t>(job.out, e, v);
+              else if (dtype == 2)
+                store_entry<uint16_t>(job.out, e, v);
+              else
+                store_entry<uint32_t>(job.out, e, v);
+            }
+            e += i;
+          }
+          __syncwarp();  // the buffer is rewritten by the next chunk
         }
       }
       // the accumulators may be overwritten
