@@ -506,17 +506,25 @@ hd_alignment *build_alignment(hd_ctx *ctx, hd::Records &rec, int remove_duplicat
 }
 
 // ---------------------------------------------------------------- file out
+// Text output files, (re)created as the reference's writers do, written in
+// order with write(). (A shared mapping of the file copied by 8 threads took
+// 2.82 s for the 10 GB text of n=100,000 on ext4 with 64 KB pages, against
+// 1.69 s for write(): page faults on the mapping cost more than one thread's
+// copy saves.)
 struct OutFile {
   int fd = -1;
   std::string path;
-  OutFile(const char *p, bool truncate) : path(p) {
-    fd = ::open(p, O_WRONLY | O_CREAT | (truncate ? O_TRUNC : O_APPEND), 0644);
+  explicit OutFile(const char *p) : path(p) {
+    fd = ::open(p, O_WRONLY | O_CREAT | O_TRUNC, 0644);
     if (fd < 0) fail(HD_ERR_IO, "Error: Failed to open file '" + path + "'");
   }
   void write(const char *buf, uint64_t n) {
     while (n) {
-      ssize_t w = ::write(fd, buf, n > (1ull << 30) ? (1ull << 30) : n);
-      if (w < 0) fail(HD_ERR_IO, "Error: Failed to write file '" + path + "'");
+      const ssize_t w = ::write(fd, buf, n > (1ull << 30) ? (1ull << 30) : n);
+      if (w < 0) {
+        if (errno == EINTR) continue;
+        fail(HD_ERR_IO, "Error: Failed to write file '" + path + "'");
+      }
       buf += w;
       n -= (uint64_t)w;
     }
@@ -583,7 +591,7 @@ void stream_lt_text(hd_ctx *ctx, uint64_t n, int dtype_bytes, const char *path, 
   }
   DevBuf d_lt((max_e + 1) * dtype_bytes, ctx->stream), d_text(max_text + 16, ctx->stream);
   PinnedPair pin(max_text + 16);
-  OutFile f(path, true);
+  OutFile f(path);
   uint64_t pending_bytes = 0;
   int pending = -1;
   for (size_t k = 0; k < chunks.size(); ++k) {
@@ -902,20 +910,20 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       }
     };
     // The file is ingested in parts that end at the first record headers
-    // after the given fractions of its bytes. After each part the whole prefix is
-    // deduplicated (first occurrences keep their order, so earlier unique
-    // rows keep their positions) and the new unique rows are packed; the tile
-    // rows that are complete then run on the side stream, with 16 SMs left
-    // for the next part's ingest. The last part's tile rows run as two
-    // launches on two streams (the second fills the first's tail), split at
-    // 90% of the rows, so that the copy of every finished range to the host
-    // overlaps the rest of the distances.
+    // after the given fractions of its bytes. After each part its new records
+    // are deduplicated against the earlier ones (first occurrences keep their
+    // order, so earlier unique rows keep their positions) and the new unique
+    // rows are packed; the tile rows that are complete then run on the side
+    // stream, with 16 SMs left for the next part's ingest. The last part's
+    // tile rows run as two launches on two streams (the second fills the
+    // first's tail), split at 90% of the rows, so that the copy of every
+    // finished range to the host overlaps the rest of the distances.
     // part ends as fractions of the file (HAMMINGDIST_STREAM_SPLITS="f1,f2,...",
-    // increasing, at most 3). At n=20,000 x L=29,903 splits at 20% and 50%
-    // and a single split at 50% are within noise of each other (the former
-    // steadier: 17.9-18.0 against 18.0-18.8 ms per bench step); no split takes
-    // 16.1 ms for the call against 14.2-14.5.
-    std::vector<double> ends = {0.2, 0.5};
+    // increasing, at most 3). At n=20,000 x L=29,903 the bench step took
+    // 15.92-15.98 ms with splits at 10%, 30% and 60%, 16.2-16.5 at 20% and
+    // 50%, and 16.5-17.9 at the other three-split settings tried; a small
+    // first part shortens the ingest that nothing overlaps.
+    std::vector<double> ends = {0.1, 0.3, 0.6};
     if (const char *e = std::getenv("HAMMINGDIST_STREAM_SPLITS")) {
       ends.clear();
       for (const char *q = e; *q && ends.size() < 3;) {
@@ -1225,12 +1233,15 @@ int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, int64_
     }
     const uint32_t nb = (uint32_t)hd::ceil_div(n, hd::kTile);
     hd::trace_begin(ctx, "hd_pairwise_lt");
-    // the tensor-core engine's operand first, so that the timing below is the
+    // the tensor-core engine's operand and the launch plan (item lists,
+    // tensor maps, job tables) first, so that the timing below is the
     // distance kernel's alone
     if (!aln->base && hd::mma_eligible(aln) && hd::ensure_fp8(ctx, aln, n, ctx->stream))
       hd::trace_mark(ctx, "FP8 operand");
+    hd::PairLaunchPlan plan;
+    hd::plan_pairwise_tiles(ctx, aln, dtype_bytes, md, d_out, 0, 0, nb, &plan);
     HD_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
-    hd::pairwise_tiles(ctx, aln, dtype_bytes, md, d_out, 0, 0, nb);
+    hd::launch_pairwise_plan(ctx, plan, ctx->stream);
     HD_CUDA(cudaEventRecord(ctx->ev_stop, ctx->stream));
     hd::trace_mark(ctx, "pairwise");
     if (!out_on_device) {
@@ -1267,7 +1278,7 @@ int hd_write_full_matrix(hd_ctx *ctx, const void *lt, uint64_t entries, uint64_t
   if (!ctx || !path || (!lt && entries)) return HD_ERR_ARG;
   return guard(ctx, [&] {
     check_dtype(dtype_bytes);
-    OutFile f(path, true);
+    OutFile f(path);
     if (!nsamples) return;
     DevBuf d_lt((entries ? entries : 1) * dtype_bytes, ctx->stream);
     if (entries)
@@ -1370,7 +1381,7 @@ int hd_write_sparse(hd_ctx *ctx, const void *lt, uint64_t nsamples, int dtype_by
   if (!ctx || !path || (!lt && nsamples > 1)) return HD_ERR_ARG;
   return guard(ctx, [&] {
     check_dtype(dtype_bytes);
-    OutFile f(path, true);  // the reference always (re)creates the file
+    OutFile f(path);  // the reference always (re)creates the file
     uint64_t lines_total = 0;
     if (nsamples >= 2) {
       // bytes per line <= 2 * digits(n) + digits(dtype max) + 3

@@ -437,6 +437,11 @@ void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStr
                            PairLaunchPlan *plan,
                            int sm_limit = 0);
 void launch_pairwise_plan(hd_ctx *ctx, PairLaunchPlan &plan, cudaStream_t stream);
+// pairwise_tiles in two steps: the plan (host work and the job-table upload
+// on ctx->stream), then launch_pairwise_plan on ctx->stream
+void plan_pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
+                         void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi,
+                         PairLaunchPlan *plan);
 void run_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStream_t stream,
                        PairLaunchPlan *keep);
 void make_tmap(hd_ctx *ctx, CUtensorMap *tm, const void *base, uint64_t words, uint64_t rows,

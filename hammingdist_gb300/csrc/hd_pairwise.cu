@@ -471,13 +471,10 @@ void run_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStream_
   if (keep) *keep = std::move(plan);
 }
 
-void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
-                    void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi) {
+void plan_pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
+                         void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi,
+                         PairLaunchPlan *plan) {
   if (aln->n_rows < 2 || tile_hi <= tile_lo) return;
-  // the dense AND rule runs on the tensor cores (hd_mma.cu)
-  if (pairwise_mma(ctx, aln, dtype_bytes, max_dist, d_out, out_base, tile_lo, tile_hi, ctx->stream,
-                   0))
-    return;
   std::vector<PairJobSpec> specs(1);
   PairJobSpec &s = specs[0];
   s.aln = aln;
@@ -491,7 +488,17 @@ void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint3
   const uint32_t nb = (uint32_t)ceil_div(aln->n_rows, s.cfg.tile);
   s.tile_lo = tile_lo * scale;
   s.tile_hi = std::min(tile_hi * scale, nb);
-  run_pairwise_jobs(ctx, specs, ctx->stream, nullptr);
+  // the dense AND rule and the sparse rules go to the tensor cores
+  // (hd_mma.cu) when the launch has enough items for them
+  prepare_pairwise_jobs(ctx, specs, ctx->stream, plan);
+}
+
+void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
+                    void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi) {
+  PairLaunchPlan plan;
+  plan_pairwise_tiles(ctx, aln, dtype_bytes, max_dist, d_out, out_base, tile_lo, tile_hi, &plan);
+  // the plan's job tables are released in stream order, after the kernels
+  launch_pairwise_plan(ctx, plan, ctx->stream);
 }
 
 }  // namespace hd

@@ -1,6 +1,7 @@
 """from_fasta with the distances overlapping the read (hd_pairwise_lt_fasta_file):
 for files of 64 MB or more the file is ingested in parts (by default split
-after ~20% and ~50% of its bytes; HAMMINGDIST_STREAM_SPLITS sets up to three),
+after ~10%, ~30% and ~60% of its bytes; HAMMINGDIST_STREAM_SPLITS sets up to
+three),
 and each part's complete tile rows run while the rest is read. Every result
 must equal the plain order (read, ingest, distances) bit for bit: duplicates
 that cross the parts, dtypes, max_distance, no dedupe, every split setting,
@@ -145,9 +146,10 @@ def test_module_from_fasta_uses_it(big):
 
 @pytest.mark.parametrize("where", [0.35, 0.8])
 def test_multiline_record_in_a_later_part(ctx, tmp_path, where):
-    # the file is ingested in parts that end after 20% and 50% of its bytes:
-    # one multi-line record in the second or third part, found after earlier
-    # parts' distances have started, still gives the plain order's results
+    # the file is ingested in parts that end after 10%, 30% and 60% of its
+    # bytes: one multi-line record in the third or fourth part, found after
+    # earlier parts' distances have started, still gives the plain order's
+    # results
     rows, _, _ = synth.alignment(2500, 29903, p=1e-3, seed=43, dup_frac=0.2)
     k0 = int(where * len(rows))
     out = bytearray()
@@ -168,7 +170,8 @@ def test_multiline_record_in_a_later_part(ctx, tmp_path, where):
 
 @pytest.mark.parametrize("where", [0.35, 0.7])
 def test_error_in_a_part(ctx, tmp_path, big, where):
-    # a short record in the second or the third part (default splits at 20%, 50%)
+    # a short record in the third or the fourth part (default splits at 10%,
+    # 30% and 60%)
     from hammingdist_gb300 import abi
 
     path, fa, rows = big
@@ -186,8 +189,8 @@ def test_error_in_a_part(ctx, tmp_path, big, where):
 
 @pytest.mark.parametrize("splits", ["", "0.5", "0.2,0.5", "0.25,0.5,0.75", "0.9"])
 def test_every_split_setting(ctx, big, monkeypatch, splits):
-    # no split (one part), one, two (the default) and three splits: the same
-    # matrix and sequence indices as the plain order
+    # no split (one part), one, two and three splits (the default is three:
+    # 10%, 30%, 60%): the same matrix and sequence indices as the plain order
     path, fa, rows = big
     monkeypatch.setenv("HAMMINGDIST_STREAM_SPLITS", splits)
     _touch(path)
