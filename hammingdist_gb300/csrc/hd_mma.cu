@@ -26,7 +26,7 @@
 // alignment caches its operand; a view of a resident alignment (a serving
 // window) gets one of its own rows.
 //
-// One launch serves a job table of matrices. Persistent CTAs (192 threads,
+// One launch serves a job table of matrices. Persistent CTAs (320 threads,
 // one per SM) walk a list of items: 256 columns J x one or two 128-row tiles
 // I of one job, in bands of 16 tile rows, column-major within a band, so
 // resident CTAs share operands in L2; the list ends with single-row-tile items
@@ -40,13 +40,15 @@
 //    h of the item at columns 256 h), so each column stage feeds up to eight
 //    MMAs; each stage's MMAs are committed to its empty barrier, an item's
 //    last ones to the `done` barrier;
-//  * warps 2-5 read their 32 rows of each accumulator (tcgen05.ld) 32
-//    columns at a time, form min(L - matches, max_dist) (safe_int_cast,
+//  * warps 2-9, two per TMEM lane quarter, each read 32 rows x 128 columns
+//    of each accumulator (tcgen05.ld, 64 columns at a time), form
+//    min(L - matches, max_dist) (safe_int_cast,
 //    include/hamming/hamming_impl.hh:37-45), turn each 32 x 32 chunk around
 //    in a padded shared buffer and store it row by row, 32 consecutive
 //    entries of the job's dtype per store; they then release the
 //    accumulators (`tmem_free`) for the MMAs of the next item, whose first
-//    stages the producer has already loaded.
+//    stages the producer has already loaded. The MMAs wait for this, so the
+//    epilogue's length is paid once per item.
 // Every wait is bounded; on a timeout the CTA records it in the status word,
 // waits (bounded) for its own copies and MMAs, frees its TMEM and returns.
 #include <algorithm>
@@ -60,16 +62,18 @@
 namespace hd {
 namespace {
 
-constexpr int kMmaThreads = 192;   // warp 0: TMA, warp 1: MMA, warps 2-5: epilogue
-constexpr int kEpiThreads = 128;
+constexpr int kEpiWarps = 8;      // two per TMEM lane quarter, one per 128 columns
+constexpr int kMmaThreads = 64 + 32 * kEpiWarps;  // warp 0: TMA, warp 1: MMA, warps 2-9: epilogue
+constexpr int kEpiThreads = 32 * kEpiWarps;
 constexpr int kMmaStages = 3;
 constexpr int kTM = 128, kTN = 256;                   // MMA tile: rows x columns
+constexpr uint32_t kEpiCols = kTN / (kEpiWarps / 4);  // accumulator columns per epilogue warp
 constexpr uint32_t kHalfBytes = kTM * 128;            // one 128-byte K block of 128 rows
 constexpr uint32_t kABytes = 2 * kHalfBytes;          // up to two row tiles
 constexpr uint32_t kBBytes = kTN * 128;
 constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 64 KB
 constexpr uint32_t kEpiPitch = 33;                    // words per row of an epilogue chunk
-constexpr uint32_t kEpiBytes = 4 * 32 * kEpiPitch * 4;  // 32 x 32 words per epilogue warp
+constexpr uint32_t kEpiBytes = kEpiWarps * 32 * kEpiPitch * 4;  // 32 x 32 words per epilogue warp
 constexpr int kMmaSmem = kMmaStages * kStageBytes + kEpiBytes + 1024;
 constexpr uint32_t kTmemCols = 512;                   // row tile h at columns 256 h
 constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
@@ -199,17 +203,26 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// 32 lanes x 32 consecutive 32-bit columns: thread t gets row (lane base + t)
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+// 32 lanes x 64 consecutive 32-bit columns: thread t gets row (lane base + t)
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&v)[64]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
-      "%30, %31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x64.b32 {"
+      "%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, "
+      "%19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33, %34, %35, "
+      "%36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, "
+      "%53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63 "
+      "}, [%64];"
       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
         "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
         "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
         "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
-        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31]),
+        "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]),
+        "=r"(v[38]), "=r"(v[39]), "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]),
+        "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]), "=r"(v[48]), "=r"(v[49]),
+        "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]),
+        "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]),
+        "=r"(v[62]), "=r"(v[63])
       : "r"(taddr)
       : "memory");
 }
@@ -217,10 +230,66 @@ __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// one entry of a lower-triangle row segment in the job's dtype
+// min(sites - matches, max_dist) of accumulator columns OFF .. OFF + 31
+// (FP32 integers) into the warp's buffer, row `lane` at words 33 lane
+template <int OFF>
+__device__ __forceinline__ void turn_chunk(uint32_t *buf, const uint32_t (&d)[64], uint32_t sites,
+                                           uint32_t max_dist, uint32_t lane) {
+#pragma unroll
+  for (uint32_t j = 0; j < 32; ++j) {
+    const uint32_t mism = sites - (uint32_t)__uint_as_float(d[OFF + j]);
+    buf[lane * kEpiPitch + j] = mism < max_dist ? mism : max_dist;
+  }
+}
+
+// The buffered chunk of rows i0 .. i0 + rows - 1, columns j0 .. j0 + 31, row
+// by row: lane l stores column j0 + l of row i0 + r, lower-triangle entry
+// tri(i0 + r) + j0 + l = e0 + r i0 + r (r - 1) / 2, where it is below the
+// diagonal (j0 + l < i0 + r). The row loop is unrolled so that several rows'
+// loads and stores are in flight.
 template <typename T>
-__device__ __forceinline__ void store_entry(void *out, unsigned long long e, uint32_t v) {
-  static_cast<T *>(out)[e] = (T)v;
+__device__ __forceinline__ void store_chunk(T *out, unsigned long long e0, uint32_t i0,
+                                            uint32_t rows, uint32_t j0, const uint32_t *buf,
+                                            uint32_t lane) {
+#pragma unroll 8
+  for (uint32_t r = 0; r < 32; ++r)
+    if (r < rows && j0 + lane < i0 + r)
+      out[e0 + (unsigned long long)r * i0 + r * (r - 1) / 2] = (T)buf[r * kEpiPitch + lane];
+}
+
+// One epilogue warp's share of an item: TMEM lanes of its quarter (rows
+// 32 sub + lane of each row tile) x its columns [c_lo, c_lo + kEpiCols),
+// read 64 columns at a time.
+template <typename T>
+__device__ __forceinline__ void epilogue_share(const MmaItem &tl, const MmaJob &job,
+                                               uint32_t t_lane, uint32_t c_lo, uint32_t sub,
+                                               uint32_t lane, uint32_t *buf) {
+  const uint32_t n = job.n, sites = job.sites, max_dist = job.max_dist;
+  T *out = static_cast<T *>(job.out);
+  for (uint32_t h = 0; h < tl.halves; ++h) {
+    const uint32_t i0 = (tl.I + h) * kTM + sub * 32;  // output row of lane 0
+    if (i0 >= n) continue;                           // warp-uniform
+    const uint32_t rows = n - i0 < 32u ? n - i0 : 32u;
+    const unsigned long long t0 = (unsigned long long)i0 * (i0 - 1) / 2 - job.out_base + lane;
+#pragma unroll 1
+    for (uint32_t c = c_lo; c < c_lo + kEpiCols; c += 64) {
+      const uint32_t j0 = tl.J * kTN + c;  // first column of this group
+      if (j0 + 1 >= i0 + rows) break;      // no row reaches column j0 (warp-uniform)
+      uint32_t d[64];
+      __syncwarp();
+      tmem_ld64(t_lane + 256u * h + c, d);
+      tmem_ld_wait();
+      turn_chunk<0>(buf, d, sites, max_dist, lane);
+      __syncwarp();
+      store_chunk<T>(out, t0 + j0, i0, rows, j0, buf, lane);
+      __syncwarp();  // the buffer is rewritten next
+      if (j0 + 33 >= i0 + rows) break;  // no row reaches column j0 + 32
+      turn_chunk<32>(buf, d, sites, max_dist, lane);
+      __syncwarp();
+      store_chunk<T>(out, t0 + j0 + 32, i0, rows, j0 + 32, buf, lane);
+      __syncwarp();
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kMmaThreads, 1)
@@ -340,15 +409,17 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       mbar_wait_bounded(&fin, 0, 4 * kMmaWaitNs);
     }
   } else {
-    // epilogue warps 2-5: warp w reads TMEM lanes 32 (w % 4) .. + 31, which
-    // are rows 32 (w % 4) + lane of each row tile of the item. Each 32 x 32
-    // chunk goes through the warp's padded shared buffer (row r at words
-    // 33 r: conflict-free both ways), so that one store instruction writes
-    // 32 consecutive entries of one row rather than one entry of 32 rows.
-    const uint32_t sub = warp & 3u;
+    // epilogue warps 2 .. 2 + kEpiWarps - 1: warp w reads TMEM lanes
+    // 32 (w % 4) .. + 31, which are rows 32 (w % 4) + lane of each row tile
+    // of the item, in columns kEpiCols ((w - 2) / 4) .. + kEpiCols - 1. Each
+    // 32 x 32 chunk goes through the warp's padded shared buffer (row r at
+    // words 33 r: conflict-free both ways), so that one store instruction
+    // writes 32 consecutive entries of one row rather than one entry of 32
+    // rows.
+    const uint32_t sub = warp & 3u, c_lo = ((warp - 2) / 4) * kEpiCols;
     const uint32_t t_lane = tmem + ((sub * 32) << 16);
     uint32_t *buf = reinterpret_cast<uint32_t *>(smem + kMmaStages * kStageBytes) +
-                    sub * 32 * kEpiPitch;
+                    (warp - 2) * 32 * kEpiPitch;
     uint32_t it = 0;
     for (uint32_t t = blockIdx.x; t < n_items; t += gridDim.x, ++it) {
       const bool got = mbar_wait_bounded(&done, it & 1u, 4 * kMmaWaitNs);
@@ -361,46 +432,12 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       tc_after_sync();
       const MmaItem tl = items[t];
       const MmaJob &job = jobs[tl.job];
-      const uint32_t n = job.n, sites = job.sites, max_dist = job.max_dist, dtype = job.dtype;
-      for (uint32_t h = 0; h < tl.halves; ++h) {
-        const uint32_t i0 = (tl.I + h) * kTM + sub * 32;  // output row of lane 0
-        if (i0 >= n) continue;                           // warp-uniform
-        const uint32_t rows = n - i0 < 32u ? n - i0 : 32u;
-#pragma unroll 1
-        for (uint32_t c = 0; c < (uint32_t)kTN; c += 32) {
-          const uint32_t j0 = tl.J * kTN + c;  // first column of this chunk
-          if (j0 + 1 >= i0 + rows) break;      // no row reaches column j0 (warp-uniform)
-          uint32_t d[32];
-          __syncwarp();
-          tmem_ld32(t_lane + 256u * h + c, d);
-          tmem_ld_wait();
-          // min(sites - matches, max_dist) (FP32 integers)
-#pragma unroll
-          for (uint32_t j = 0; j < 32; ++j) {
-            const uint32_t mism = sites - (uint32_t)__uint_as_float(d[j]);
-            buf[lane * kEpiPitch + j] = mism < max_dist ? mism : max_dist;
-          }
-          __syncwarp();
-          // row i = i0 + r holds entries tri(i) + j0 .. + min(i - j0, 32) - 1
-          unsigned long long e =
-              (unsigned long long)i0 * (i0 - 1) / 2 + j0 - job.out_base + lane;
-#pragma unroll 1
-          for (uint32_t r = 0; r < rows; ++r) {
-            const uint32_t i = i0 + r;
-            if (j0 < i && lane < i - j0) {
-              const uint32_t v = buf[r * kEpiPitch + lane];
-              if (dtype == 1)
-                store_entry<uint8_t>(job.out, e, v);
-              else if (dtype == 2)
-                store_entry<uint16_t>(job.out, e, v);
-              else
-                store_entry<uint32_t>(job.out, e, v);
-            }
-            e += i;
-          }
-          __syncwarp();  // the buffer is rewritten by the next chunk
-        }
-      }
+      if (job.dtype == 1)
+        epilogue_share<uint8_t>(tl, job, t_lane, c_lo, sub, lane, buf);
+      else if (job.dtype == 2)
+        epilogue_share<uint16_t>(tl, job, t_lane, c_lo, sub, lane, buf);
+      else
+        epilogue_share<uint32_t>(tl, job, t_lane, c_lo, sub, lane, buf);
       // the accumulators may be overwritten
       tc_before_sync();
       mbar_arrive(&tmem_free);
