@@ -109,6 +109,28 @@ def test_reference_distances_oracle(tmp_path):
                                   o.fasta_sequence_indices(fa, 777))
 
 
+def test_reference_distances_ragged(tmp_path):
+    """Records of lengths 1 to past two 4,096-site segments, starting at every
+    byte position within 16-byte blocks of the file, against a longer
+    reference: each count runs over the record's own length."""
+    rng = np.random.default_rng(21)
+    alphabet = np.frombuffer(b"ACGT-NXacgt*-", dtype=np.uint8)
+    ref = alphabet[rng.integers(0, 5, 9001)].tobytes()  # A, C, G, T, -
+    recs = []
+    for k in range(300):
+        n = k + 1 if k < 40 else int(rng.integers(1, 9002))
+        r = bytearray(ref[:n])
+        for f in rng.integers(0, n, size=n // 40 + 1):
+            r[f] = alphabet[rng.integers(0, len(alphabet))]
+        recs.append(bytes(r))
+    # names of varying length move each record's start within 16-byte blocks
+    fa = b"".join(b">r%d%s\n" % (i, b"x" * (i % 17)) + r + b"\n" for i, r in enumerate(recs))
+    path = write(tmp_path, "ragged.fasta", fa)
+    for x in (False, True):
+        got = hd.fasta_reference_distances(ref.decode(), path, include_x=x)
+        np.testing.assert_array_equal(got, o.reference_distances(ref, fa, x))
+
+
 def test_resident_alignment_queries(ctx):
     rows, root, _ = synth.alignment(600, 2999, p=1e-3, seed=13, dup_frac=0.3)
     fa = synth.to_fasta(rows)
