@@ -961,60 +961,63 @@ __global__ void __launch_bounds__(32 * kRefWarps)
               uint64_t R, uint64_t max_len, const uint8_t *ref, Table256 lookup, uint32_t *out) {
   __shared__ uint8_t lk[256];
   __shared__ uint4 rsm[kRefSeg / 16];
-  const uint64_t s_lo = (uint64_t)blockIdx.y * kRefSeg;  // < max_len
-  // the reference is 16-byte aligned with 16 readable bytes past max_len
-  const uint64_t avail = max_len - s_lo < kRefSeg ? max_len - s_lo : kRefSeg;
-  const uint4 *rg = reinterpret_cast<const uint4 *>(ref + s_lo);
-  for (uint64_t i = threadIdx.x; i < (avail + 15) / 16; i += blockDim.x) rsm[i] = rg[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) lk[i] = lookup.v[i];
-  __syncthreads();
   const int lane = threadIdx.x & 31;
   const uint64_t r = (uint64_t)blockIdx.x * kRefWarps + (threadIdx.x >> 5);
-  if (r >= R) return;
-  const uint64_t len = rl[r];
-  if (s_lo >= len) return;  // warp-uniform
+  const uint64_t len = r < R ? rl[r] : 0;
   const uint64_t lo = reinterpret_cast<uint64_t>(base), hi = lo + bytes;
-  const uint64_t seg = len - s_lo < kRefSeg ? len - s_lo : kRefSeg;
-  const uint64_t P = lo + rs[r] + s_lo;  // the record's site s_lo
-  const uint64_t A = P & ~15ull, end = P + seg;
-  const uint32_t d = (uint32_t)(P - A), dw = d >> 2, db = d & 3;
-  uint32_t cnt = 0;
-  for (uint64_t o0 = 0; o0 < seg; o0 += 512) {  // warp-uniform steps
-    const uint64_t o = o0 + 16 * (uint64_t)lane;
-    const uint4 va = A + o < end ? load16_in(A + o, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
-    uint4 vn;
-    vn.x = __shfl_down_sync(0xffffffffu, va.x, 1);
-    vn.y = __shfl_down_sync(0xffffffffu, va.y, 1);
-    vn.z = __shfl_down_sync(0xffffffffu, va.z, 1);
-    vn.w = __shfl_down_sync(0xffffffffu, va.w, 1);
-    if (lane == 31)
-      vn = (d && A + o + 16 < end) ? load16_in(A + o + 16, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
-    if (o >= seg) continue;
-    const uint4 vr = rsm[o >> 4];
-    const uint32_t bw[8] = {va.x, va.y, va.z, va.w, vn.x, vn.y, vn.z, vn.w};
-    const uint32_t rw[4] = {vr.x, vr.y, vr.z, vr.w};
+  const uint64_t S = (max_len + kRefSeg - 1) / kRefSeg;
+  for (uint64_t y = blockIdx.y; y < S; y += gridDim.y) {  // block-uniform
+    const uint64_t s_lo = y * kRefSeg;                     // < max_len
+    // the reference is 16-byte aligned with 16 readable bytes past max_len
+    const uint64_t avail = max_len - s_lo < kRefSeg ? max_len - s_lo : kRefSeg;
+    const uint4 *rg = reinterpret_cast<const uint4 *>(ref + s_lo);
+    __syncthreads();  // no warp still reads the previous stretch
+    for (uint64_t i = threadIdx.x; i < (avail + 15) / 16; i += blockDim.x) rsm[i] = rg[i];
+    __syncthreads();
+    if (s_lo >= len) continue;  // warp-uniform (also r >= R)
+    const uint64_t seg = len - s_lo < kRefSeg ? len - s_lo : kRefSeg;
+    const uint64_t P = lo + rs[r] + s_lo;  // the record's site s_lo
+    const uint64_t A = P & ~15ull, end = P + seg;
+    const uint32_t d = (uint32_t)(P - A), dw = d >> 2, db = d & 3;
+    uint32_t cnt = 0;
+    for (uint64_t o0 = 0; o0 < seg; o0 += 512) {  // warp-uniform steps
+      const uint64_t o = o0 + 16 * (uint64_t)lane;
+      const uint4 va = A + o < end ? load16_in(A + o, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+      uint4 vn;
+      vn.x = __shfl_down_sync(0xffffffffu, va.x, 1);
+      vn.y = __shfl_down_sync(0xffffffffu, va.y, 1);
+      vn.z = __shfl_down_sync(0xffffffffu, va.z, 1);
+      vn.w = __shfl_down_sync(0xffffffffu, va.w, 1);
+      if (lane == 31)
+        vn = (d && A + o + 16 < end) ? load16_in(A + o + 16, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+      if (o >= seg) continue;
+      const uint4 vr = rsm[o >> 4];
+      const uint32_t bw[8] = {va.x, va.y, va.z, va.w, vn.x, vn.y, vn.z, vn.w};
+      const uint32_t rw[4] = {vr.x, vr.y, vr.z, vr.w};
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      uint32_t blo = bw[j], bhi = bw[j + 1];
+      for (int j = 0; j < 4; ++j) {
+        uint32_t blo = bw[j], bhi = bw[j + 1];
 #pragma unroll
-      for (int t = 1; t < 4; ++t)
-        if (dw == (uint32_t)t) {
-          blo = bw[j + t];
-          bhi = bw[j + t + 1];
+        for (int t = 1; t < 4; ++t)
+          if (dw == (uint32_t)t) {
+            blo = bw[j + t];
+            bhi = bw[j + t + 1];
+          }
+        const uint32_t aw = __funnelshift_r(blo, bhi, 8 * db);  // record sites o + 4j ..
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (o + 4 * j + k >= seg) break;
+          const uint32_t a = (aw >> (8 * k)) & 0xffu, b = (rw[j] >> (8 * k)) & 0xffu;
+          const uint32_t la = lk[a], lb = lk[b];
+          const bool count = (la & lb) == 0 || (a != b && la != 0xffu && lb != 0xffu);
+          cnt += count ? 1u : 0u;
         }
-      const uint32_t aw = __funnelshift_r(blo, bhi, 8 * db);  // record sites o + 4j ..
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (o + 4 * j + k >= seg) break;
-        const uint32_t a = (aw >> (8 * k)) & 0xffu, b = (rw[j] >> (8 * k)) & 0xffu;
-        const uint32_t la = lk[a], lb = lk[b];
-        const bool count = (la & lb) == 0 || (a != b && la != 0xffu && lb != 0xffu);
-        cnt += count ? 1u : 0u;
       }
     }
+    cnt = warp_sum(cnt);
+    if (lane == 0 && cnt) atomicAdd(&out[r], cnt);
   }
-  cnt = warp_sum(cnt);
-  if (lane == 0 && cnt) atomicAdd(&out[r], cnt);
 }
 
 void reference_distances_device(hd_ctx *ctx, const Records &rec, const uint8_t *d_ref,
@@ -1031,8 +1034,10 @@ void reference_distances_device(hd_ctx *ctx, const Records &rec, const uint8_t *
   HD_CUDA(cudaMemsetAsync(d_out, 0, rec.n * sizeof(uint32_t), ctx->stream));
   if (!rec.max_len) return;
   const uint64_t S = ceil_div(rec.max_len, kRefSeg), X = ceil_div(rec.n, (uint64_t)kRefWarps);
-  if (S > 65535 || X > 0x7fffffffull) fail(HD_ERR_ARG, "records too long or too many");
-  k_refdist<<<dim3((unsigned)X, (unsigned)S), 32 * kRefWarps, 0, ctx->stream>>>(
+  if (X > 0x7fffffffull) fail(HD_ERR_ARG, "too many records");
+  // stretches past 65,535 are taken by the blocks' loop
+  k_refdist<<<dim3((unsigned)X, (unsigned)std::min<uint64_t>(S, 65535)), 32 * kRefWarps, 0,
+              ctx->stream>>>(
       rec.base, rec.bytes, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(), rec.n,
       rec.max_len, d_ref, lk, d_out);
   HD_LAUNCHED(ctx);
