@@ -154,9 +154,23 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(tmpdir):
-    from hammingdist_gb300 import synth
+def synth_module():
+    """The seeded generator (hammingdist_gb300/synth.py, pure numpy), loaded
+    from its file: the reference arm must not import the product package,
+    whose __init__ loads the native library."""
+    import importlib.util
 
+    if "_hd_synth" not in sys.modules:
+        spec = importlib.util.spec_from_file_location(
+            "_hd_synth", os.path.join(ROOT, "hammingdist_gb300", "synth.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        sys.modules["_hd_synth"] = mod
+    return sys.modules["_hd_synth"]
+
+
+def make_workload(tmpdir):
+    synth = synth_module()
     rows, root, _ = synth.alignment(N, L, p=P_SUB, seed=SEED, dup_frac=DUP)
     fa = synth.to_fasta(rows)
     path = os.path.join(tmpdir, "bench.fasta")
@@ -174,74 +188,55 @@ def measured_peaks():
         return {}
 
 
-def profile_traffic():
-    """DRAM bytes per pairwise launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "pairwise_mma_n14000_L29903.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the distance kernel on this workload's 14,000 distinct rows at L=29,903,
+# from one ncu capture (one launch, one pass):
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none
+#       -k regex:k_pairwise_mma -s 1 -c 1
+#       python bench.py --kernel-only --n 14000 --steps 1 --warmup 1
+# bench.py cannot run ncu itself, so the figure is a constant of the kernel
+# build it was measured on (KERNEL_DRAM_SOURCE).
+KERNEL_DRAM_BYTES = 20_063_901_440
+KERNEL_DRAM_SOURCE = "ncu capture of k_pairwise_mma (FP8 operand), n=14000 L=29903, one launch"
 
 
 # ------------------------------------------------------------------ CPU leg
-def cpu_sample_rows(rows, budget_s):
-    """Unique rows of a bounded sample sized to ~budget_s of oracle work."""
+def oracle_pass(fa, root):
+    """One pass of the reference's CPU algorithm over the whole workload, as
+    restated by the oracle port (from_fasta(remove_duplicates=True): read +
+    dedupe + pack + the dense AND-rule lower triangle on all host threads,
+    include/hamming/hamming_impl.hh:161-175; then fasta_reference_distances,
+    src/hamming.cc:104-141, single-threaded as in the reference). Returns
+    (lt, sequence indices, reference distances, seconds)."""
     from oracle import hd_oracle as o
 
-    uniq = list(dict.fromkeys(r.tobytes() for r in rows))
-    cal = uniq[:600]
     t = time.perf_counter()
-    o.lt_dense(cal)
-    dt = time.perf_counter() - t
-    rate = len(cal) * (len(cal) - 1) / 2 * L / dt  # pair-sites/s
-    n_s = int((2 * budget_s * rate / L) ** 0.5)
-    n_s = max(600, min(n_s, len(uniq)))
-    return uniq[:n_s], rate
-
-
-def cpu_baseline(rows, budget_s):
-    """The reference's CPU algorithm on the host cores, bounded sample."""
-    from oracle import hd_oracle as o
-
-    kind = "port"
-    sample, _ = cpu_sample_rows(rows, budget_s)
-    fa = b"".join(b">s\n" + s + b"\n" for s in sample)
-    t = time.perf_counter()
-    o.from_fasta_dense(fa, remove_duplicates=True)
-    dt = time.perf_counter() - t
-    n_s = len(sample)
-    ps = n_s * (n_s - 1) / 2 * L
-    return {"value": ps / dt / 1e9, "unit": "Gpair-sites/s", "cores": o.num_threads(),
-            "kind": kind,
-            "sample": f"{n_s} unique rows of the workload (L={L}): parse+dedupe+pack+dense "
-                      f"AND-rule lower triangle, {dt:.1f} s, OpenMP"}
+    lt, idx = o.from_fasta_dense(fa, remove_duplicates=True)
+    rd = o.reference_distances(root, fa)
+    return lt, idx, rd, time.perf_counter() - t
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU algorithm (the oracle port: the
+    GPU machine has no reference sources to compile) on the host cores, on the
+    same workload as the GPU arm: all 20,000 records (14,000 unique rows) of
+    the n=20,000 file plus the reference distances, every step. The product
+    package is not imported: the workload comes from the generator's file."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
+    from oracle import hd_oracle as o
+
     with tempfile.TemporaryDirectory() as d:
         fa, root, path, rows = make_workload(d)
-        from oracle import hd_oracle as o
-
-        budget = max(3.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
-        sample, _ = cpu_sample_rows(rows, budget)
-        sfa = b"".join(b">s\n" + s + b"\n" for s in sample)
-        n_s = len(sample)
+        n_u = len(dict.fromkeys(r.tobytes() for r in rows))
+        del rows
         times = []
         for k in range(args.warmup + args.steps):
-            t = time.perf_counter()
-            o.from_fasta_dense(sfa, remove_duplicates=True)
-            dt = time.perf_counter() - t
+            _, _, _, dt = oracle_pass(fa, root)
             if k >= args.warmup:
                 times.append(dt)
-        ps = n_s * (n_s - 1) / 2 * L
+        ps = n_u * (n_u - 1) / 2 * L
         mean = sum(times) / len(times)
         value = ps / mean / 1e9
         line = {
@@ -249,11 +244,14 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic (seeded generator; no public dataset)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "sample_rows": n_s, "l2": "inputs larger than L2"},
+            "config": {"workload": WORKLOAD, "unique_rows": n_u,
+                       "pairs": n_u * (n_u - 1) // 2, "same_config": True,
+                       "l2": "inputs larger than L2"},
             "cpu_baseline": {"value": value, "unit": "Gpair-sites/s", "cores": o.num_threads(),
                              "kind": "port",
-                             "sample": f"{n_s} unique rows per step (bounded sample of the "
-                                       f"workload), dense AND rule, OpenMP"},
+                             "sample": f"the whole workload every step: {N} records, {n_u} unique "
+                                       f"rows, dense AND-rule lower triangle (OpenMP) + reference "
+                                       f"distances (one thread)"},
             "e2e": {"value": value, "unit": "Gpair-sites/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
         }
@@ -261,6 +259,28 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU leg
+def value_phases(ctx, d_fa, nbytes, root, d_lt):
+    """One untimed traced step through the C ABI: the stream time of each
+    phase (CUDA events on the library's stream)."""
+    ctx.trace(True)
+    a = ctx.alignment_from_fasta(d_fa.data_ptr(), nbytes, on_device=True, remove_duplicates=True)
+    t1 = ctx.trace_last()
+    ctx.pairwise_lt(a, dtype=np.uint8, max_distance=255, out=d_lt.data_ptr(), out_on_device=True)
+    t2 = ctx.trace_last()
+    ctx.alignment_reference_distances(a, root)
+    a.free()
+    ctx.trace(False)
+    phases = {}
+    for text in (t1, t2):
+        body = text.split(":", 1)[1] if ":" in text else ""
+        for part in body.split(","):
+            part = part.strip()
+            if part.endswith(" ms") and not part.startswith("stream time"):
+                name, ms = part[:-3].rsplit(" ", 1)
+                phases[name] = round(float(ms), 3)
+    return phases
+
+
 def run_ours(args):
     import torch
 
@@ -274,71 +294,58 @@ def run_ours(args):
     import hammingdist_gb300 as hd
     from hammingdist_gb300 import abi
 
-    ctx = abi.Context(local)
+    dev = f"cuda:{local}"
     with tempfile.TemporaryDirectory() as d:
         fa, root, path, rows = make_workload(d)
         nbytes = len(fa)
-        d_fa = torch.frombuffer(bytearray(fa), dtype=torch.uint8).to(f"cuda:{local}")
-        stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
-
-        # sizes from a first pass (also warms the pools)
-        aln = ctx.alignment_from_fasta(d_fa.data_ptr(), nbytes, on_device=True,
-                                       remove_duplicates=True)
-        n_u = aln.n_rows
+        uniq_rows = len(dict.fromkeys(r.tobytes() for r in rows))
+        del rows
+        d_fa = torch.frombuffer(bytearray(fa), dtype=torch.uint8).to(dev)
+        n_u = uniq_rows
         pairs = n_u * (n_u - 1) // 2
-        aln.free()
-        d_lt = torch.empty(pairs, dtype=torch.uint8, device=f"cuda:{local}")
-        refq = root
+        d_lt = torch.empty(pairs, dtype=torch.uint8, device=dev)
+        refq = root.decode()
 
+        # one step = one call of the module: parse + dedupe + pack + distances
+        # + reference distances on the device, results in HBM (distances) and
+        # on the host (indices, reference distances)
         def step():
-            a = ctx.alignment_from_fasta(d_fa.data_ptr(), nbytes, on_device=True,
-                                         remove_duplicates=True)
-            ctx.pairwise_lt(a, dtype=np.uint8, max_distance=255, out=d_lt.data_ptr(),
-                            out_on_device=True)
-            pair_ms, tiles = ctx.last_pairwise_timing()
-            rd = ctx.alignment_reference_distances(a, refq)
-            a.free()
-            return pair_ms, tiles, rd
+            return hd.from_fasta_device(d_fa.data_ptr(), nbytes, d_lt.data_ptr(), pairs,
+                                        remove_duplicates=True, max_distance=255,
+                                        reference_sequence=refq)
 
         for _ in range(args.warmup):
-            step()
+            r = step()
+        assert r["nsamples"] == n_u, (r["nsamples"], n_u)
+        stream = torch.cuda.ExternalStream(hd._stream(), device=dev)
         torch.cuda.synchronize()
         if ws > 1:
             torch.distributed.barrier()
         clocks = Clocks(local)
         clocks.start()
-        launches0 = ctx.kernel_launches
+        launches0 = hd._kernel_launches()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         ev0.record(stream)
         pair_ms = []
         for _ in range(args.steps):
-            pm, tiles, rd = step()
-            pair_ms.append(pm)
+            r = step()
+            pair_ms.append(r["kernel_ms"])
         ev1.record(stream)
         torch.cuda.synchronize()
         clk = clocks.stop()
-        launches = ctx.kernel_launches - launches0
-        elapsed = replica_elapsed(ev0.elapsed_time(ev1) / 1e3, ws, f"cuda:{local}")
+        launches = hd._kernel_launches() - launches0
+        elapsed = replica_elapsed(ev0.elapsed_time(ev1) / 1e3, ws, dev)
         ms_step = elapsed / args.steps * 1e3
         value = replica_value(pairs * L * args.steps, ws, elapsed) / 1e9
+        lt_dev = d_lt.cpu().numpy()
+        idx_dev, rd_dev = r["sequence_indices"], r["reference_distances"]
 
-        # parity on the final step's device results: sampled rows vs the oracle
-        from oracle import hd_oracle as o
+        # per-phase stream times of one more (untimed, traced) step
+        ctx = abi.Context(local)
+        phases = value_phases(ctx, d_fa, nbytes, root, d_lt)
 
-        uniq = list(dict.fromkeys(r.tobytes() for r in rows))
-        assert len(uniq) == n_u
-        rng = np.random.default_rng(1)
-        pick = np.sort(rng.choice(n_u, size=min(48, n_u), replace=False))
-        want = o.lt_dense([uniq[i] for i in pick])
-        lt_host = d_lt.cpu().numpy()
-        got = np.array([lt_host[pick[a] * (pick[a] - 1) // 2 + pick[b]]
-                        for a in range(len(pick)) for b in range(a)], dtype=np.uint8)
-        parity = bool(np.array_equal(got, want))
-        rd_want = o.reference_distances(root, fa)
-        parity = parity and bool(np.array_equal(rd, rd_want))
-
-        # e2e: the public API with host buffers (file -> pinned -> device -> host)
+        # e2e: the public API with host buffers (file -> device -> host)
         e2e_times = []
         h2d = d2h = 0
         for k in range(args.warmup + args.steps):
@@ -352,28 +359,43 @@ def run_ours(args):
                 t = time.perf_counter()
                 ds = hd.from_fasta(path, use_gpu=True, remove_duplicates=True)
                 lt_arr = ds.lt_array
-                rd2 = hd.fasta_reference_distances(root.decode(), path)
+                rd2 = hd.fasta_reference_distances(refq, path)
                 torch.cuda.synchronize()
                 dt = time.perf_counter() - t
             if k >= args.warmup:
                 e2e_times.append(dt)
             h2d = nbytes  # the FASTA goes up once per step
             d2h = lt_arr.nbytes + 8 * N + rd2.nbytes
-        parity = parity and bool(np.array_equal(np.asarray(lt_arr), lt_host)) and \
-            bool(np.array_equal(rd2, rd_want))
         e2e_mean = sum(e2e_times) / len(e2e_times)
         e2e_value = ws * pairs * L / e2e_mean / 1e9
+
+        # parity at full size: the oracle port computes the whole workload
+        # (every one of the 97,993,000 distances, the 20,000 sequence indices
+        # and reference distances) and both GPU paths must equal it byte for
+        # byte; the same pass is the timed CPU baseline
+        lt_o, idx_o, rd_o, cpu_s = oracle_pass(fa, root)
+        checks = {
+            "lt_resident": bool(np.array_equal(lt_dev, lt_o)),
+            "lt_e2e": bool(np.array_equal(np.asarray(lt_arr), lt_o)),
+            "sequence_indices": bool(np.array_equal(np.asarray(idx_dev), idx_o)) and
+            bool(np.array_equal(np.asarray(ds_indices(ds, d)), idx_o)),
+            "reference_distances": bool(np.array_equal(rd_dev, rd_o)) and
+            bool(np.array_equal(rd2, rd_o)),
+        }
+        exact = all(checks.values())
+        entries_equal = int(np.count_nonzero(lt_dev == lt_o)) if lt_dev.size == lt_o.size else 0
 
         # roofline of the dominant kernel, the tensor-core engine: 5 multiply-adds
         # (10 FLOP) per pair-site, matches = <planes, planes'> - 3 <dash, dash'>
         peaks = ctx.measure_int_peaks()
         fp8_peak = ctx.measure_mma_peak()
+        ctx.close()
         kern_s = statistics.mean(pair_ms) / 1e3
         flop_per_launch = 10.0 * pairs * L
         achieved = flop_per_launch / kern_s / 1e12
         peak = fp8_peak / 1e12
-        traffic = profile_traffic()
         bf16 = measured_peaks().get("bf16_tflops")
+        busy = sum(phases.values())
 
         if rank == 0:
             line = {
@@ -384,11 +406,16 @@ def run_ours(args):
                 "config": {"workload": WORKLOAD, "unique_rows": n_u, "pairs": pairs,
                            "nominal_value": ws * (N * (N - 1) // 2) * L * args.steps / elapsed / 1e9,
                            "l2": "inputs larger than L2 (598 MB FASTA, 209 MB packed rows); no flush",
-                           "parallelism": "replicas" if ws > 1 else "single GPU"},
-                "parity": "bit-exact (sampled rows + all reference distances vs oracle)"
-                if parity else "MISMATCH",
+                           "parallelism": "replicas" if ws > 1 else "single GPU",
+                           "step_phases_ms": phases,
+                           "step_host_gap_ms": ms_step - busy},
+                "parity": ("bit-exact: %d/%d distances, %d sequence indices and %d reference "
+                           "distances equal the oracle (resident and e2e results)"
+                           % (entries_equal, lt_o.size, len(idx_o), len(rd_o)))
+                if exact else "MISMATCH " + json.dumps(checks),
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
-                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                             "unit": "TFLOP/s", "frac": achieved / peak,
+                             "traffic": KERNEL_DRAM_BYTES, "traffic_source": KERNEL_DRAM_SOURCE,
                              "kernel_ms": kern_s * 1e3,
                              "peak_source": "in-run FP8 tcgen05 MMA microbenchmark "
                                             "(hd_measure_mma_peak); MEASURED_PEAKS.json has "
@@ -406,11 +433,48 @@ def run_ours(args):
                 "clocks": clk,
             }
             if not args.no_cpu:
-                line["cpu_baseline"] = cpu_baseline(rows, args.cpu_seconds)
+                from oracle import hd_oracle as o
+
+                line["cpu_baseline"] = {
+                    "value": pairs * L / cpu_s / 1e9, "unit": "Gpair-sites/s",
+                    "cores": o.num_threads(), "kind": "port",
+                    "sample": f"the whole workload once: {N} records, {n_u} unique rows, dense "
+                              f"AND-rule lower triangle (OpenMP) + reference distances, "
+                              f"{cpu_s:.1f} s"}
+            del d_fa, d_lt
+            torch.cuda.empty_cache()
+            if not args.headline_only and ws == 1:
+                line.update(extra_legs(args))
             print(json.dumps(line), flush=True)
-    ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def ds_indices(ds, tmpdir):
+    """The DataSet's sequence indices through its own writer."""
+    p = os.path.join(tmpdir, "idx.txt")
+    ds.dump_sequence_indices(p)
+    return np.loadtxt(p, dtype=np.uint64, ndmin=1)
+
+
+def extra_legs(args):
+    """The rest of the reference's workload list, each bounded in time and
+    reported under its own key of the headline line: config 1 (n=1,000 from
+    file, against the CPU port), config 4 (64 uneven alignments batched
+    against a loop of plain calls) and config 5 (serving, a shorter Poisson
+    stream than the --serve run's 60 s)."""
+    out = {}
+    legs = (("config1_small", lambda: small_leg(steps=10, warmup=3)),
+            ("config4_batched", lambda: batched_leg(args, steps=5, warmup=2)),
+            ("config5_serve", lambda: serve_leg(args, seconds=args.extra_serve_seconds)))
+    for key, fn in legs:
+        t = time.perf_counter()
+        try:
+            out[key] = fn()
+        except Exception as e:  # reported in the line, not hidden
+            out[key] = {"error": f"{type(e).__name__}: {e}"}
+        out[key]["leg_seconds"] = round(time.perf_counter() - t, 1)
+    return out
 
 
 def run_kernel_only(args):
@@ -419,8 +483,9 @@ def run_kernel_only(args):
     into a device buffer, CUDA-event time per launch."""
     import torch
 
-    from hammingdist_gb300 import abi, synth
+    from hammingdist_gb300 import abi
 
+    synth = synth_module()
     ctx = abi.Context(0)
     rows, _, _ = synth.alignment(args.n, args.L, p=P_SUB, seed=SEED)
     seqs = [r.tobytes() for r in rows]
@@ -443,6 +508,10 @@ def run_kernel_only(args):
 
 
 def run_batched(args):
+    print(json.dumps(batched_leg(args, args.steps, args.warmup)), flush=True)
+
+
+def batched_leg(args, steps, warmup):
     """Batched alignments: 64 independent alignments, n log-uniform in
     [50, 5000], L from {1000, 5000, 10000, 29903}, substitution p uniform in
     [1e-4, 1e-2], each from its own seeded root, mixed uint8/uint16 outputs.
@@ -453,8 +522,8 @@ def run_batched(args):
     import torch
 
     import hammingdist_gb300 as hd
-    from hammingdist_gb300 import synth
 
+    synth = synth_module()
     rng = np.random.default_rng(4242)
     k = args.batch_size
     with tempfile.TemporaryDirectory() as d:
@@ -483,14 +552,14 @@ def run_batched(args):
         res = {}
         for name, fn in (("plain", plain), ("batched", batched)):
             times = []
-            for it in range(args.warmup + args.steps):
+            for it in range(warmup + steps):
                 with quiet_stdout():
                     torch.cuda.synchronize()
                     t = time.perf_counter()
                     out = fn()
                     torch.cuda.synchronize()
                     dt = time.perf_counter() - t
-                if it >= args.warmup:
+                if it >= warmup:
                     times.append(dt)
             res[name] = (out, statistics.median(times))
         same = all(np.array_equal(np.asarray(a.lt_array), np.asarray(b.lt_array))
@@ -511,13 +580,13 @@ def run_batched(args):
         for a, dt, md in zip(alns, dts, mds):
             batch.add(a, dtype=dt, max_distance=md)
         r_plain, r_batch = [], []
-        for it in range(args.warmup + args.steps):
+        for it in range(warmup + steps):
             t = time.perf_counter()
             outs_p = [ctx.pairwise_lt(a, dtype=dt, max_distance=md) for a, dt, md in zip(alns, dts, mds)]
             t1 = time.perf_counter()
             outs_b = batch.run()
             t2 = time.perf_counter()
-            if it >= args.warmup:
+            if it >= warmup:
                 r_plain.append(t1 - t)
                 r_batch.append(t2 - t1)
         same_r = all(np.array_equal(x, y) for x, y in zip(outs_p, outs_b))
@@ -525,16 +594,16 @@ def run_batched(args):
         graph_ms, n_launch, n_tiles = batch.timing()
         batch.free()
         ctx.close()
-        print(json.dumps({
+        return {
             "mode": "batched", "metric": "matrices/s (64 uneven alignments)",
             "batched_matrices_per_s": k / tb, "plain_loop_matrices_per_s": k / tp,
             "speedup": tp / tb, "batched_ms": tb * 1e3, "plain_ms": tp * 1e3,
             "pair_sites": work, "batched_Gpair_sites_per_s": work / tb / 1e9,
-            "bit_exact_vs_plain": same and same_r, "steps": args.steps, "warmup": args.warmup,
+            "bit_exact_vs_plain": same and same_r, "steps": steps, "warmup": warmup,
             "resident": {"plain_loop_ms": rp * 1e3, "batched_ms": rb * 1e3, "speedup": rp / rb,
                          "batch_graph_ms": graph_ms, "persistent_launches": n_launch,
                          "tiles": n_tiles, "Gpair_sites_per_s": work / rb / 1e9},
-            "tuning": args.tuning or "built-in"}), flush=True)
+            "tuning": args.tuning or "built-in"}
 
 
 def _device_fasta_file(ctx, path, n, L_, p, seed):
@@ -633,15 +702,19 @@ def run_streaming(args):
 
 
 def run_small(args):
+    print(json.dumps(small_leg(args.steps, args.warmup)), flush=True)
+
+
+def small_leg(steps, warmup):
     """The reference's config 1: from_fasta(use_gpu=True) on n=1,000 rows,
     L=29,903, p=1e-3, uint8, through the public API from the file, every step
     reading the file again (new mtime). Beside it the oracle port computes the
     same matrix from the same file on all host threads. Both must agree bit
     for bit."""
     import hammingdist_gb300 as hd
-    from hammingdist_gb300 import synth
     from oracle import hd_oracle as o
 
+    synth = synth_module()
     n, L_ = 1000, 29903
     rows, root, _ = synth.alignment(n, L_, p=1e-3, seed=11, dup_frac=0.0)
     fa = synth.to_fasta(rows)
@@ -651,14 +724,14 @@ def run_small(args):
         with open(path, "wb") as f:
             f.write(fa)
         times = []
-        for k in range(args.warmup + args.steps):
+        for k in range(warmup + steps):
             st = time.time_ns()
             os.utime(path, ns=(st, st))
             with quiet_stdout():
                 t = time.perf_counter()
                 lt = hd.from_fasta(path, use_gpu=True).lt_array
                 dt = time.perf_counter() - t
-            if k >= args.warmup:
+            if k >= warmup:
                 times.append(dt)
         gpu_s = statistics.median(times)
         cpu_times = []
@@ -667,12 +740,12 @@ def run_small(args):
             want = o.from_fasta_dense(open(path, "rb").read())[0]
             cpu_times.append(time.perf_counter() - t)
         cpu_s = statistics.median(cpu_times)
-    print(json.dumps({
+    return {
         "mode": "config1", "workload": "from_fasta(use_gpu=True) n=1000 L=29903 p=1e-3 uint8, file to lt_array",
         "pairs": pairs, "gpu_e2e_ms": gpu_s * 1e3, "gpu_Gpair_sites_per_s": pairs * L_ / gpu_s / 1e9,
         "cpu_port_ms": cpu_s * 1e3, "cpu_cores": o.num_threads(),
         "cpu_Gpair_sites_per_s": pairs * L_ / cpu_s / 1e9, "speedup": cpu_s / gpu_s,
-        "bit_exact": bool(np.array_equal(np.asarray(lt), want))}), flush=True)
+        "bit_exact": bool(np.array_equal(np.asarray(lt), want))}
 
 
 def run_formats(args):
@@ -749,6 +822,10 @@ def run_formats(args):
 
 
 def run_serve(args):
+    print(json.dumps(serve_leg(args, args.serve_seconds)), flush=True)
+
+
+def serve_leg(args, seconds):
     """Serving: 8 alignments resident in HBM (n = 200k, 100k, 50k, 50k, 20k,
     20k, 10k, 10k at --serve-scale 1; L=29,903; generated on the device), a
     Poisson request stream (--serve-rate per s for --serve-seconds): 60%
@@ -761,8 +838,9 @@ def run_serve(args):
 
     import torch
 
-    from hammingdist_gb300 import abi, synth
+    from hammingdist_gb300 import abi
 
+    synth = synth_module()
     ctx = abi.Context(0)
     L_ = 29903
     sizes = [int(x * args.serve_scale) for x in (200000, 100000, 50000, 50000, 20000, 20000,
@@ -780,7 +858,7 @@ def run_serve(args):
     roots = [synth.device_root(900 + k, L_) for k in range(len(sizes))]
 
     rng = np.random.default_rng(31337)
-    n_req = int(args.serve_rate * args.serve_seconds)
+    n_req = int(args.serve_rate * seconds)
     gaps = rng.exponential(1.0 / args.serve_rate, n_req)
     arrivals = np.cumsum(gaps)
     reqs = []
@@ -869,16 +947,17 @@ def run_serve(args):
                     ctx.write_sparse(lt, r[3], r[4], sp)
                 v.free()
     serial = n_serial / (time.perf_counter() - t)
-    print(json.dumps({
-        "mode": "serve", "metric": "p50/p99 ms and req/s (8 resident alignments)",
-        "resident_rows": sizes, "L": L_, "requests": len(reqs), "rate_per_s": args.serve_rate,
-        "seconds": args.serve_seconds, "load_s": load_s, "paced": paced,
-        "saturated": saturated, "serial_plain_req_per_s": serial,
-        "saturated_vs_serial": saturated["req_per_s"] / serial,
-        "budget_gb": args.serve_budget_gb}), flush=True)
     for a in alns:
         a.free()
     ctx.close()
+    return {
+        "mode": "serve", "metric": "p50/p99 ms and req/s (8 resident alignments)",
+        "resident_rows": sizes, "L": L_, "requests": len(reqs), "rate_per_s": args.serve_rate,
+        "seconds": seconds, "load_s": load_s, "paced": paced,
+        "saturated": saturated, "serial_plain_req_per_s": serial,
+        "saturated_vs_serial": saturated["req_per_s"] / serial,
+        "all_results_checked": "alone == in the mix: tests/test_gpu_serve.py",
+        "budget_gb": args.serve_budget_gb}
 
 
 def main():
@@ -888,7 +967,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true",
+                    help="leave out cpu_baseline (the full-size oracle parity pass still runs)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="leave out the config 1 / 4 / 5 legs of the default line")
+    ap.add_argument("--extra-serve-seconds", type=float, default=15.0,
+                    help="length of the paced serving stream in the default line")
     ap.add_argument("--kernel-only", action="store_true",
                     help="profiling harness: the pairwise kernel alone on --n distinct rows")
     ap.add_argument("--n", type=int, default=12000)

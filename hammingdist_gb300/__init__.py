@@ -32,6 +32,7 @@ from ._C import (  # noqa: E402,F401
     from_csv,
     from_fasta,
     from_fasta_batch,
+    from_fasta_device,
     from_fasta_large,
     from_fasta_to_lower_triangular,
     from_lower_triangular,
@@ -39,6 +40,7 @@ from ._C import (  # noqa: E402,F401
     from_stringlist,
     load_tuning,
     _kernel_launches,
+    _stream,
 )
 
 LIBHD_PATH = _os.path.join(_PKG, "libhd.so")

@@ -285,6 +285,60 @@ DataSet<T> from_fasta(const std::string &filename, bool include_x, bool remove_d
   return ds;
 }
 
+// from_fasta(use_gpu=True) for FASTA text already in device memory, with the
+// lower triangle written to device memory: `fasta` and `out` are CUDA device
+// pointers (e.g. tensor.data_ptr()), `out_bytes` the room at `out`. Parse,
+// dedupe, pack and distances run on the device; optionally the distances of
+// `reference_sequence` to every record (fasta_reference_distances,
+// src/hamming.cc:104-141) come from the same resident rows. Returns a dict:
+// nsamples, sequence_indices (uint64, empty without dedupe), kernel_ms (the
+// distance launch's CUDA-event time) and reference_distances (uint32) when a
+// reference was given. No reference counterpart: the reference reads files.
+py::dict from_fasta_device(uintptr_t fasta, uint64_t nbytes, uintptr_t out, uint64_t out_bytes,
+                           bool remove_duplicates, int max_distance, bool large,
+                           py::object reference_sequence) {
+  std::string ref;
+  const bool want_ref = !reference_sequence.is_none();
+  if (want_ref) ref = py::cast<std::string>(reference_sequence);
+  std::lock_guard<std::mutex> lk(g_mu);
+  hd_ctx *c = ctx();
+  const int dtype = large ? 2 : 1;
+  uint64_t n_rows = 0, n_in = 0;
+  double kernel_ms = 0;
+  uint64_t tiles = 0;
+  std::vector<uint64_t> idx;
+  std::vector<uint32_t> rd;
+  {
+    py::gil_scoped_release nogil;
+    Aln a;
+    check(hd_alignment_from_fasta(c, reinterpret_cast<const char *>(fasta), nbytes, 1,
+                                  remove_duplicates, 0, 0, HD_SEM_GPU, &a.p));
+    check(hd_alignment_info(a.p, &n_rows, nullptr, &n_in, nullptr));
+    const uint64_t entries = n_rows < 2 ? 0 : n_rows * (n_rows - 1) / 2;
+    if (entries * dtype > out_bytes)
+      throw std::invalid_argument("from_fasta_device: the output needs " +
+                                  std::to_string(entries * dtype) + " bytes");
+    if (entries) {
+      check(hd_pairwise_lt(c, a.p, dtype, max_distance, reinterpret_cast<void *>(out), 1));
+      hd_last_pairwise_timing(c, &kernel_ms, &tiles);
+    }
+    if (remove_duplicates) {
+      idx.resize(n_in);
+      check(hd_alignment_sequence_indices(a.p, idx.data()));
+    }
+    if (want_ref) {
+      rd.resize(n_in);
+      check(hd_alignment_reference_distances(c, a.p, ref.data(), ref.size(), 0, rd.data()));
+    }
+  }
+  py::dict r;
+  r["nsamples"] = n_rows;
+  r["sequence_indices"] = py::array_t<uint64_t>((py::ssize_t)idx.size(), idx.data());
+  r["kernel_ms"] = kernel_ms;
+  if (want_ref) r["reference_distances"] = py::array_t<uint32_t>((py::ssize_t)rd.size(), rd.data());
+  return r;
+}
+
 DataSet<uint8_t> from_stringlist(const std::vector<std::string> &data, bool include_x, bool use_gpu,
                                  int max_distance) {
   std::lock_guard<std::mutex> lk(g_mu);
@@ -587,6 +641,14 @@ PYBIND11_MODULE(_C, m) {
         "Distance matrices of several fasta files computed together on the GPU (one batch: "
         "concurrent ingest, one persistent kernel, launches replayed from a CUDA graph). "
         "Returns a list of DataSet (or DataSetLarge where `large`).");
+  m.def("from_fasta_device", &from_fasta_device, py::arg("fasta_ptr"), py::arg("nbytes"),
+        py::arg("out_ptr"), py::arg("out_bytes"), py::arg("remove_duplicates") = false,
+        py::arg("max_distance") = 255, py::arg("large") = false,
+        py::arg("reference_sequence") = py::none(),
+        "from_fasta(use_gpu=True) on FASTA text already in device memory, the lower triangle "
+        "written to device memory (uint8, or uint16 where `large`); optionally the reference "
+        "distances of `reference_sequence` from the same resident rows. Returns a dict with "
+        "nsamples, sequence_indices, kernel_ms and reference_distances.");
   m.def("autotune", &autotune, py::arg("path") = std::string(),
         "Times the pairwise kernel configurations on this GPU, keeps the fastest per "
         "(n, L, dtype) bucket and optionally saves the table as JSON");
@@ -594,5 +656,11 @@ PYBIND11_MODULE(_C, m) {
   m.def("_kernel_launches", []() -> uint64_t {
     std::lock_guard<std::mutex> lk(g_mu);
     return g_ctx ? hd_ctx_kernel_launches(g_ctx) : 0;
+  });
+  // the module context's CUDA stream (cudaStream_t as an integer), on which
+  // every call of this module runs: CUDA events recorded on it bracket calls
+  m.def("_stream", []() -> uintptr_t {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return reinterpret_cast<uintptr_t>(hd_ctx_stream(ctx()));
   });
 }

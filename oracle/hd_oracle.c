@@ -550,6 +550,52 @@ int hdo_from_fasta_dense(const char *buf, size_t nbytes, int remove_duplicates,
   return rc;
 }
 
+/* The same in one pass over the text, as the reference's from_fasta reads
+ * its file once (include/hamming/hamming.hh:168-178): the lower triangle is
+ * returned in *out (malloc'd, n(n-1)/2 entries of dtype_bytes, release with
+ * hdo_free) and, with remove_duplicates, the sequence indices in *indices.  */
+int hdo_from_fasta_dense_once(const char *buf, size_t nbytes, int remove_duplicates,
+                              uint64_t n_limit, int64_t max_distance, int dtype_bytes,
+                              void **out, uint64_t *n_rows, uint64_t **indices,
+                              uint64_t *n_input) {
+  char *seqs;
+  uint64_t *offsets, n, *idx;
+  *out = NULL;
+  *indices = NULL;
+  if (dtype_bytes != 1 && dtype_bytes != 2 && dtype_bytes != 4) return HDO_ERR_ARG;
+  int rc = hdo_read_fasta(buf, nbytes, remove_duplicates, n_limit, &seqs, &offsets, &n,
+                          &idx, n_input);
+  if (rc) return rc;
+  hdo_records r = {{seqs, offsets[n], 0}, offsets, n, 0};
+  rc = hdo_validate(&r);
+  *n_rows = n;
+  if (!rc) {
+    const uint64_t entries = n * (n - 1) / 2;
+    uint64_t L = offsets[1] - offsets[0];
+    uint64_t rb = hdo_packed_row_bytes(L);
+    uint8_t *packed = malloc(n * rb);
+    void *lt = malloc((entries ? entries : 1) * (uint64_t)dtype_bytes);
+    if (!packed || !lt) {
+      free(packed);
+      free(lt);
+      rc = HDO_ERR_ALLOC;
+    } else {
+#pragma omp parallel for
+      for (int64_t k = 0; k < (int64_t)n; ++k)
+        hdo_pack_row(seqs + offsets[k], L, packed + (uint64_t)k * rb);
+      rc = hdo_lt_dense(packed, n, rb, max_distance, dtype_bytes, lt);
+      free(packed);
+      if (rc) free(lt);
+      else *out = lt;
+    }
+  }
+  if (!rc) *indices = idx;
+  else free(idx);
+  free(seqs);
+  free(offsets);
+  return rc;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Writers.                                                                  */
 

@@ -69,6 +69,8 @@ def lib():
             L.hdo_distance.argtypes = [cp, u64, cp, u64, ctypes.c_int, P(ctypes.c_uint32)]
             L.hdo_from_fasta_dense.argtypes = [cp, ctypes.c_size_t, ctypes.c_int, u64, i64,
                                                ctypes.c_int, vp, u64, P(u64), vp, P(u64)]
+            L.hdo_from_fasta_dense_once.argtypes = [cp, ctypes.c_size_t, ctypes.c_int, u64, i64,
+                                                    ctypes.c_int, P(vp), P(u64), P(vp), P(u64)]
             L.hdo_format_lower_triangular.argtypes = [vp, u64, ctypes.c_int, vp]
             L.hdo_format_lower_triangular.restype = u64
             L.hdo_format_sparse.argtypes = [vp, u64, ctypes.c_int, i64, vp, P(u64)]
@@ -96,8 +98,8 @@ def _take(ptr: int, n: int, dtype) -> np.ndarray:
         if ptr:
             lib().hdo_free(ptr)
         return np.zeros(0, dtype=dtype)
-    buf = (ctypes.c_char * (n * np.dtype(dtype).itemsize)).from_address(ptr)
-    arr = np.frombuffer(bytes(buf), dtype=dtype).copy()
+    arr = np.empty(n, dtype=dtype)
+    ctypes.memmove(arr.ctypes.data, ptr, arr.nbytes)
     lib().hdo_free(ptr)
     return arr
 
@@ -173,20 +175,18 @@ def lt_dense(seqs, max_distance=255, dtype=np.uint8) -> np.ndarray:
 
 def from_fasta_dense(data: bytes, remove_duplicates=False, n=0, max_distance=255,
                      dtype=np.uint8):
-    """from_fasta(use_gpu=True) semantics on the CPU: (lt, sequence_indices)."""
-    L = lib()
-    nrows, nin = ctypes.c_uint64(), ctypes.c_uint64()
-    _check(L.hdo_from_fasta_dense(data, len(data), int(remove_duplicates), n, int(max_distance),
-                                  np.dtype(dtype).itemsize, None, 0, ctypes.byref(nrows), None,
-                                  ctypes.byref(nin)))
+    """from_fasta(use_gpu=True) semantics on the CPU: (lt, sequence_indices).
+    One pass over the text, as the reference's from_fasta
+    (include/hamming/hamming.hh:168-178) reads its file once."""
+    lt, nrows, idx, nin = ctypes.c_void_p(), ctypes.c_uint64(), ctypes.c_void_p(), ctypes.c_uint64()
+    _check(lib().hdo_from_fasta_dense_once(data, len(data), int(remove_duplicates), n,
+                                           int(max_distance), np.dtype(dtype).itemsize,
+                                           ctypes.byref(lt), ctypes.byref(nrows),
+                                           ctypes.byref(idx), ctypes.byref(nin)))
     m = nrows.value
-    out = np.zeros(max(m * (m - 1) // 2, 1), dtype=dtype)
-    idx = np.zeros(max(nin.value, 1), dtype=np.uint64)
-    _check(L.hdo_from_fasta_dense(data, len(data), int(remove_duplicates), n, int(max_distance),
-                                  np.dtype(dtype).itemsize, out.ctypes.data, out.size,
-                                  ctypes.byref(nrows), idx.ctypes.data if remove_duplicates else None,
-                                  ctypes.byref(nin)))
-    return out[: m * (m - 1) // 2], (idx[: nin.value] if remove_duplicates else np.zeros(0, np.uint64))
+    out = _take(lt.value, m * (m - 1) // 2, dtype)
+    ind = _take(idx.value, nin.value, np.uint64)
+    return out, (ind if remove_duplicates else np.zeros(0, np.uint64))
 
 
 def fasta_sequence_indices(data: bytes, n: int = 0) -> np.ndarray:

@@ -58,3 +58,16 @@ def test_reference_arm_other_ranks_exit_quietly():
                        env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_reference_arm_loads_no_product_code():
+    # the reference arm's workload generator and CPU pass must not import the
+    # product package (whose __init__ loads its native library)
+    code = ("import sys; sys.path.insert(0, %r); import bench; "
+            "s = bench.synth_module(); rows, root, _ = s.alignment(40, 300, seed=3, dup_frac=0.3); "
+            "fa = s.to_fasta(rows); lt, idx, rd, sec = bench.oracle_pass(fa, root.tobytes()); "
+            "assert len(idx) == 40 and len(rd) == 40 and lt.size > 0; "
+            "bad = [m for m in sys.modules if m.startswith('hammingdist')]; "
+            "assert not bad, bad" % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr

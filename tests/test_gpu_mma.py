@@ -137,3 +137,67 @@ def test_mma_views(ctx, row0, n):
     np.testing.assert_array_equal(got, want)
     v.free()
     sp.free()
+
+
+def _cap_rows(L, rng, mixed, n=130):
+    """n rows of length L whose match counts reach the length: one root with a
+    few substitutions and '-' runs at both ends ('-' against '-' carries the
+    largest plane products); with `mixed`, long '-' runs, rows all '-', rows
+    all 'N' (distance L under the AND rule) and rows over ACGT-N; without, a
+    low-diversity set (under 0.5% of sites off the consensus), on which the
+    reference CPU takes its sparse rule."""
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    root = acgt[rng.integers(0, 4, L)]
+    rows = []
+    for k in range(n):
+        if k < 100 or not mixed:
+            r = root.copy()
+            pos = rng.integers(0, L, 80)
+            r[pos] = acgt[rng.integers(0, 4, pos.size)]
+            a, b = rng.integers(0, L // 4 if mixed else L // 1000, 2)
+            r[:a] = ord("-")
+            r[L - b:] = ord("-")
+            if k % 10 == 3:
+                r[rng.integers(0, L, 40)] = ord("X")
+        elif k < 110:
+            r = np.full(L, ord("-"), np.uint8)
+        elif k < 115:
+            r = np.full(L, ord("N"), np.uint8)
+        else:
+            r = np.frombuffer(b"ACGT-N", np.uint8)[rng.integers(0, 6, L)]
+        rows.append(r.tobytes())
+    return rows
+
+
+@pytest.mark.parametrize("planes,L", [(4, 4_194_303), (5, 3_355_443), (6, 2_796_202)])
+def test_mma_exact_at_length_cap(ctx, planes, L):
+    # the engine takes alignments with P L < 2^24 (hd_mma.cu mma_eligible):
+    # at the largest such L, 130 rows (a full 128-row tile and part of the
+    # next), match counts near L and distances up to L in uint32 must equal
+    # the bit-plane engine's integer counts and the oracle's
+    from hammingdist_gb300 import abi
+
+    assert planes * L < 2**24 and planes * (L + 1) >= 2**24
+    seqs = _cap_rows(L, np.random.default_rng(planes), mixed=planes != 5)
+    if planes == 4:
+        aln = ctx.alignment_from_sequences(seqs)
+    else:
+        aln = ctx.alignment_from_sequences(seqs, include_x=planes == 6, semantics=abi.SEM_CPU)
+    assert aln.rule == {4: "and", 5: "sparse", 6: "sparse_x"}[planes]
+    got, want = _both(ctx, aln, dtype=np.uint32, max_distance=2**32 - 1)
+    np.testing.assert_array_equal(got, want)
+    if planes == 4:
+        assert got.max() == L  # an 'N' row against an all-'-' row
+    pick = [0, 1, 57, 99, 100, 110, 120, 129] if planes != 5 else [0, 1, 57, 98, 99, 129]
+    sub = [seqs[i] for i in pick]
+    g = np.array([got[pick[a] * (pick[a] - 1) // 2 + pick[b]]
+                  for a in range(len(pick)) for b in range(a)], dtype=np.uint32)
+    if planes == 4:
+        # the oracle's max_dist is a C int, as in the reference
+        np.testing.assert_array_equal(g, o.lt_dense(sub, max_distance=2**31 - 1, dtype=np.uint32))
+    else:
+        # the reference CPU's DataSet types end at uint16
+        ref, sparse = o.lt_cpu(sub, include_x=planes == 6, max_distance=65535, dtype=np.uint16)
+        assert sparse
+        np.testing.assert_array_equal(np.minimum(g, 65535), ref)
+    aln.free()
