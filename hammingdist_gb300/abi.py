@@ -489,7 +489,7 @@ class Context:
         return {"lop3_per_s": a.value, "popc_per_s": b.value, "mix_pair_sites_per_s": c.value}
 
     def measure_mma_peak(self):
-        """Dense FP8 tensor-core FLOP/s (hd_measure_mma_peak)."""
+        """Dense FP4 (kind::mxf4) tensor-core FLOP/s (hd_measure_mma_peak)."""
         f = ctypes.c_double()
         self._check(lib().hd_measure_mma_peak(self.h, ctypes.byref(f)))
         return f.value

@@ -1105,11 +1105,11 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         }
       }
       hd::pack_rows_and(ctx, all, rows + K, Kc - K, L, words, g0 + K * words);
-      // the new rows' FP8 operand, before the launches of any stream read it
-      if (use_mma && Kc >= 2 && !hd::ensure_fp8(ctx, owner.get(), Kc, ctx->stream, R_max)) {
+      // the new rows' tensor-core operand, before the launches of any stream read it
+      if (use_mma && Kc >= 2 && !hd::ensure_operand(ctx, owner.get(), Kc, ctx->stream, R_max)) {
         use_mma = false;
         T = (uint32_t)cfg.tile;
-        if (t_done) fail(HD_ERR_OOM, "no memory for the FP8 operand of a streamed call");
+        if (t_done) fail(HD_ERR_OOM, "no memory for the tensor-core operand of a streamed call");
       }
       hd::trace_mark(ctx, kPacked[c]);
       K = Kc;
@@ -1236,8 +1236,8 @@ int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, int64_
     // the tensor-core engine's operand and the launch plan (item lists,
     // tensor maps, job tables) first, so that the timing below is the
     // distance kernel's alone
-    if (!aln->base && hd::mma_eligible(aln) && hd::ensure_fp8(ctx, aln, n, ctx->stream))
-      hd::trace_mark(ctx, "FP8 operand");
+    if (!aln->base && hd::mma_eligible(aln) && hd::ensure_operand(ctx, aln, n, ctx->stream))
+      hd::trace_mark(ctx, "FP4 operand");
     hd::PairLaunchPlan plan;
     hd::plan_pairwise_tiles(ctx, aln, dtype_bytes, md, d_out, 0, 0, nb, &plan);
     HD_CUDA(cudaEventRecord(ctx->ev_start, ctx->stream));
@@ -1522,10 +1522,10 @@ int hd_distance(hd_ctx *ctx, const char *s0, uint64_t l0, const char *s1, uint64
   });
 }
 
-int hd_measure_mma_peak(hd_ctx *ctx, double *fp8_flop_per_s) {
-  if (!ctx || !fp8_flop_per_s) return HD_ERR_ARG;
+int hd_measure_mma_peak(hd_ctx *ctx, double *fp4_flop_per_s) {
+  if (!ctx || !fp4_flop_per_s) return HD_ERR_ARG;
   return guard(ctx, [&] {
-    *fp8_flop_per_s = hd::measure_mma_peak(ctx);
+    *fp4_flop_per_s = hd::measure_mma_peak(ctx);
     check_status(ctx);
   });
 }

@@ -151,11 +151,11 @@ struct hd_alignment {
   hd::DevBuf plane_buf[2];
   std::vector<uint64_t> seqidx;  // host, n_input entries (empty = identity)
   hd::DevBuf d_seqidx;           // device copy (serving / reference queries)
-  // FP8 operand of the tensor-core engine (hd_mma.cu), rows [0, fp8_rows)
-  // expanded so far out of fp8_cap; built on first use, freed with the
+  // E2M1 (FP4) operand of the tensor-core engine (hd_mma.cu), rows [0, op_rows)
+  // expanded so far out of op_cap; built on first use, freed with the
   // alignment
-  mutable hd::DevBuf fp8;
-  mutable uint64_t fp8_rows = 0, fp8_cap = 0;
+  mutable hd::DevBuf op;
+  mutable uint64_t op_rows = 0, op_cap = 0;
   // Freed on the null stream: every API call has synchronised its own stream
   // before returning, so no queued work still reads these buffers, and the
   // creating context (and its streams) may already be gone.
@@ -166,7 +166,7 @@ struct hd_alignment {
   }
   ~hd_alignment() {
     cudaSetDevice(device);
-    for (auto *b : {&plane_buf[0], &plane_buf[1], &d_seqidx, &fp8}) {
+    for (auto *b : {&plane_buf[0], &plane_buf[1], &d_seqidx, &op}) {
       b->s = nullptr;
       b->release();
     }
@@ -454,10 +454,10 @@ TileConfig tile_config_for(hd_ctx *ctx, uint64_t n_rows, uint64_t length, int dt
 // mma.cu: the tensor-core engine for every rule (4, 5 or 6 planes, with
 // P L < 2^24; HAMMINGDIST_KERNEL=lop3 turns it off).
 bool mma_eligible(const hd_alignment *aln);
-// expands rows [fp8_rows, rows) of the alignment's planes into its FP8
+// expands rows [op_rows, rows) of the alignment's planes into its E2M1
 // operand on `stream` (room for cap_hint rows if it must grow); false if the
 // operand cannot be allocated
-bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream,
+bool ensure_operand(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream,
                 uint64_t cap_hint = 0);
 // tile rows [tile_lo, tile_hi) (128 rows each) x all earlier columns into
 // d_out (lt index out_base at d_out[0]) on `stream`; sm_limit > 0 caps the
@@ -466,7 +466,7 @@ bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_
 bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
                   void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi,
                   cudaStream_t stream, int sm_limit);
-// FP8 dense MMA rate (FLOP/s) of this device from shared-memory operands
+// dense FP4 (kind::mxf4) MMA rate (FLOP/s) of this device from shared-memory operands
 double measure_mma_peak(hd_ctx *ctx);
 // One tensor-core launch for the specs it can take (dense AND rule, row
 // range starting on a 128-row tile, operand memory available); taken[k] marks

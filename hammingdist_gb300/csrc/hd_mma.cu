@@ -1,5 +1,5 @@
-// Tensor-core lower-triangle distances (tcgen05, FP8) for the dense AND rule
-// and the sparse rules.
+// Tensor-core lower-triangle distances (tcgen05, block-scaled FP4) for the
+// dense AND rule and the sparse rules.
 //
 // Replaces the reference's Dist<T> kernel (src/distance_cuda.cu:9-202) and,
 // for use_gpu=False, its CPU loops (include/hamming/hamming_impl.hh:120-175).
@@ -16,33 +16,36 @@
 // P for '-' against '-' (hence the -(P - 1)), and 0 otherwise. Summed over
 // the sites of two rows this is one dot product of P + 1 values per site, the
 // dash value being 1 on the row side and -(P - 1) on the column side. All
-// values are 0, 1, -3, -4 or -5: exact in FP8 (E4M3) with FP32 accumulation
-// while P L < 2^24. mismatches = L - matches.
+// values are 0, 1, -3 or -4, exact in E2M1 (FP4: 0, 0.5, 1, 1.5, 2, 3, 4, 6
+// and their negatives); -5 (P = 6) is not, so there the column side's dash
+// is -4 and -1 in two blocks, each paired with the row side's +1. The MMAs
+// are kind::mxf4 with every UE8M0 scale factor 1.0 and FP32 accumulation,
+// exact while P L < 2^24. mismatches = L - matches.
 //
 // Operand (one buffer serves rows and columns): each row's bit planes are
-// expanded to (P + 2) x 32 bytes per 32-site word, K-major: for every 128
-// sites, P + 2 blocks of 128 bytes, the P planes, the dash as 1 (read for
-// rows) and the dash as -(P - 1) (read for columns); sites past L are 0. An
-// alignment caches its operand; a view of a resident alignment (a serving
-// window) gets one of its own rows.
+// expanded to packed E2M1, two sites per byte, K-major: for every 256 sites,
+// the P planes (1.0), the dash as 1.0 (read for rows) and the dash as -(P - 1)
+// (read for columns; -4 and -1 for P = 6), 128 bytes each; sites past L are
+// 0. An alignment caches its operand; a view of a resident alignment (a
+// serving window) gets one of its own rows.
 //
 // One launch serves a job table of matrices. Persistent CTAs (320 threads,
-// one per SM) walk a list of items: 256 columns J x one or two 128-row tiles
+// one per SM) walk a list of items: 224 columns J x one or two 128-row tiles
 // I of one job, in bands of 16 tile rows, column-major within a band, so
 // resident CTAs share operands in L2; the list ends with single-row-tile items
 // so that every CTA gets the same work to within a row tile.
 //  * warp 0 (one thread) issues TMA loads (128-byte swizzle) per stage of
-//    one 128-byte K block of the item's 128 or 256 rows and 256 columns,
-//    3 stages of 64 KB with full/empty mbarriers; warp 0 also allocates and
-//    frees the TMEM;
-//  * warp 1 (one thread) issues tcgen05.mma.cta_group::1.kind::f8f6f4
-//    (M=128, N=256, K=32), four per row tile per stage, into TMEM (row tile
-//    h of the item at columns 256 h), so each column stage feeds up to eight
-//    MMAs; each stage's MMAs are committed to its empty barrier, an item's
-//    last ones to the `done` barrier;
-//  * warps 2-9, two per TMEM lane quarter, each read 32 rows x 128 columns
-//    of each accumulator (tcgen05.ld, 64 columns at a time), form
-//    min(L - matches, max_dist) (safe_int_cast,
+//    one 128-byte K block (256 sites) of the item's 128 or 256 rows and 224
+//    columns, 3 stages of 60 KB with full/empty mbarriers; warp 0 also
+//    allocates and frees the TMEM;
+//  * warp 1 (one thread) issues tcgen05.mma.cta_group::1.kind::mxf4
+//    .block_scale (M=128, N=224, K=64), four per row tile per stage, into
+//    TMEM (row tile h of the item at columns 256 h); the unit scale factors
+//    sit in TMEM columns 224-255, written once per CTA. Each stage's MMAs are
+//    committed to its empty barrier, an item's last ones to `done`;
+//  * warps 2-9, two per TMEM lane quarter, each read 32 rows x 128 or 96
+//    columns of each accumulator (tcgen05.ld, 64 or 32 columns at a time),
+//    form min(L - matches, max_dist) (safe_int_cast,
 //    include/hamming/hamming_impl.hh:37-45), turn each 32 x 32 chunk around
 //    in a padded shared buffer and store it row by row, 32 consecutive
 //    entries of the job's dtype per store; they then release the
@@ -62,16 +65,18 @@
 namespace hd {
 namespace {
 
-constexpr int kEpiWarps = 8;      // two per TMEM lane quarter, one per 128 columns
+constexpr int kEpiWarps = 8;      // two per TMEM lane quarter
 constexpr int kMmaThreads = 64 + 32 * kEpiWarps;  // warp 0: TMA, warp 1: MMA, warps 2-9: epilogue
 constexpr int kEpiThreads = 32 * kEpiWarps;
 constexpr int kMmaStages = 3;
-constexpr int kTM = 128, kTN = 256;                   // MMA tile: rows x columns
-constexpr uint32_t kEpiCols = kTN / (kEpiWarps / 4);  // accumulator columns per epilogue warp
+constexpr int kTM = 128, kTN = 224;                   // MMA tile: rows x columns
+constexpr uint32_t kEpiSplit = 128;                   // epilogue halves: [0, 128), [128, kTN)
+constexpr uint32_t kSfCol = 224;                      // TMEM columns 224-255: scale factors
+constexpr uint32_t kSfWord = 0x7F7F7F7Fu;             // four UE8M0 scale factors of 2^0
 constexpr uint32_t kHalfBytes = kTM * 128;            // one 128-byte K block of 128 rows
 constexpr uint32_t kABytes = 2 * kHalfBytes;          // up to two row tiles
 constexpr uint32_t kBBytes = kTN * 128;
-constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 64 KB
+constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 60 KB
 constexpr uint32_t kEpiPitch = 33;                    // words per row of an epilogue chunk
 constexpr uint32_t kEpiBytes = kEpiWarps * 32 * kEpiPitch * 4;  // 32 x 32 words per epilogue warp
 constexpr int kMmaSmem = kMmaStages * kStageBytes + kEpiBytes + 1024;
@@ -79,32 +84,47 @@ constexpr uint32_t kTmemCols = 512;                   // row tile h at columns 2
 constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
 constexpr uint64_t kMmaMinItems = 48;                 // HAMMINGDIST_MMA_MIN_ITEMS overrides
 constexpr uint32_t kMmaBand = 16;  // tile rows per L2 band (HAMMINGDIST_MMA_BAND overrides)
-// operand bytes per 32-site word: P planes + the two dash blocks, 32 B each
+// 128-byte blocks per 256 sites of the operand: the P planes, the row side's
+// dash and the column side's dash (two blocks for P = 6: -4 and -1)
+__host__ __device__ constexpr uint32_t op_blocks(uint32_t planes) {
+  return planes + (planes == 6 ? 3u : 2u);
+}
+// K blocks per 256 sites and side: the planes and the dash products
+__host__ __device__ constexpr uint32_t op_kblocks(uint32_t planes) {
+  return planes + (planes == 6 ? 2u : 1u);
+}
+// operand bytes per 32-site word: 16 bytes (32 sites of E2M1) per block
 __host__ __device__ constexpr uint64_t row_bytes_per_word(uint32_t planes) {
-  return (uint64_t)(planes + 2) * 32;
+  return (uint64_t)op_blocks(planes) * 16;
 }
-// the column side's dash value -(P - 1) in E4M3: -3 (0xC4), -4 (0xC8), -5 (0xCA)
-__device__ __forceinline__ uint32_t dash_neg(uint32_t planes) {
-  return planes == 4 ? 0xC4u : planes == 5 ? 0xC8u : 0xCAu;
+// E2M1 codes: 1.0, and the column side's -(P - 1): -3 for P = 4, -4 else
+// (then -1 for P = 6)
+constexpr uint32_t kE2M1One = 0x2u, kE2M1Neg1 = 0xAu;
+__device__ __forceinline__ uint32_t dash_neg(uint32_t planes) { return planes == 4 ? 0xDu : 0xEu; }
+// instruction descriptor (block-scaled kinds): A and B E2M1 (1 at bits 7-9
+// and 10-12), both K-major, N >> 3 at bits 17-22, scale factors UE8M0 (bit
+// 23), M >> 4 at bits 24-28, scale factor ids 0, K = 64; D is FP32
+__host__ __device__ constexpr uint32_t idesc_mxf4(uint32_t n) {
+  return (1u << 7) | (1u << 10) | ((n >> 3) << 17) | (1u << 23) | ((uint32_t)(kTM >> 4) << 24);
 }
-// instruction descriptor: D F32 (bits 4-5 = 1), A and B E4M3 (0), both
-// K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28
-constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t)(kTN >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+constexpr uint32_t kIdesc = idesc_mxf4(kTN);
 
 }  // namespace
 
 // One matrix of a launch (device copy): its operand's tensor maps (boxes of
-// 256 and 128 rows) and its output.
+// 256 and 128 rows for the row side, kTN rows for the column side) and its
+// output.
 struct MmaJob {
   const CUtensorMap *tm256;
   const CUtensorMap *tm128;
+  const CUtensorMap *tmb;
   void *out;                     // lt index out_base at out[0]
   unsigned long long out_base;
   uint32_t n, nkb, sites, max_dist, dtype;  // rows, K blocks per side, L, cap, 1/2/4 bytes
-  uint32_t planes;                          // P: P + 1 K blocks per 128 sites and side
+  uint32_t planes;                          // P: op_kblocks(P) K blocks per 256 sites and side
 };
 
-// One work item: 256 columns J x row tiles [I, I + halves) of job `job`.
+// One work item: kTN columns J x row tiles [I, I + halves) of job `job`.
 struct MmaItem {
   uint32_t job;
   uint32_t I;       // first 128-row tile
@@ -114,27 +134,32 @@ struct MmaItem {
 
 namespace {
 
-// 4 bits -> 4 bytes, each `one` (an FP8 value) or 0
-__device__ __forceinline__ uint32_t spread4(uint32_t nib, uint32_t one) {
-  return ((nib * 0x00204081u) & 0x01010101u) * one;
+// 8 bits -> 8 nibbles (bit i -> the low bit of nibble i), times the E2M1
+// code `v` (no carries: each nibble is 0 or 1 before the multiply)
+__device__ __forceinline__ uint32_t nib8(uint32_t b, uint32_t v) {
+  b = (b | (b << 12)) & 0x000F000Fu;
+  b = (b | (b << 6)) & 0x03030303u;
+  b = (b | (b << 3)) & 0x11111111u;
+  return b * v;
 }
-__device__ __forceinline__ void put32(uint8_t *dst, uint32_t b, uint32_t one) {
-  uint4 *d = reinterpret_cast<uint4 *>(dst);
-  d[0] = make_uint4(spread4(b & 15u, one), spread4((b >> 4) & 15u, one),
-                    spread4((b >> 8) & 15u, one), spread4((b >> 12) & 15u, one));
-  d[1] = make_uint4(spread4((b >> 16) & 15u, one), spread4((b >> 20) & 15u, one),
-                    spread4((b >> 24) & 15u, one), spread4(b >> 28, one));
+// 32 sites (one plane word) -> 16 bytes of E2M1: site s in nibble s (byte
+// s / 2, low nibble for even s), `v` where the bit is set, else 0
+__device__ __forceinline__ void put16(uint8_t *dst, uint32_t w, uint32_t v) {
+  *reinterpret_cast<uint4 *>(dst) =
+      make_uint4(nib8(w & 0xFFu, v), nib8((w >> 8) & 0xFFu, v), nib8((w >> 16) & 0xFFu, v),
+                 nib8(w >> 24, v));
 }
 
 // Rows [row_lo, row_hi) of a P-plane alignment (P = 4: the AND rule; 5, 6:
-// the sparse rules, planes 4-5 in the second group) -> FP8 operand rows.
-// One thread per (row, 32-site word): 16 or 32 bytes read, (P + 2) x 32
-// bytes written. The dash is the AND of the P planes ('-' has every plane).
-__global__ void k_expand_fp8(const uint4 *__restrict__ g0, const uint4 *__restrict__ g1,
-                             uint32_t planes, uint64_t words, uint64_t row_lo, uint64_t row_hi,
-                             uint64_t L, uint8_t *__restrict__ x) {
+// the sparse rules, planes 4-5 in the second group) -> E2M1 operand rows.
+// One thread per (row, 32-site word): 16 or 32 bytes read, 16 bytes written
+// per block; eight consecutive words fill each 128-byte block of their 256
+// sites. The dash is the AND of the P planes ('-' has every plane).
+__global__ void k_expand_op(const uint4 *__restrict__ g0, const uint4 *__restrict__ g1,
+                            uint32_t planes, uint64_t words, uint64_t row_lo, uint64_t row_hi,
+                            uint64_t L, uint8_t *__restrict__ x) {
   const uint64_t total = (row_hi - row_lo) * words;
-  const uint32_t nb = planes + 2;  // 128-byte blocks per 128 sites
+  const uint32_t nb = op_blocks(planes);  // 128-byte blocks per 256 sites
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
        t += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t r = row_lo + t / words, w = t % words;
@@ -145,15 +170,16 @@ __global__ void k_expand_fp8(const uint4 *__restrict__ g0, const uint4 *__restri
     uint32_t dash = p.x & p.y & p.z & p.w & valid;
     if (planes > 4) dash &= p1.x;
     if (planes > 5) dash &= p1.y;
-    uint8_t *blk = x + r * (words * row_bytes_per_word(planes)) + (w / 4) * (nb * 128) + (w % 4) * 32;
-    put32(blk, p.x & valid, 0x38u);
-    put32(blk + 128, p.y & valid, 0x38u);
-    put32(blk + 256, p.z & valid, 0x38u);
-    put32(blk + 384, p.w & valid, 0x38u);
-    if (planes > 4) put32(blk + 512, p1.x & valid, 0x38u);
-    if (planes > 5) put32(blk + 640, p1.y & valid, 0x38u);
-    put32(blk + planes * 128, dash, 0x38u);               // 1.0: the row side
-    put32(blk + (planes + 1) * 128, dash, dash_neg(planes));  // -(P - 1): the column side
+    uint8_t *blk = x + r * (words * row_bytes_per_word(planes)) + (w / 8) * (nb * 128) + (w % 8) * 16;
+    put16(blk, p.x & valid, kE2M1One);
+    put16(blk + 128, p.y & valid, kE2M1One);
+    put16(blk + 256, p.z & valid, kE2M1One);
+    put16(blk + 384, p.w & valid, kE2M1One);
+    if (planes > 4) put16(blk + 512, p1.x & valid, kE2M1One);
+    if (planes > 5) put16(blk + 640, p1.y & valid, kE2M1One);
+    put16(blk + planes * 128, dash, kE2M1One);                // 1.0: the row side
+    put16(blk + (planes + 1) * 128, dash, dash_neg(planes));  // the column side
+    if (planes == 6) put16(blk + (planes + 2) * 128, dash, kE2M1Neg1);
   }
 }
 
@@ -185,14 +211,29 @@ __device__ __forceinline__ void tc_before_sync() {
 __device__ __forceinline__ void tc_after_sync() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
-                                       uint32_t accumulate) {
+// D (+)= A B^T over K = 64 E2M1 values, every block of 32 scaled by the UE8M0
+// factors at TMEM addresses sfa and sfb
+__device__ __forceinline__ void mma_f4(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                       uint32_t idesc, uint32_t accumulate, uint32_t sfa,
+                                       uint32_t sfb) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(kIdesc), "r"(accumulate)
+      "tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%5], "
+      "[%6], p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate), "r"(sfa), "r"(sfb)
       : "memory");
+}
+// The unit scale factors: this warp writes kSfWord to the 32 TMEM columns
+// from col0 in its lane quarter (lane base `t_lane`) and waits for the
+// stores; the caller fences before the MMAs read them.
+__device__ __forceinline__ void write_unit_scales(uint32_t t_lane, uint32_t col0) {
+#pragma unroll
+  for (uint32_t c = col0; c < col0 + 32; c += 4)
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(t_lane + c),
+                 "r"(kSfWord), "r"(kSfWord), "r"(kSfWord), "r"(kSfWord)
+                 : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 // arrives on `bar` once every earlier tcgen05.mma of this thread has completed
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
@@ -226,14 +267,29 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&v)[64]) {
       : "r"(taddr)
       : "memory");
 }
+// 32 lanes x 32 consecutive 32-bit columns
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {"
+      "%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, "
+      "%19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31 "
+      "}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr)
+      : "memory");
+}
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 // min(sites - matches, max_dist) of accumulator columns OFF .. OFF + 31
 // (FP32 integers) into the warp's buffer, row `lane` at words 33 lane
-template <int OFF>
-__device__ __forceinline__ void turn_chunk(uint32_t *buf, const uint32_t (&d)[64], uint32_t sites,
+template <int OFF, int N>
+__device__ __forceinline__ void turn_chunk(uint32_t *buf, const uint32_t (&d)[N], uint32_t sites,
                                            uint32_t max_dist, uint32_t lane) {
 #pragma unroll
   for (uint32_t j = 0; j < 32; ++j) {
@@ -258,12 +314,12 @@ __device__ __forceinline__ void store_chunk(T *out, unsigned long long e0, uint3
 }
 
 // One epilogue warp's share of an item: TMEM lanes of its quarter (rows
-// 32 sub + lane of each row tile) x its columns [c_lo, c_lo + kEpiCols),
-// read 64 columns at a time.
+// 32 sub + lane of each row tile) x its columns [c_lo, c_hi), read 64
+// columns at a time (32 for a last piece of 32).
 template <typename T>
 __device__ __forceinline__ void epilogue_share(const MmaItem &tl, const MmaJob &job,
-                                               uint32_t t_lane, uint32_t c_lo, uint32_t sub,
-                                               uint32_t lane, uint32_t *buf) {
+                                               uint32_t t_lane, uint32_t c_lo, uint32_t c_hi,
+                                               uint32_t sub, uint32_t lane, uint32_t *buf) {
   const uint32_t n = job.n, sites = job.sites, max_dist = job.max_dist;
   T *out = static_cast<T *>(job.out);
   for (uint32_t h = 0; h < tl.halves; ++h) {
@@ -272,11 +328,21 @@ __device__ __forceinline__ void epilogue_share(const MmaItem &tl, const MmaJob &
     const uint32_t rows = n - i0 < 32u ? n - i0 : 32u;
     const unsigned long long t0 = (unsigned long long)i0 * (i0 - 1) / 2 - job.out_base + lane;
 #pragma unroll 1
-    for (uint32_t c = c_lo; c < c_lo + kEpiCols; c += 64) {
+    for (uint32_t c = c_lo; c < c_hi; c += 64) {
       const uint32_t j0 = tl.J * kTN + c;  // first column of this group
       if (j0 + 1 >= i0 + rows) break;      // no row reaches column j0 (warp-uniform)
-      uint32_t d[64];
       __syncwarp();
+      if (c + 64 > c_hi) {  // a last piece of 32 columns
+        uint32_t d[32];
+        tmem_ld32(t_lane + 256u * h + c, d);
+        tmem_ld_wait();
+        turn_chunk<0>(buf, d, sites, max_dist, lane);
+        __syncwarp();
+        store_chunk<T>(out, t0 + j0, i0, rows, j0, buf, lane);
+        __syncwarp();
+        break;
+      }
+      uint32_t d[64];
       tmem_ld64(t_lane + 256u * h + c, d);
       tmem_ld_wait();
       turn_chunk<0>(buf, d, sites, max_dist, lane);
@@ -321,6 +387,11 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   __syncthreads();
   tc_after_sync();
   const uint32_t tmem = s_tmem;
+  // the unit scale factors, once per CTA: warps 2-5 cover the lane quarters
+  if (warp >= 2 && warp < 6) write_unit_scales(tmem + (((warp & 3u) * 32) << 16), kSfCol);
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
 
   if (warp == 0) {
     if (lane == 0) {
@@ -332,9 +403,10 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
         const MmaJob &job = jobs[tl.job];
         const CUtensorMap *ta = tl.halves == 2 ? job.tm256 : job.tm128;
         prefetch_tmap(ta);
-        prefetch_tmap(job.tm256);
+        prefetch_tmap(job.tmb);
         const int32_t ya = (int32_t)(tl.I * kTM), yb = (int32_t)(tl.J * kTN);
         const uint32_t bytes = kBBytes + tl.halves * kHalfBytes, nkb = job.nkb, P = job.planes;
+        const uint32_t Q = op_kblocks(P), NB = op_blocks(P);
         for (uint32_t kb = 0; kb < nkb; ++kb) {
           const uint32_t s = g % kMmaStages;
           if ((g >= (uint32_t)kMmaStages &&
@@ -343,16 +415,16 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
             ok = false;
             break;
           }
-          // K block kb: 128 sites of chunk kb / (P + 1), block kb % (P + 1)
-          // (planes 0 .. P-1, then the dash: the +1 block for the rows, the
-          // -(P - 1) block for the columns)
-          const uint32_t c = kb / (P + 1), q = kb % (P + 1);
-          const int32_t xa = (int32_t)(((P + 2) * c + q) * 128);
-          const int32_t xb = (int32_t)(((P + 2) * c + (q == P ? P + 1 : q)) * 128);
+          // K block kb: 256 sites of chunk kb / Q, block kb % Q (planes 0 ..
+          // P-1, then the dash: the +1 block for the rows, the -(P - 1) block
+          // for the columns; for P = 6 the +1 block twice, against -4 and -1)
+          const uint32_t c = kb / Q, q = kb % Q;
+          const int32_t xa = (int32_t)((NB * c + (q < P ? q : P)) * 128);
+          const int32_t xb = (int32_t)((NB * c + (q < P ? q : q + 1)) * 128);
           uint8_t *st = smem + s * kStageBytes;
           mbar_expect_tx(&full[s], bytes);
           tma_load_2d(st, ta, xa, ya, &full[s]);
-          tma_load_2d(st + kABytes, job.tm256, xb, yb, &full[s]);
+          tma_load_2d(st + kABytes, job.tmb, xb, yb, &full[s]);
           ++g;
         }
       }
@@ -391,7 +463,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
             const uint64_t ad = sw128_desc(a0 + h * kHalfBytes);
 #pragma unroll
             for (uint32_t k = 0; k < 4; ++k)  // 32 bytes of K per MMA: +2 in 16-byte units
-              mma_f8(tmem + 256u * h, ad + 2 * k, bd + 2 * k, (kb | k) ? 1u : 0u);
+              mma_f4(tmem + 256u * h, ad + 2 * k, bd + 2 * k, kIdesc, (kb | k) ? 1u : 0u,
+                     tmem + kSfCol, tmem + kSfCol + 16);
           }
           mma_commit(&empty[s]);
           ++g;
@@ -411,12 +484,12 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   } else {
     // epilogue warps 2 .. 2 + kEpiWarps - 1: warp w reads TMEM lanes
     // 32 (w % 4) .. + 31, which are rows 32 (w % 4) + lane of each row tile
-    // of the item, in columns kEpiCols ((w - 2) / 4) .. + kEpiCols - 1. Each
+    // of the item, in columns [0, 128) (w < 6) or [128, kTN) (w >= 6). Each
     // 32 x 32 chunk goes through the warp's padded shared buffer (row r at
     // words 33 r: conflict-free both ways), so that one store instruction
     // writes 32 consecutive entries of one row rather than one entry of 32
     // rows.
-    const uint32_t sub = warp & 3u, c_lo = ((warp - 2) / 4) * kEpiCols;
+    const uint32_t sub = warp & 3u, c_lo = warp < 6 ? 0u : kEpiSplit, c_hi = warp < 6 ? kEpiSplit : (uint32_t)kTN;
     const uint32_t t_lane = tmem + ((sub * 32) << 16);
     uint32_t *buf = reinterpret_cast<uint32_t *>(smem + kMmaStages * kStageBytes) +
                     (warp - 2) * 32 * kEpiPitch;
@@ -433,11 +506,11 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       const MmaItem tl = items[t];
       const MmaJob &job = jobs[tl.job];
       if (job.dtype == 1)
-        epilogue_share<uint8_t>(tl, job, t_lane, c_lo, sub, lane, buf);
+        epilogue_share<uint8_t>(tl, job, t_lane, c_lo, c_hi, sub, lane, buf);
       else if (job.dtype == 2)
-        epilogue_share<uint16_t>(tl, job, t_lane, c_lo, sub, lane, buf);
+        epilogue_share<uint16_t>(tl, job, t_lane, c_lo, c_hi, sub, lane, buf);
       else
-        epilogue_share<uint32_t>(tl, job, t_lane, c_lo, sub, lane, buf);
+        epilogue_share<uint32_t>(tl, job, t_lane, c_lo, c_hi, sub, lane, buf);
       // the accumulators may be overwritten
       tc_before_sync();
       mbar_arrive(&tmem_free);
@@ -452,16 +525,18 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   }
 }
 
-// FP8 MMA rate from shared memory alone (no loads): one CTA per SM (the
-// shared-memory request keeps it alone) issues `rounds` x 4 MMAs of M=128,
-// N=256, K=32 on a zeroed stage (the values do not change the rate).
+// FP4 (kind::mxf4) MMA rate from shared memory alone (no loads): one CTA per
+// SM (the shared-memory request keeps it alone) issues `rounds` x 4 MMAs of
+// M=128, N=256, K=64 on a zeroed stage (the values do not change the rate),
+// with unit scale factors in TMEM columns 256-287.
+constexpr uint32_t kPeakN = 256, kPeakSf = 256;
 __global__ void __launch_bounds__(128, 1) k_peak_mma(uint32_t rounds, int *status) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t s_tmem;
   uint8_t *smem =
       reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  for (uint32_t k = threadIdx.x; k < kStageBytes / 16; k += blockDim.x)
+  for (uint32_t k = threadIdx.x; k < (kABytes + kPeakN * 128) / 16; k += blockDim.x)
     reinterpret_cast<uint4 *>(smem)[k] = make_uint4(0, 0, 0, 0);
   // the generic-proxy writes above, before the tensor cores read them
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -477,12 +552,18 @@ __global__ void __launch_bounds__(128, 1) k_peak_mma(uint32_t rounds, int *statu
   __syncthreads();
   tc_after_sync();
   const uint32_t tmem = s_tmem;
+  write_unit_scales(tmem + (((threadIdx.x >> 5) * 32) << 16), kPeakSf);
+  tc_before_sync();
+  __syncthreads();
+  tc_after_sync();
   if (threadIdx.x == 0) {
     const uint32_t a0 = smem_u32(smem);
     const uint64_t ad = sw128_desc(a0), bd = sw128_desc(a0 + kABytes);
     for (uint32_t r = 0; r < rounds; ++r)
 #pragma unroll
-      for (uint32_t k = 0; k < 4; ++k) mma_f8(tmem, ad + 2 * k, bd + 2 * k, (r | k) ? 1u : 0u);
+      for (uint32_t k = 0; k < 4; ++k)
+        mma_f4(tmem, ad + 2 * k, bd + 2 * k, idesc_mxf4(kPeakN), (r | k) ? 1u : 0u,
+               tmem + kPeakSf, tmem + kPeakSf + 16);
     mma_commit(&bar);
     if (!mbar_wait_bounded(&bar, 0, 4 * kMmaWaitNs)) atomicExch(status, kStatusTmaTimeout);
   }
@@ -532,13 +613,13 @@ bool mma_eligible(const hd_alignment *aln) {
          aln->n_rows < (1ull << 31);
 }
 
-bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream,
+bool ensure_operand(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_t stream,
                 uint64_t cap_hint) {
   const hd_alignment *o = aln->base ? aln->base : aln;
-  if (o->fp8_rows >= rows) return true;
+  if (o->op_rows >= rows) return true;
   const uint32_t P = (uint32_t)o->planes;
   const uint64_t words = o->words, rb = words * row_bytes_per_word(P);
-  if (rows > o->fp8_cap) {
+  if (rows > o->op_cap) {
     // room for the rows asked for, or for what the caller says will come
     const uint64_t plane_rows = o->plane_buf[0].bytes / (words * 16);
     const uint64_t cap = std::max(rows, std::min(cap_hint, plane_rows));
@@ -550,22 +631,22 @@ bool ensure_fp8(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStream_
       cudaGetLastError();
       return false;  // the bit-plane engine needs no extra memory
     }
-    if (o->fp8_rows) {
-      HD_CUDA(cudaMemcpyAsync(grown.p, o->fp8.p, o->fp8_rows * rb, cudaMemcpyDeviceToDevice, stream));
+    if (o->op_rows) {
+      HD_CUDA(cudaMemcpyAsync(grown.p, o->op.p, o->op_rows * rb, cudaMemcpyDeviceToDevice, stream));
       // launches on the context's other streams may still read the old
       // operand: they finish before it is freed
       for (cudaStream_t st : {ctx->side, ctx->side2, ctx->stream}) HD_CUDA(cudaStreamSynchronize(st));
     }
-    o->fp8 = std::move(grown);
-    o->fp8_cap = cap;
+    o->op = std::move(grown);
+    o->op_cap = cap;
   }
-  const uint64_t total = (rows - o->fp8_rows) * words;
+  const uint64_t total = (rows - o->op_rows) * words;
   const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
-  k_expand_fp8<<<(unsigned)grid, 256, 0, stream>>>(
+  k_expand_op<<<(unsigned)grid, 256, 0, stream>>>(
       o->plane_buf[0].as<uint4>(), P > 4 ? o->plane_buf[1].as<uint4>() : nullptr, P, words,
-      o->fp8_rows, rows, o->length, o->fp8.as<uint8_t>());
+      o->op_rows, rows, o->length, o->op.as<uint8_t>());
   HD_LAUNCHED(ctx);
-  o->fp8_rows = rows;
+  o->op_rows = rows;
   return true;
 }
 
@@ -586,11 +667,11 @@ double measure_mma_peak(hd_ctx *ctx) {
   HD_CUDA(cudaStreamSynchronize(ctx->stream));
   float ms = 0;
   HD_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
-  const double flop = (double)ctx->sm_count * rounds * 4 * 2.0 * kTM * kTN * 32;
+  const double flop = (double)ctx->sm_count * rounds * 4 * 2.0 * kTM * kPeakN * 64;
   return flop / (ms / 1e3);
 }
 
-// The FP8 operand rows of a job: the alignment's own cache (an alignment, or
+// The E2M1 operand rows of a job: the alignment's own cache (an alignment, or
 // a view at row 0 of a base whose cache already holds its rows: the streamed
 // from_fasta), else the view's rows expanded into a buffer the plan keeps
 // until the kernel has run (a serving window must not expand a large base).
@@ -599,12 +680,12 @@ bool operand_for(hd_ctx *ctx, const hd_alignment *a, cudaStream_t stream, PairLa
                  const uint8_t *&op) {
   const hd_alignment *o = a->base ? a->base : a;
   if (!a->base) {
-    if (!ensure_fp8(ctx, a, a->n_rows, stream)) return false;
-    op = a->fp8.as<uint8_t>();
+    if (!ensure_operand(ctx, a, a->n_rows, stream)) return false;
+    op = a->op.as<uint8_t>();
     return true;
   }
-  if (a->row0 == 0 && o->fp8.p && o->fp8_rows >= a->n_rows) {
-    op = o->fp8.as<uint8_t>();
+  if (a->row0 == 0 && o->op.p && o->op_rows >= a->n_rows) {
+    op = o->op.as<uint8_t>();
     return true;
   }
   const uint32_t P = (uint32_t)o->planes;
@@ -620,7 +701,7 @@ bool operand_for(hd_ctx *ctx, const hd_alignment *a, cudaStream_t stream, PairLa
   }
   const uint64_t total = a->n_rows * o->words;
   const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
-  k_expand_fp8<<<(unsigned)grid, 256, 0, stream>>>(
+  k_expand_op<<<(unsigned)grid, 256, 0, stream>>>(
       static_cast<const uint4 *>(a->planes_ptr(0)),
       P > 4 ? static_cast<const uint4 *>(a->planes_ptr(1)) : nullptr, P, o->words, 0, a->n_rows,
       o->length, tmp.as<uint8_t>());
@@ -641,7 +722,7 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
   };
   std::vector<Job> js;
   // A launch with few items leaves SMs idle: below kMmaMinItems single row
-  // tiles (128 x 256) in all, the bit-plane engine's finer tiles finish first
+  // tiles (128 x kTN) in all, the bit-plane engine's finer tiles finish first
   // (its rate is a third, but it fills the SMs); a batch of small matrices
   // still goes here when together they are enough.
   uint64_t min_items = kMmaMinItems;
@@ -674,7 +755,7 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
   uint32_t band = kMmaBand;
   if (const char *e = std::getenv("HAMMINGDIST_MMA_BAND")) band = (uint32_t)std::max(2, std::atoi(e)) & ~1u;
   // Items of each job: pairs of 128-row tiles (a single one where a range is
-  // odd) x 256-column tiles up to the last column any of their rows needs, in
+  // odd) x kTN-column tiles up to the last column any of their rows needs, in
   // bands of `band` tile rows, column-major within a band.
   std::vector<MmaItem> list;
   for (uint32_t q = 0; q < (uint32_t)js.size(); ++q)
@@ -684,8 +765,13 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
       for (uint32_t J = 0; J < j_end; ++J)
         for (uint32_t I = b; I < e; I += 2) {
           const uint32_t h = std::min(2u, e - I);
-          // rows [128 I, 128 (I + h)) need columns < 128 (I + h) - 1
-          if ((uint64_t)J * kTN < (uint64_t)(I + h) * kTM - 1) list.push_back({q, I, J, h});
+          // rows [128 I, 128 (I + h)) need columns < 128 (I + h) - 1; where
+          // only the second row tile reaches column tile J, it goes alone
+          if ((uint64_t)J * kTN >= (uint64_t)(I + h) * kTM - 1) continue;
+          if (h == 2 && (uint64_t)J * kTN >= (uint64_t)(I + 1) * kTM - 1)
+            list.push_back({q, I + 1, J, 1});
+          else
+            list.push_back({q, I, J, h});
         }
     }
   // Persistent CTAs take items round-robin: split the last pairs into single
@@ -706,9 +792,9 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     --split;
   }
   list.insert(list.end(), tail.rbegin(), tail.rend());
-  // one device block: [tensor maps (2 per job)][jobs][items]
+  // one device block: [tensor maps (3 per job)][jobs][items]
   const size_t nj = js.size();
-  const size_t tm_bytes = nj * 2 * sizeof(CUtensorMap);
+  const size_t tm_bytes = nj * 3 * sizeof(CUtensorMap);
   const size_t job_bytes = round_up(nj * sizeof(MmaJob), 64);
   std::vector<uint8_t> host(tm_bytes + job_bytes + list.size() * sizeof(MmaItem), 0);
   DevBuf dev(host.size(), stream);
@@ -720,15 +806,17 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     const hd_alignment *a = sp.aln;
     const hd_alignment *o = a->base ? a->base : a;
     const uint64_t rb = o->words * row_bytes_per_word((uint32_t)o->planes);
-    make_tmap_u8(ctx, &tms[2 * q], ops[js[q].k], rb, a->n_rows, kTN);
-    make_tmap_u8(ctx, &tms[2 * q + 1], ops[js[q].k], rb, a->n_rows, kTM);
+    make_tmap_u8(ctx, &tms[3 * q], ops[js[q].k], rb, a->n_rows, 2 * kTM);
+    make_tmap_u8(ctx, &tms[3 * q + 1], ops[js[q].k], rb, a->n_rows, kTM);
+    make_tmap_u8(ctx, &tms[3 * q + 2], ops[js[q].k], rb, a->n_rows, kTN);
     MmaJob &m = jobs[q];
-    m.tm256 = d_tms + 2 * q;
-    m.tm128 = d_tms + 2 * q + 1;
+    m.tm256 = d_tms + 3 * q;
+    m.tm128 = d_tms + 3 * q + 1;
+    m.tmb = d_tms + 3 * q + 2;
     m.out = sp.d_out;
     m.out_base = sp.out_base;
     m.n = (uint32_t)a->n_rows;
-    m.nkb = (uint32_t)(o->words / 4 * (o->planes + 1));
+    m.nkb = (uint32_t)(o->words / 8 * op_kblocks((uint32_t)o->planes));
     m.planes = (uint32_t)o->planes;
     m.sites = (uint32_t)a->length;
     m.max_dist = sp.max_dist;

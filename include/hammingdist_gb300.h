@@ -430,11 +430,11 @@ const char *hd_trace_last(const hd_ctx *ctx);
  * IMAD per 32 pair-sites; pair-sites per second). No reference counterpart. */
 int hd_measure_int_peaks(hd_ctx *ctx, double *lop3_per_s, double *popc_per_s,
                          double *mix_pair_sites_per_s);
-/* Dense FP8 tensor-core rate of this device (FLOP per second): one CTA per SM
- * issues back-to-back tcgen05.mma.kind::f8f6f4 (M=128, N=256, K=32) on
- * shared-memory operands, the instruction of the tensor-core distance engine.
- * No reference counterpart. */
-int hd_measure_mma_peak(hd_ctx *ctx, double *fp8_flop_per_s);
+/* Dense FP4 tensor-core rate of this device (FLOP per second): one CTA per SM
+ * issues back-to-back tcgen05.mma.kind::mxf4.block_scale (E2M1, M=128,
+ * N=256, K=64) on shared-memory operands, the instruction of the
+ * tensor-core distance engine. No reference counterpart. */
+int hd_measure_mma_peak(hd_ctx *ctx, double *fp4_flop_per_s);
 /* Failure-path self-test: a kernel waits, with the bounded wait of the
  * pairwise kernel and a limit of limit_ns (<= 1 s), on an mbarrier that is
  * never completed; *status receives the kernel's status word (1 = the wait
