@@ -73,6 +73,7 @@ SIGNATURES = {
     "hd_server_free": (None, [vp]),
     "hd_autotune": (ci, [vp, u64]),
     "hd_tune_lookup": (ci, [vp, u64, u64, ci, P(ci), P(ci)]),
+    "hd_tune_lookup_mma": (ci, [vp, u64, u64, ci, P(ci), P(ci), P(u64)]),
     "hd_tune_save": (ci, [vp, cp]),
     "hd_tune_load": (ci, [vp, cp]),
     "hd_pairwise_lt_files": (ci, [vp, u64, vp, ci, u64, ci, ci, vp, vp, vp, vp, vp]),
@@ -389,6 +390,14 @@ class Context:
         self._check(lib().hd_tune_lookup(self.h, n_rows, length, np.dtype(dtype).itemsize,
                                          ctypes.byref(t), ctypes.byref(s)))
         return t.value, s.value
+
+    def tune_lookup_mma(self, n_rows, length, dtype):
+        """(band, row tiles per item, minimum launch items) of the tensor-core
+        engine for a matrix of n_rows x length sites."""
+        b, r, m = ci(), ci(), u64()
+        self._check(lib().hd_tune_lookup_mma(self.h, n_rows, length, np.dtype(dtype).itemsize,
+                                             ctypes.byref(b), ctypes.byref(r), ctypes.byref(m)))
+        return b.value, r.value, m.value
 
     def tune_save(self, path):
         self._check(lib().hd_tune_save(self.h, path.encode()))

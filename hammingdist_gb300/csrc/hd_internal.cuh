@@ -95,6 +95,20 @@ struct Trace {
   std::vector<const char *> names;  // phase ending at event k (k >= 1)
   std::string last;                 // text of the last traced call
 };
+// Kernel configuration of one matrix (autotuned per n, L and dtype bucket).
+struct TileConfig {
+  int tile = 128;    // bit-plane engine: tile edge (64 or 128 rows)
+  int stages = 3;    // bit-plane engine: TMA staging depth
+  int mma_band = 0;  // tensor-core engine: tile rows per L2 band (0: built-in)
+  int mma_rows = 0;  // tensor-core engine: row tiles per item, 1 or 2 (0: built-in 2)
+};
+// The autotuner's table: a configuration per (n bucket, L bucket, dtype),
+// and per L bucket the fewest single-row-tile items for which a launch goes
+// to the tensor-core engine rather than the bit-plane engine.
+struct TuneTable {
+  std::vector<std::pair<uint32_t, TileConfig>> entries;
+  uint64_t mma_min_items[4] = {0, 0, 0, 0};  // 0: built-in
+};
 }  // namespace hd
 
 struct hd_ctx {
@@ -118,8 +132,11 @@ struct hd_ctx {
   std::shared_ptr<void> parsed;
   std::string parsed_tag;
   uint64_t parsed_limit = 0;
-  // autotuned kernel configurations: key = (n bucket, L bucket, dtype)
-  std::vector<std::pair<uint32_t, std::pair<int, int>>> tune;
+  // autotuned kernel configurations
+  hd::TuneTable tune;
+  // engine choice for the autotuner's timings: -1 as configured, 0 the
+  // bit-plane engine only, 1 the tensor-core engine at any launch size
+  int engine_force = -1;
   // child contexts (own streams) for concurrent ingest of many inputs
   std::vector<hd_ctx *> workers;
   // pinned staging for file reads by this context (grows)
@@ -405,10 +422,6 @@ constexpr uint32_t kTile = 128;
 
 // Kernel configuration of one job: tile edge (64 or 128 rows; 4 or 8 rows
 // per thread) and TMA staging depth.
-struct TileConfig {
-  int tile = 128;
-  int stages = 3;
-};
 // One matrix (or a range of its tile rows, in units of cfg.tile) for the
 // persistent engine.
 struct PairJobSpec {
@@ -429,6 +442,7 @@ struct PairLaunchPlan {
     unsigned long long *d_counter = nullptr;
     bool mma = false;              // the tensor-core engine (hd_mma.cu): d_items holds
     const void *d_items = nullptr; // its work items, `tiles` of them
+    bool queue = false;            // its CTAs draw items from d_counter (else round-robin)
   };
   std::vector<Launch> launches;
   std::vector<DevBuf> blocks;  // job tables + tensor maps + tile counters
@@ -450,6 +464,15 @@ TileConfig default_tile_config(uint64_t n_rows, uint64_t length, int dtype_bytes
 bool tile_config_valid(int tile, int stages);
 // tune.cu: the autotuned table (or the default) for (n, L, dtype)
 TileConfig tile_config_for(hd_ctx *ctx, uint64_t n_rows, uint64_t length, int dtype_bytes);
+// the tensor-core engine's minimum launch size (single-row-tile items) for
+// rows of `length` sites: HAMMINGDIST_MMA_MIN_ITEMS, else the table, else
+// the built-in value
+uint64_t mma_min_items_for(hd_ctx *ctx, uint64_t length);
+// mma.cu: the tensor-core engine's L2 band (tile rows) and row tiles per item
+// for a configuration: HAMMINGDIST_MMA_BAND / HAMMINGDIST_MMA_ROWS, else the
+// configuration's own, else the built-in 16 and 2
+int mma_band_of(const TileConfig &c);
+int mma_rows_of(const TileConfig &c);
 
 // mma.cu: the tensor-core engine for every rule (4, 5 or 6 planes, with
 // P L < 2^24; HAMMINGDIST_KERNEL=lop3 turns it off).

@@ -82,8 +82,9 @@ constexpr uint32_t kEpiBytes = kEpiWarps * 32 * kEpiPitch * 4;  // 32 x 32 words
 constexpr int kMmaSmem = kMmaStages * kStageBytes + kEpiBytes + 1024;
 constexpr uint32_t kTmemCols = 512;                   // row tile h at columns 256 h
 constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
-constexpr uint64_t kMmaMinItems = 48;                 // HAMMINGDIST_MMA_MIN_ITEMS overrides
 constexpr uint32_t kMmaBand = 16;  // tile rows per L2 band (HAMMINGDIST_MMA_BAND overrides)
+constexpr int kItemRing = 4;                          // item indices handed to the consumers
+constexpr uint32_t kNoItem = 0xFFFFFFFFu;             // end of this CTA's items
 // 128-byte blocks per 256 sites of the operand: the P planes, the row side's
 // dash and the column side's dash (two blocks for P = 6: -4 and -1)
 __host__ __device__ constexpr uint32_t op_blocks(uint32_t planes) {
@@ -360,9 +361,12 @@ __device__ __forceinline__ void epilogue_share(const MmaItem &tl, const MmaJob &
 
 __global__ void __launch_bounds__(kMmaThreads, 1)
     k_pairwise_mma(const MmaJob *__restrict__ jobs, const MmaItem *__restrict__ items,
-                   uint32_t n_items, int *status) {
+                   uint32_t n_items, unsigned *__restrict__ counter, uint32_t queue,
+                   int *status) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full[kMmaStages], empty[kMmaStages], done, tmem_free, fin;
+  __shared__ __align__(8) uint64_t item_full[kItemRing], item_empty[kItemRing];
+  __shared__ uint32_t s_item[kItemRing];
   __shared__ uint32_t s_tmem;
   __shared__ int s_abort;
   uint8_t *smem =
@@ -372,6 +376,10 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     for (int s = 0; s < kMmaStages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
+    }
+    for (int r = 0; r < kItemRing; ++r) {
+      mbar_init(&item_full[r], 1);
+      mbar_init(&item_empty[r], 1 + kEpiWarps);  // the MMA thread and each epilogue warp
     }
     mbar_init(&done, 1);
     mbar_init(&tmem_free, kEpiThreads);
@@ -395,10 +403,26 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      // producer: every K block of every item of this CTA, in order
+      // producer: draws this CTA's items from the launch's queue (its first
+      // item is blockIdx.x, later ones gridDim.x + an atomic count) or, with
+      // `queue` 0, round-robin (blockIdx.x + k gridDim.x); hands each item's
+      // index to the MMA and epilogue warps through the ring, then loads
+      // every K block of the item
       uint32_t g = 0;  // K blocks issued (stage g % S, phase g / S)
       bool ok = true;
-      for (uint32_t t = blockIdx.x; ok && t < n_items; t += gridDim.x) {
+      for (uint32_t k = 0; ok; ++k) {
+        const uint32_t r = k % kItemRing;
+        if (k >= (uint32_t)kItemRing &&
+            !mbar_wait_bounded(&item_empty[r], ((k / kItemRing) - 1) & 1u, kMmaWaitNs)) {
+          ok = false;
+          break;
+        }
+        uint32_t t = k == 0 ? blockIdx.x
+                            : (queue ? gridDim.x + atomicAdd(counter, 1u) : blockIdx.x + k * gridDim.x);
+        if (t >= n_items || *(volatile int *)&s_abort) t = kNoItem;
+        *(volatile uint32_t *)&s_item[r] = t;
+        mbar_arrive(&item_full[r]);  // releases the index to the waiting warps
+        if (t == kNoItem) break;
         const MmaItem tl = items[t];
         const MmaJob &job = jobs[tl.job];
         const CUtensorMap *ta = tl.halves == 2 ? job.tm256 : job.tm128;
@@ -439,9 +463,17 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       // MMA issuer
-      uint32_t g = 0, it = 0;
+      uint32_t g = 0;
       bool ok = true;
-      for (uint32_t t = blockIdx.x; ok && t < n_items; t += gridDim.x, ++it) {
+      for (uint32_t it = 0; ok; ++it) {
+        const uint32_t r = it % kItemRing;
+        if (!mbar_wait_bounded(&item_full[r], (it / kItemRing) & 1u, 4 * kMmaWaitNs)) {
+          ok = false;
+          break;
+        }
+        const uint32_t t = *(volatile uint32_t *)&s_item[r];
+        mbar_arrive(&item_empty[r]);
+        if (t == kNoItem) break;
         const uint32_t halves = items[t].halves, nkb = jobs[items[t].job].nkb;
         // the epilogue has read the previous item's accumulators
         if (it > 0 && !mbar_wait_bounded(&tmem_free, (it - 1) & 1u, kMmaWaitNs)) {
@@ -493,9 +525,25 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     const uint32_t t_lane = tmem + ((sub * 32) << 16);
     uint32_t *buf = reinterpret_cast<uint32_t *>(smem + kMmaStages * kStageBytes) +
                     (warp - 2) * 32 * kEpiPitch;
-    uint32_t it = 0;
-    for (uint32_t t = blockIdx.x; t < n_items; t += gridDim.x, ++it) {
-      const bool got = mbar_wait_bounded(&done, it & 1u, 4 * kMmaWaitNs);
+    for (uint32_t it = 0;; ++it) {
+      const uint32_t r = it % kItemRing;
+      // lane 0 waits and reads the index; the warp takes its answer
+      uint32_t t = kNoItem;
+      bool got = true;
+      if (lane == 0) {
+        got = mbar_wait_bounded(&item_full[r], (it / kItemRing) & 1u, 4 * kMmaWaitNs);
+        if (got) t = *(volatile uint32_t *)&s_item[r];
+      }
+      got = __shfl_sync(0xffffffffu, got ? 1u : 0u, 0) != 0;
+      t = __shfl_sync(0xffffffffu, t, 0);
+      if (got && lane == 0) mbar_arrive(&item_empty[r]);
+      if (!got) {
+        atomicExch(&s_abort, 1);
+        atomicExch(status, kStatusTmaTimeout);
+      }
+      // one decision per warp: tcgen05.ld needs the whole warp
+      if (__any_sync(0xffffffffu, t == kNoItem)) break;
+      got = mbar_wait_bounded(&done, it & 1u, 4 * kMmaWaitNs);
       if (!got) {
         atomicExch(&s_abort, 1);
         atomicExch(status, kStatusTmaTimeout);
@@ -601,6 +649,15 @@ void make_tmap_u8(hd_ctx *ctx, CUtensorMap *tm, const void *base, uint64_t row_b
 }
 
 }  // namespace
+
+int mma_band_of(const TileConfig &c) {
+  if (const char *e = std::getenv("HAMMINGDIST_MMA_BAND")) return std::max(2, std::atoi(e)) & ~1;
+  return c.mma_band > 0 ? std::max(2, c.mma_band) & ~1 : (int)kMmaBand;
+}
+int mma_rows_of(const TileConfig &c) {
+  if (const char *e = std::getenv("HAMMINGDIST_MMA_ROWS")) return std::atoi(e) == 1 ? 1 : 2;
+  return c.mma_rows == 1 ? 1 : 2;
+}
 
 bool mma_eligible(const hd_alignment *aln) {
   if (const char *e = std::getenv("HAMMINGDIST_KERNEL"))
@@ -721,20 +778,21 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     double cost;
   };
   std::vector<Job> js;
-  // A launch with few items leaves SMs idle: below kMmaMinItems single row
-  // tiles (128 x kTN) in all, the bit-plane engine's finer tiles finish first
-  // (its rate is a third, but it fills the SMs); a batch of small matrices
-  // still goes here when together they are enough.
-  uint64_t min_items = kMmaMinItems;
-  if (const char *e = std::getenv("HAMMINGDIST_MMA_MIN_ITEMS")) min_items = (uint64_t)std::max(0, std::atoi(e));
-  uint64_t items_total = 0;
+  // A launch with few items leaves SMs idle: below a minimum of single row
+  // tiles (128 x kTN) in all (mma_min_items_for, autotuned per row length),
+  // the bit-plane engine's finer tiles finish first; a batch of small
+  // matrices still goes here when together they are enough.
+  if (ctx->engine_force == 0) return;
+  uint64_t items_total = 0, max_len = 0;
   for (const PairJobSpec &sp : specs) {
     if (!mma_eligible(sp.aln) || sp.tile_hi <= sp.tile_lo) continue;
+    max_len = std::max<uint64_t>(max_len, sp.aln->length);
     const uint64_t edge = sp.cfg.tile > 0 ? (uint64_t)sp.cfg.tile : kTile;
     const uint64_t lo = sp.tile_lo * edge / kTM;
     const uint64_t hi = ceil_div(std::min<uint64_t>(sp.tile_hi * edge, sp.aln->n_rows), kTM);
     for (uint64_t I = lo; I < hi; ++I) items_total += ((I + 1) * kTM - 2) / kTN + 1;
   }
+  const uint64_t min_items = ctx->engine_force == 1 ? 0 : mma_min_items_for(ctx, max_len);
   if (items_total < min_items) return;
   for (size_t k = 0; k < specs.size(); ++k) {
     const PairJobSpec &sp = specs[k];
@@ -750,21 +808,28 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     taken[k] = 1;
   }
   if (js.empty()) return;
-  // biggest jobs first: their items start early, small ones fill the tail
-  std::stable_sort(js.begin(), js.end(), [](const Job &a, const Job &b) { return a.cost > b.cost; });
-  uint32_t band = kMmaBand;
-  if (const char *e = std::getenv("HAMMINGDIST_MMA_BAND")) band = (uint32_t)std::max(2, std::atoi(e)) & ~1u;
+  // CTAs draw items from a queue in list order: the costliest items first
+  // (longest rows: an item's cost is its K length), biggest jobs first among
+  // equals, so that the cheap items fill the tail
+  std::stable_sort(js.begin(), js.end(), [&](const Job &a, const Job &b) {
+    const uint64_t wa = specs[a.k].aln->words * op_kblocks((uint32_t)specs[a.k].aln->planes);
+    const uint64_t wb = specs[b.k].aln->words * op_kblocks((uint32_t)specs[b.k].aln->planes);
+    return wa != wb ? wa > wb : a.cost > b.cost;
+  });
   // Items of each job: pairs of 128-row tiles (a single one where a range is
-  // odd) x kTN-column tiles up to the last column any of their rows needs, in
-  // bands of `band` tile rows, column-major within a band.
+  // odd; single ones throughout with mma_rows 1) x kTN-column tiles up to the
+  // last column any of their rows needs, in bands of mma_band tile rows,
+  // column-major within a band.
   std::vector<MmaItem> list;
-  for (uint32_t q = 0; q < (uint32_t)js.size(); ++q)
+  for (uint32_t q = 0; q < (uint32_t)js.size(); ++q) {
+    const TileConfig &cfg = specs[js[q].k].cfg;
+    const uint32_t band = (uint32_t)mma_band_of(cfg), rows = (uint32_t)mma_rows_of(cfg);
     for (uint32_t b = js[q].t_lo; b < js[q].t_hi; b += band) {
       const uint32_t e = std::min(b + band, js[q].t_hi);
       const uint32_t j_end = (uint32_t)ceil_div((uint64_t)e * kTM - 1, kTN);
       for (uint32_t J = 0; J < j_end; ++J)
-        for (uint32_t I = b; I < e; I += 2) {
-          const uint32_t h = std::min(2u, e - I);
+        for (uint32_t I = b; I < e; I += rows) {
+          const uint32_t h = std::min(rows, e - I);
           // rows [128 I, 128 (I + h)) need columns < 128 (I + h) - 1; where
           // only the second row tile reaches column tile J, it goes alone
           if ((uint64_t)J * kTN >= (uint64_t)(I + h) * kTM - 1) continue;
@@ -774,16 +839,24 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
             list.push_back({q, I, J, h});
         }
     }
-  // Persistent CTAs take items round-robin: split the last pairs into single
-  // row tiles until the item count is a multiple of the grid, so that every
-  // CTA ends within one row tile of the others (a short list splits them all
-  // to fill more SMs).
+  }
+  // Work distribution. One matrix: every item costs the same, and the CTAs
+  // take them round-robin, the last pairs split into single row tiles until
+  // the count is a multiple of the grid, so that every CTA ends within one
+  // row tile of the others. Several matrices (items of unequal length): the
+  // CTAs draw items from a queue, and its last `grid` pairs are split, so
+  // that the CTAs finish within about half an item of each other.
+  // HAMMINGDIST_MMA_SCHEDULE=static|queue picks one for every launch. A
+  // short list splits every pair to fill more SMs.
   const int sms = sm_limit > 0 && sm_limit < ctx->sm_count ? sm_limit : ctx->sm_count;
+  bool queue = js.size() > 1;
+  if (const char *e = std::getenv("HAMMINGDIST_MMA_SCHEDULE")) queue = std::string(e) == "queue";
   uint64_t pairs = 0;
   for (const MmaItem &m : list) pairs += m.halves == 2;
   const uint64_t grid_n = std::min<uint64_t>(list.size() + pairs, (uint64_t)sms);
-  uint64_t split = list.size() < grid_n ? grid_n - list.size()
-                                        : (grid_n - list.size() % grid_n) % grid_n;
+  uint64_t split = list.size() < grid_n ? pairs
+                   : queue ? std::min<uint64_t>(pairs, grid_n)
+                           : (grid_n - list.size() % grid_n) % grid_n;
   std::vector<MmaItem> tail;
   for (size_t k = list.size(); k-- > 0 && split > 0;) {
     if (list[k].halves != 2) continue;
@@ -792,11 +865,12 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     --split;
   }
   list.insert(list.end(), tail.rbegin(), tail.rend());
-  // one device block: [tensor maps (3 per job)][jobs][items]
+  // one device block: [tensor maps (3 per job)][jobs][items][queue counter]
   const size_t nj = js.size();
   const size_t tm_bytes = nj * 3 * sizeof(CUtensorMap);
   const size_t job_bytes = round_up(nj * sizeof(MmaJob), 64);
-  std::vector<uint8_t> host(tm_bytes + job_bytes + list.size() * sizeof(MmaItem), 0);
+  const size_t item_bytes = round_up(list.size() * sizeof(MmaItem), 16);
+  std::vector<uint8_t> host(tm_bytes + job_bytes + item_bytes + 16, 0);
   DevBuf dev(host.size(), stream);
   auto *tms = reinterpret_cast<CUtensorMap *>(host.data());
   auto *jobs = reinterpret_cast<MmaJob *>(host.data() + tm_bytes);
@@ -835,15 +909,21 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
   L.grid = grid_n;
   L.d_jobs = dev.as<uint8_t>() + tm_bytes;
   L.d_items = dev.as<uint8_t>() + tm_bytes + job_bytes;
+  L.d_counter = reinterpret_cast<unsigned long long *>(dev.as<uint8_t>() + tm_bytes + job_bytes +
+                                                       item_bytes);
+  L.queue = queue;
   plan->launches.push_back(L);
   plan->blocks.push_back(std::move(dev));
 }
 
 void launch_mma(hd_ctx *ctx, const PairLaunchPlan::Launch &L, cudaStream_t stream) {
   set_smem_once();
+  // the item queue starts empty at every launch (also when a graph replays it)
+  HD_CUDA(cudaMemsetAsync(L.d_counter, 0, sizeof(unsigned), stream));
   k_pairwise_mma<<<(unsigned)L.grid, kMmaThreads, kMmaSmem, stream>>>(
       static_cast<const MmaJob *>(L.d_jobs), static_cast<const MmaItem *>(L.d_items),
-      (uint32_t)L.tiles, ctx->d_status);
+      (uint32_t)L.tiles, reinterpret_cast<unsigned *>(L.d_counter), L.queue ? 1u : 0u,
+      ctx->d_status);
   HD_LAUNCHED(ctx);
   ctx->last_pair_tiles += L.tiles;
 }
@@ -859,6 +939,8 @@ bool pairwise_mma(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_
   sp.max_dist = max_dist;
   sp.d_out = d_out;
   sp.out_base = out_base;
+  // the tensor-core settings of the whole matrix's bucket; row tiles of 128
+  sp.cfg = tile_config_for(ctx, aln->n_rows, aln->length, dtype_bytes);
   sp.cfg.tile = kTM;
   sp.tile_lo = tile_lo;
   sp.tile_hi = std::min<uint32_t>(tile_hi, (uint32_t)ceil_div(aln->n_rows, kTM));

@@ -375,7 +375,8 @@ void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStr
     if (taken[k] || s.aln->n_rows < 2 || s.tile_hi <= s.tile_lo) continue;
     if (s.aln->n_rows > 0xffffffffull) fail(HD_ERR_ARG, "too many rows");
     const Variant *v = &find_variant(s.cfg.tile, s.cfg.stages, s.aln->planes);
-    s.cfg = {v->tile, v->stages};
+    s.cfg.tile = v->tile;
+    s.cfg.stages = v->stages;
     auto it = std::find_if(groups.begin(), groups.end(), [&](const Group &g) { return g.v == v; });
     if (it == groups.end()) groups.push_back({v, {k}});
     else it->idx.push_back(k);

@@ -400,14 +400,26 @@ int hd_server_stats(hd_server *s, uint64_t *waves, uint64_t *completed,
 void hd_server_free(hd_server *s);
 
 /* ---- autotuning ------------------------------------------------------------ */
-/* Times every kernel configuration (tile edge 64/128 = 4/8 rows per thread,
- * TMA staging depth 2-4) for each (n bucket <= max_n_bucket, L bucket,
- * dtype) with the GPU filled, and keeps the fastest per bucket in the
- * context. Without a table (or with HAMMINGDIST_TILE=<tile>x<stages>) a
- * built-in choice applies. No reference counterpart. */
+/* Times every kernel configuration of both distance engines for each
+ * (n bucket <= max_n_bucket, L bucket, dtype) with the GPU filled, and keeps
+ * the fastest per bucket in the context: for the bit-plane engine the tile
+ * edge (64/128 = 4/8 rows per thread) and TMA staging depth (2-4), for the
+ * tensor-core engine the L2 band (8, 16 or 32 tile rows) and the item shape
+ * (one or two 128-row tiles). Then, per L bucket, it times single matrices
+ * of growing size on both engines and keeps the launch size (single-row-tile
+ * items) from which the tensor-core engine wins. Without a table (or with
+ * HAMMINGDIST_TILE=<tile>x<stages>, HAMMINGDIST_MMA_BAND, HAMMINGDIST_MMA_ROWS,
+ * HAMMINGDIST_MMA_MIN_ITEMS) built-in choices apply. No reference
+ * counterpart (the reference has one kernel shape,
+ * src/distance_cuda.cu:142-155). */
 int hd_autotune(hd_ctx *ctx, uint64_t max_n_bucket);
 int hd_tune_lookup(hd_ctx *ctx, uint64_t n_rows, uint64_t length,
                    int dtype_bytes, int *tile, int *stages);
+/* The tensor-core engine's settings that apply to a matrix of n_rows x length
+ * sites: L2 band (tile rows), row tiles per item (1 or 2) and the launch
+ * size from which a launch goes to that engine. No reference counterpart. */
+int hd_tune_lookup_mma(hd_ctx *ctx, uint64_t n_rows, uint64_t length,
+                       int dtype_bytes, int *band, int *rows, uint64_t *min_items);
 int hd_tune_save(hd_ctx *ctx, const char *path);
 int hd_tune_load(hd_ctx *ctx, const char *path);
 

@@ -110,6 +110,38 @@ def test_every_kernel_configuration(ctx, tmp_path, tile, stages):
         ctx.tune_load(path)  # back to the built-in choice
 
 
+@pytest.mark.parametrize("band,rows", [(8, 2), (16, 2), (32, 2), (16, 1), (2, 1)])
+def test_every_tensor_core_configuration(ctx, tmp_path, band, rows):
+    """A table that maps every bucket to one tensor-core configuration and
+    sends every launch to that engine: results are the same bit for bit, on
+    single matrices and on a batch."""
+    entries = [{"n_bucket": nb, "L_bucket": lb, "dtype": dt, "tile": 128, "stages": 3,
+                "mma_band": band, "mma_rows": rows}
+               for nb in range(7) for lb in range(4) for dt in (1, 2)]
+    path = str(tmp_path / "tune.json")
+    with open(path, "w") as f:
+        json.dump({"device": "test", "mma_min_items": [1, 1, 1, 1], "entries": entries}, f)
+    ctx.tune_load(path)
+    try:
+        assert ctx.tune_lookup_mma(300, 1000, np.uint8) == (band, rows, 1)
+        inputs = [synth.random_strings(n, L, b"ACGT-N", seed=910 + k)
+                  for k, (n, L) in enumerate([(2, 5), (300, 300), (600, 4097), (1100, 64)])]
+        alns = [ctx.alignment_from_sequences(s) for s in inputs]
+        b = ctx.batch()
+        for a, seqs in zip(alns, inputs):
+            want = o.lt_dense(seqs, max_distance=40, dtype=np.uint16)
+            np.testing.assert_array_equal(ctx.pairwise_lt(a, dtype=np.uint16, max_distance=40), want)
+            b.add(a, dtype=np.uint16, max_distance=40)
+        for got, seqs in zip(b.run(), inputs):
+            np.testing.assert_array_equal(got, o.lt_dense(seqs, max_distance=40, dtype=np.uint16))
+        b.free()
+    finally:
+        with open(path, "w") as f:
+            json.dump({"entries": []}, f)
+        ctx.tune_load(path)  # back to the built-in choice
+    assert ctx.tune_lookup_mma(300, 1000, np.uint8) == (16, 2, 48)
+
+
 def test_autotune_small_buckets(ctx, tmp_path):
     ctx.autotune(max_n_bucket=1)
     path = str(tmp_path / "t.json")
@@ -118,7 +150,12 @@ def test_autotune_small_buckets(ctx, tmp_path):
     assert len(table["entries"]) == 2 * 4 * 2
     for e in table["entries"]:
         assert (e["tile"], e["stages"]) in {(128, 3), (128, 2), (128, 4), (64, 3), (64, 4)}
+        assert (e["mma_band"], e["mma_rows"]) in {(16, 2), (8, 2), (32, 2), (16, 1)}
+    assert len(table["mma_min_items"]) == 4 and all(m >= 0 for m in table["mma_min_items"])
     ctx.tune_load(path)
+    e = table["entries"][0]
+    band, rows, _ = ctx.tune_lookup_mma(60, 1000, np.uint8)
+    assert (band, rows) == (e["mma_band"], e["mma_rows"])
     seqs = synth.random_strings(150, 1500, b"ACGT-", seed=3)
     aln = ctx.alignment_from_sequences(seqs)
     np.testing.assert_array_equal(ctx.pairwise_lt(aln), o.lt_dense(seqs))

@@ -203,3 +203,27 @@ def test_mma_exact_at_length_cap(ctx, planes, L):
         assert sparse
         np.testing.assert_array_equal(np.minimum(g, 65535), ref)
     aln.free()
+
+
+@pytest.mark.parametrize("schedule", ["static", "queue"])
+def test_mma_schedules(ctx, monkeypatch, schedule):
+    # both work distributions of the tensor-core engine (round-robin items,
+    # or items drawn from the launch's queue), on one matrix and on a batch
+    # of matrices of unequal row length, bit for bit against the oracle
+    monkeypatch.setenv("HAMMINGDIST_MMA_SCHEDULE", schedule)
+    rows, _, _ = synth.alignment(1200, 4001, p=2e-3, seed=77, dash_max=100)
+    seqs = [r.tobytes() for r in rows]
+    aln = ctx.alignment_from_sequences(seqs)
+    np.testing.assert_array_equal(ctx.pairwise_lt(aln), o.lt_dense(seqs))
+    inputs = [synth.random_strings(n, L, b"ACGT-N", seed=n + L)
+              for n, L in ((300, 5000), (129, 257), (700, 333), (450, 2999), (2, 33))]
+    alns = [ctx.alignment_from_sequences(s) for s in inputs]
+    b = ctx.batch()
+    for a in alns:
+        b.add(a, dtype=np.uint16, max_distance=65535)
+    for rep in range(2):  # the second run replays the captured graph
+        for got, s in zip(b.run(), inputs):
+            np.testing.assert_array_equal(got, o.lt_dense(s, max_distance=65535, dtype=np.uint16))
+    b.free()
+    for a in alns + [aln]:
+        a.free()
