@@ -85,6 +85,7 @@ SIGNATURES = {
     "hd_measure_int_peaks": (ci, [vp, P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
     "hd_measure_mma_peak": (ci, [vp, P(ctypes.c_double)]),
     "hd_last_pairwise_timing": (ci, [vp, P(ctypes.c_double), P(u64)]),
+    "hd_last_pairwise_work": (ci, [vp, P(ctypes.c_double)]),
 }
 
 SEM_GPU, SEM_CPU = 0, 1
@@ -507,6 +508,12 @@ class Context:
         ms, tiles = ctypes.c_double(), u64()
         self._check(lib().hd_last_pairwise_timing(self.h, ctypes.byref(ms), ctypes.byref(tiles)))
         return ms.value, tiles.value
+
+    def last_pairwise_work(self):
+        """Multiply-adds of the last pairwise call's tensor-core launches."""
+        m = ctypes.c_double()
+        self._check(lib().hd_last_pairwise_work(self.h, ctypes.byref(m)))
+        return m.value
 
 
 class Batch:

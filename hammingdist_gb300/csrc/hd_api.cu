@@ -1223,6 +1223,7 @@ int hd_pairwise_lt(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, int64_
     const uint64_t n = aln->n_rows, entries = n < 2 ? 0 : tri(n);
     ctx->last_pair_ms = 0;
     ctx->last_pair_tiles = 0;
+    HD_CUDA(cudaMemsetAsync(hd::mma_mac_counter(ctx), 0, 8, ctx->stream));
     if (!entries) return;
     if (!out) fail(HD_ERR_ARG, "null output");
     DevBuf tmp;
@@ -1540,6 +1541,15 @@ int hd_last_pairwise_timing(const hd_ctx *ctx, double *ms, uint64_t *tiles) {
   if (!ctx) return HD_ERR_ARG;
   if (ms) *ms = ctx->last_pair_ms;
   if (tiles) *tiles = ctx->last_pair_tiles;
+  return HD_OK;
+}
+
+int hd_last_pairwise_work(const hd_ctx *ctx, double *mma_macs) {
+  if (!ctx || !mma_macs) return HD_ERR_ARG;
+  unsigned long long m = 0;
+  if (cudaMemcpy(&m, hd::mma_mac_counter(ctx), 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return HD_ERR_CUDA;
+  *mma_macs = (double)m;
   return HD_OK;
 }
 

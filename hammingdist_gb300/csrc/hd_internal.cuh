@@ -152,6 +152,14 @@ struct hd_ctx {
   hd::Trace trace;
 };
 
+namespace hd {
+// tensor-core multiply-adds counted by the planning kernels (a 64-bit counter
+// in the context's status block, after the status word)
+inline unsigned long long *mma_mac_counter(const hd_ctx *ctx) {
+  return reinterpret_cast<unsigned long long *>(reinterpret_cast<uint8_t *>(ctx->d_status) + 8);
+}
+}  // namespace hd
+
 struct hd_alignment {
   hd_ctx *ctx = nullptr;  // creating context; may be destroyed before the alignment
   int device = 0;
@@ -173,6 +181,9 @@ struct hd_alignment {
   // alignment
   mutable hd::DevBuf op;
   mutable uint64_t op_rows = 0, op_cap = 0;
+  // per 256-site chunk of the operand (uint32 each): nonzero once an
+  // expanded row has a '-' in it (the chunks whose dash products count)
+  mutable hd::DevBuf op_dash;
   // Freed on the null stream: every API call has synchronised its own stream
   // before returning, so no queued work still reads these buffers, and the
   // creating context (and its streams) may already be gone.
@@ -183,7 +194,7 @@ struct hd_alignment {
   }
   ~hd_alignment() {
     cudaSetDevice(device);
-    for (auto *b : {&plane_buf[0], &plane_buf[1], &d_seqidx, &op}) {
+    for (auto *b : {&plane_buf[0], &plane_buf[1], &d_seqidx, &op, &op_dash}) {
       b->s = nullptr;
       b->release();
     }

@@ -22,6 +22,12 @@
 // are kind::mxf4 with every UE8M0 scale factor 1.0 and FP32 accumulation,
 // exact while P L < 2^24. mismatches = L - matches.
 //
+// K order: first the P plane blocks of every 256-site chunk (partial sums up
+// to P L), then the dash products, only for the chunks where some row of the
+// operand has a '-' (the expansion marks them): elsewhere every dash product
+// is 0. On aligned genomes the '-' sit mostly in leading and trailing runs, so
+// a row's P + 1 blocks per chunk shrink to about P.
+//
 // Operand (one buffer serves rows and columns): each row's bit planes are
 // expanded to packed E2M1, two sites per byte, K-major: for every 256 sites,
 // the P planes (1.0), the dash as 1.0 (read for rows) and the dash as -(P - 1)
@@ -90,10 +96,6 @@ constexpr uint32_t kNoItem = 0xFFFFFFFFu;             // end of this CTA's items
 __host__ __device__ constexpr uint32_t op_blocks(uint32_t planes) {
   return planes + (planes == 6 ? 3u : 2u);
 }
-// K blocks per 256 sites and side: the planes and the dash products
-__host__ __device__ constexpr uint32_t op_kblocks(uint32_t planes) {
-  return planes + (planes == 6 ? 2u : 1u);
-}
 // operand bytes per 32-site word: 16 bytes (32 sites of E2M1) per block
 __host__ __device__ constexpr uint64_t row_bytes_per_word(uint32_t planes) {
   return (uint64_t)op_blocks(planes) * 16;
@@ -122,7 +124,11 @@ struct MmaJob {
   void *out;                     // lt index out_base at out[0]
   unsigned long long out_base;
   uint32_t n, nkb, sites, max_dist, dtype;  // rows, K blocks per side, L, cap, 1/2/4 bytes
-  uint32_t planes;                          // P: op_kblocks(P) K blocks per 256 sites and side
+  uint32_t planes;                          // P
+  uint32_t chunks;                          // 256-site chunks per row
+  const uint32_t *dash_list;                // the chunks whose dash products count
+  const uint32_t *dash_marks;               // per chunk: some row has a '-' in it
+  unsigned long long pairs;                 // lower-triangle pairs of this launch
 };
 
 // One work item: kTN columns J x row tiles [I, I + halves) of job `job`.
@@ -155,10 +161,11 @@ __device__ __forceinline__ void put16(uint8_t *dst, uint32_t w, uint32_t v) {
 // the sparse rules, planes 4-5 in the second group) -> E2M1 operand rows.
 // One thread per (row, 32-site word): 16 or 32 bytes read, 16 bytes written
 // per block; eight consecutive words fill each 128-byte block of their 256
-// sites. The dash is the AND of the P planes ('-' has every plane).
+// sites. The dash is the AND of the P planes ('-' has every plane); a chunk
+// of 256 sites where some row has a '-' is marked in dash_chunk.
 __global__ void k_expand_op(const uint4 *__restrict__ g0, const uint4 *__restrict__ g1,
                             uint32_t planes, uint64_t words, uint64_t row_lo, uint64_t row_hi,
-                            uint64_t L, uint8_t *__restrict__ x) {
+                            uint64_t L, uint8_t *__restrict__ x, uint32_t *dash_chunk) {
   const uint64_t total = (row_hi - row_lo) * words;
   const uint32_t nb = op_blocks(planes);  // 128-byte blocks per 256 sites
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
@@ -181,6 +188,8 @@ __global__ void k_expand_op(const uint4 *__restrict__ g0, const uint4 *__restric
     put16(blk + planes * 128, dash, kE2M1One);                // 1.0: the row side
     put16(blk + (planes + 1) * 128, dash, dash_neg(planes));  // the column side
     if (planes == 6) put16(blk + (planes + 2) * 128, dash, kE2M1Neg1);
+    // the chunk holds a '-': its dash products count (every writer stores 1)
+    if (dash && !dash_chunk[w / 8]) dash_chunk[w / 8] = 1u;
   }
 }
 
@@ -430,7 +439,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
         prefetch_tmap(job.tmb);
         const int32_t ya = (int32_t)(tl.I * kTM), yb = (int32_t)(tl.J * kTN);
         const uint32_t bytes = kBBytes + tl.halves * kHalfBytes, nkb = job.nkb, P = job.planes;
-        const uint32_t Q = op_kblocks(P), NB = op_blocks(P);
+        const uint32_t NB = op_blocks(P), plane_kb = P * job.chunks;
         for (uint32_t kb = 0; kb < nkb; ++kb) {
           const uint32_t s = g % kMmaStages;
           if ((g >= (uint32_t)kMmaStages &&
@@ -439,12 +448,21 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
             ok = false;
             break;
           }
-          // K block kb: 256 sites of chunk kb / Q, block kb % Q (planes 0 ..
-          // P-1, then the dash: the +1 block for the rows, the -(P - 1) block
-          // for the columns; for P = 6 the +1 block twice, against -4 and -1)
-          const uint32_t c = kb / Q, q = kb % Q;
-          const int32_t xa = (int32_t)((NB * c + (q < P ? q : P)) * 128);
-          const int32_t xb = (int32_t)((NB * c + (q < P ? q : q + 1)) * 128);
+          // K block kb: first the P plane blocks of every 256-site chunk,
+          // then the dash products of the chunks that hold a '-' (the rows'
+          // +1 block against the columns' -(P - 1) block; for P = 6 the +1
+          // block twice, against -4 and -1). Elsewhere the dash products are
+          // all 0, so those blocks are left out.
+          uint32_t blk_a, blk_b;
+          if (kb < plane_kb) {
+            blk_a = blk_b = NB * (kb / P) + kb % P;
+          } else {
+            const uint32_t j = kb - plane_kb, two = P == 6 ? 1u : 0u;
+            const uint32_t c = job.dash_list[j >> two];
+            blk_a = NB * c + P;
+            blk_b = NB * c + P + 1 + (j & two);
+          }
+          const int32_t xa = (int32_t)(blk_a * 128), xb = (int32_t)(blk_b * 128);
           uint8_t *st = smem + s * kStageBytes;
           mbar_expect_tx(&full[s], bytes);
           tma_load_2d(st, ta, xa, ya, &full[s]);
@@ -624,6 +642,29 @@ __global__ void __launch_bounds__(128, 1) k_peak_mma(uint32_t rounds, int *statu
   }
 }
 
+// One warp per job: the ascending list of the chunks whose mark is set, and
+// the job's K blocks (P per chunk, then one per listed chunk, two for P = 6);
+// the job's multiply-adds (pairs x 256 values per K block) are added to
+// *macs. A mark set concurrently by a later expansion (rows this launch does
+// not read) only adds dash products of 0.
+__global__ void k_dash_list(MmaJob *jobs, unsigned long long *macs) {
+  MmaJob &job = jobs[blockIdx.x];
+  const uint32_t lane = threadIdx.x;
+  uint32_t *list = const_cast<uint32_t *>(job.dash_list);
+  uint32_t n = 0;
+  for (uint32_t c0 = 0; c0 < job.chunks; c0 += 32) {
+    const uint32_t c = c0 + lane;
+    const bool on = c < job.chunks && *(volatile const uint32_t *)&job.dash_marks[c] != 0u;
+    const uint32_t bits = __ballot_sync(0xffffffffu, on);
+    if (on) list[n + __popc(bits & ((1u << lane) - 1u))] = c;
+    n += __popc(bits);
+  }
+  if (lane == 0) {
+    job.nkb = job.planes * job.chunks + n * (job.planes == 6 ? 2u : 1u);
+    atomicAdd(macs, job.pairs * 256ull * job.nkb);
+  }
+}
+
 void set_smem_once() {
   static std::once_flag once;
   static cudaError_t err = cudaSuccess;
@@ -697,11 +738,15 @@ bool ensure_operand(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStr
     o->op = std::move(grown);
     o->op_cap = cap;
   }
+  if (!o->op_dash.p) {
+    o->op_dash = DevBuf(words / 8 * 4, stream);
+    HD_CUDA(cudaMemsetAsync(o->op_dash.p, 0, words / 8 * 4, stream));
+  }
   const uint64_t total = (rows - o->op_rows) * words;
   const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
   k_expand_op<<<(unsigned)grid, 256, 0, stream>>>(
       o->plane_buf[0].as<uint4>(), P > 4 ? o->plane_buf[1].as<uint4>() : nullptr, P, words,
-      o->op_rows, rows, o->length, o->op.as<uint8_t>());
+      o->op_rows, rows, o->length, o->op.as<uint8_t>(), o->op_dash.as<uint32_t>());
   HD_LAUNCHED(ctx);
   o->op_rows = rows;
   return true;
@@ -734,36 +779,44 @@ double measure_mma_peak(hd_ctx *ctx) {
 // until the kernel has run (a serving window must not expand a large base).
 // False if there is no memory for it.
 bool operand_for(hd_ctx *ctx, const hd_alignment *a, cudaStream_t stream, PairLaunchPlan *plan,
-                 const uint8_t *&op) {
+                 const uint8_t *&op, const uint32_t *&dash) {
   const hd_alignment *o = a->base ? a->base : a;
   if (!a->base) {
     if (!ensure_operand(ctx, a, a->n_rows, stream)) return false;
     op = a->op.as<uint8_t>();
+    dash = a->op_dash.as<uint32_t>();
     return true;
   }
   if (a->row0 == 0 && o->op.p && o->op_rows >= a->n_rows) {
+    // the base's chunk marks cover its other rows too: a chunk marked for
+    // them only adds dash products of 0
     op = o->op.as<uint8_t>();
+    dash = o->op_dash.as<uint32_t>();
     return true;
   }
   const uint32_t P = (uint32_t)o->planes;
   const uint64_t rb = o->words * row_bytes_per_word(P), bytes = a->n_rows * rb;
+  const uint64_t flag_bytes = o->words / 8 * 4;
   if (bytes > (8ull << 30)) return false;  // the bit-plane engine needs no extra memory
   DevBuf tmp;
   try {
-    tmp = DevBuf(bytes, stream);
+    tmp = DevBuf(bytes + flag_bytes, stream);
   } catch (const Error &e) {
     if (e.code != HD_ERR_OOM) throw;
     cudaGetLastError();
     return false;
   }
+  uint32_t *flags = reinterpret_cast<uint32_t *>(tmp.as<uint8_t>() + bytes);
+  HD_CUDA(cudaMemsetAsync(flags, 0, flag_bytes, stream));
   const uint64_t total = a->n_rows * o->words;
   const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
   k_expand_op<<<(unsigned)grid, 256, 0, stream>>>(
       static_cast<const uint4 *>(a->planes_ptr(0)),
       P > 4 ? static_cast<const uint4 *>(a->planes_ptr(1)) : nullptr, P, o->words, 0, a->n_rows,
-      o->length, tmp.as<uint8_t>());
+      o->length, tmp.as<uint8_t>(), flags);
   HD_LAUNCHED(ctx);
   op = tmp.as<uint8_t>();
+  dash = flags;
   plan->blocks.push_back(std::move(tmp));
   return true;
 }
@@ -772,6 +825,7 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
                       PairLaunchPlan *plan, int sm_limit, std::vector<char> &taken) {
   taken.assign(specs.size(), 0);
   std::vector<const uint8_t *> ops(specs.size(), nullptr);  // each job's operand rows
+  std::vector<const uint32_t *> dash_marks(specs.size(), nullptr);  // and its chunk marks
   struct Job {
     size_t k;
     uint32_t t_lo, t_hi;
@@ -802,19 +856,26 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     const uint64_t edge = sp.cfg.tile > 0 ? (uint64_t)sp.cfg.tile : kTile;
     const uint64_t row_lo = sp.tile_lo * edge, row_hi = std::min<uint64_t>(sp.tile_hi * edge, a->n_rows);
     if (row_lo % kTM || row_hi <= row_lo) continue;
-    if (!operand_for(ctx, a, stream, plan, ops[k])) continue;
+    if (!operand_for(ctx, a, stream, plan, ops[k], dash_marks[k])) continue;
     const uint32_t lo = (uint32_t)(row_lo / kTM), hi = (uint32_t)ceil_div(row_hi, kTM);
     js.push_back({k, lo, hi, (double)a->words * ((double)hi * hi - (double)lo * lo)});
     taken[k] = 1;
   }
   if (js.empty()) return;
+  // Each job's K blocks: the P plane blocks of every chunk, and the dash
+  // products of the chunks its rows have a '-' in. The chunk list is built on
+  // the device from the expansion's marks (k_dash_list, below), in stream
+  // order after the operands; the host orders the jobs by the plane blocks.
+  std::vector<uint32_t> kcost(specs.size(), 0);
+  for (const Job &j : js) {
+    const hd_alignment *o = specs[j.k].aln->base ? specs[j.k].aln->base : specs[j.k].aln;
+    kcost[j.k] = (uint32_t)(o->planes * (o->words / 8));
+  }
   // CTAs draw items from a queue in list order: the costliest items first
-  // (longest rows: an item's cost is its K length), biggest jobs first among
-  // equals, so that the cheap items fill the tail
+  // (an item's cost is its K length), biggest jobs first among equals, so
+  // that the cheap items fill the tail
   std::stable_sort(js.begin(), js.end(), [&](const Job &a, const Job &b) {
-    const uint64_t wa = specs[a.k].aln->words * op_kblocks((uint32_t)specs[a.k].aln->planes);
-    const uint64_t wb = specs[b.k].aln->words * op_kblocks((uint32_t)specs[b.k].aln->planes);
-    return wa != wb ? wa > wb : a.cost > b.cost;
+    return kcost[a.k] != kcost[b.k] ? kcost[a.k] > kcost[b.k] : a.cost > b.cost;
   });
   // Items of each job: pairs of 128-row tiles (a single one where a range is
   // odd; single ones throughout with mma_rows 1) x kTN-column tiles up to the
@@ -866,15 +927,23 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
   }
   list.insert(list.end(), tail.rbegin(), tail.rend());
   // one device block: [tensor maps (3 per job)][jobs][items][queue counter]
+  // [dash chunk lists]
   const size_t nj = js.size();
   const size_t tm_bytes = nj * 3 * sizeof(CUtensorMap);
   const size_t job_bytes = round_up(nj * sizeof(MmaJob), 64);
   const size_t item_bytes = round_up(list.size() * sizeof(MmaItem), 16);
-  std::vector<uint8_t> host(tm_bytes + job_bytes + item_bytes + 16, 0);
+  size_t dash_words = 0;
+  for (const Job &j : js) {
+    const hd_alignment *o = specs[j.k].aln->base ? specs[j.k].aln->base : specs[j.k].aln;
+    dash_words += o->words / 8;
+  }
+  const size_t dash_at = tm_bytes + job_bytes + item_bytes + 16;
+  std::vector<uint8_t> host(dash_at + dash_words * 4 + 4, 0);
   DevBuf dev(host.size(), stream);
   auto *tms = reinterpret_cast<CUtensorMap *>(host.data());
   auto *jobs = reinterpret_cast<MmaJob *>(host.data() + tm_bytes);
   const auto *d_tms = reinterpret_cast<const CUtensorMap *>(dev.p);
+  size_t dash_off = 0;
   for (size_t q = 0; q < nj; ++q) {
     const PairJobSpec &sp = specs[js[q].k];
     const hd_alignment *a = sp.aln;
@@ -890,7 +959,14 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     m.out = sp.d_out;
     m.out_base = sp.out_base;
     m.n = (uint32_t)a->n_rows;
-    m.nkb = (uint32_t)(o->words / 8 * op_kblocks((uint32_t)o->planes));
+    m.nkb = 0;  // set by k_dash_list
+    m.chunks = (uint32_t)(o->words / 8);
+    m.dash_list = reinterpret_cast<const uint32_t *>(static_cast<uint8_t *>(dev.p) + dash_at) + dash_off;
+    m.dash_marks = dash_marks[js[q].k];
+    dash_off += m.chunks;
+    // the launch's lower-triangle pairs (for its multiply-add count)
+    const uint64_t r_lo = (uint64_t)js[q].t_lo * kTM, r_hi = std::min<uint64_t>((uint64_t)js[q].t_hi * kTM, a->n_rows);
+    m.pairs = r_hi * (r_hi - 1) / 2 - (r_lo ? r_lo * (r_lo - 1) / 2 : 0);
     m.planes = (uint32_t)o->planes;
     m.sites = (uint32_t)a->length;
     m.max_dist = sp.max_dist;
@@ -899,6 +975,9 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
   std::memcpy(host.data() + tm_bytes + job_bytes, list.data(), list.size() * sizeof(MmaItem));
   // from pageable memory: the call has consumed `host` when it returns
   HD_CUDA(cudaMemcpyAsync(dev.p, host.data(), host.size(), cudaMemcpyHostToDevice, stream));
+  k_dash_list<<<(unsigned)nj, 32, 0, stream>>>(reinterpret_cast<MmaJob *>(dev.as<uint8_t>() + tm_bytes),
+                                              mma_mac_counter(ctx));
+  HD_LAUNCHED(ctx);
   PairLaunchPlan::Launch L;
   L.mma = true;
   L.fn = reinterpret_cast<const void *>(k_pairwise_mma);

@@ -304,7 +304,7 @@ py::dict from_fasta_device(uintptr_t fasta, uint64_t nbytes, uintptr_t out, uint
   hd_ctx *c = ctx();
   const int dtype = large ? 2 : 1;
   uint64_t n_rows = 0, n_in = 0;
-  double kernel_ms = 0;
+  double kernel_ms = 0, mma_macs = 0;
   uint64_t tiles = 0;
   std::vector<uint64_t> idx;
   std::vector<uint32_t> rd;
@@ -321,6 +321,7 @@ py::dict from_fasta_device(uintptr_t fasta, uint64_t nbytes, uintptr_t out, uint
     if (entries) {
       check(hd_pairwise_lt(c, a.p, dtype, max_distance, reinterpret_cast<void *>(out), 1));
       hd_last_pairwise_timing(c, &kernel_ms, &tiles);
+      hd_last_pairwise_work(c, &mma_macs);
     }
     if (remove_duplicates) {
       idx.resize(n_in);
@@ -335,6 +336,7 @@ py::dict from_fasta_device(uintptr_t fasta, uint64_t nbytes, uintptr_t out, uint
   r["nsamples"] = n_rows;
   r["sequence_indices"] = py::array_t<uint64_t>((py::ssize_t)idx.size(), idx.data());
   r["kernel_ms"] = kernel_ms;
+  r["mma_macs"] = mma_macs;
   if (want_ref) r["reference_distances"] = py::array_t<uint32_t>((py::ssize_t)rd.size(), rd.data());
   return r;
 }

@@ -457,6 +457,10 @@ int hd_selftest_wait_timeout(hd_ctx *ctx, uint64_t limit_ns, int *status,
 /* Device time of the last pairwise kernel launch sequence (ms, CUDA events on
  * the launching stream) and the number of tiles it processed. */
 int hd_last_pairwise_timing(const hd_ctx *ctx, double *ms, uint64_t *tiles);
+/* Tensor-core work of the last hd_pairwise_lt: the multiply-adds its
+ * launches performed for the lower triangle (pairs x operand values per
+ * pair; 0 if the bit-plane engine computed it). No reference counterpart. */
+int hd_last_pairwise_work(const hd_ctx *ctx, double *mma_macs);
 
 #ifdef __cplusplus
 }

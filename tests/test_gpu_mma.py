@@ -227,3 +227,39 @@ def test_mma_schedules(ctx, monkeypatch, schedule):
     b.free()
     for a in alns + [aln]:
         a.free()
+
+
+def test_mma_dash_chunks(ctx):
+    # the dash products run only for the 256-site chunks where some row has a
+    # '-': a single '-' in one middle chunk of one row, '-' runs that end
+    # exactly on chunk boundaries, rows without any '-', and windows of the
+    # alignment (a window at row 0 shares the whole alignment's marks; a
+    # window elsewhere marks its own rows' chunks)
+    from hammingdist_gb300 import abi
+
+    rng = np.random.default_rng(17)
+    L = 256 * 9 + 17
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    rows = [acgt[rng.integers(0, 4, L)] for _ in range(400)]
+    rows[3][256 * 4 + 100] = ord("-")
+    rows[250][: 256 * 2] = ord("-")
+    rows[251][256 * 7:] = ord("-")
+    rows[399][256 * 5 + 255] = ord("-")
+    seqs = [r.tobytes() for r in rows]
+    aln = ctx.alignment_from_sequences(seqs)
+    got, want = _both(ctx, aln, dtype=np.uint16, max_distance=65535)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got, o.lt_dense(seqs, max_distance=65535, dtype=np.uint16))
+    for row0, n in ((0, 260), (200, 150), (240, 160)):
+        v = aln.view(row0, n)
+        got, want = _both(ctx, v)
+        np.testing.assert_array_equal(got, want)
+        np.testing.assert_array_equal(got, o.lt_dense(seqs[row0:row0 + n]))
+        v.free()
+    aln.free()
+    # the sparse rules (5 and 6 planes) on the same rows
+    for include_x in (False, True):
+        sp = ctx.alignment_from_sequences(seqs, include_x=include_x, semantics=abi.SEM_CPU)
+        got, want = _both(ctx, sp, dtype=np.uint16, max_distance=65535)
+        np.testing.assert_array_equal(got, want)
+        sp.free()
