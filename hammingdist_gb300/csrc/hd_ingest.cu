@@ -65,33 +65,35 @@ __device__ inline uint32_t nl_mask16(const uint8_t *p, uint64_t off, uint64_t n)
   return m;
 }
 
-__global__ void k_nl_count(const uint8_t *p, uint64_t n, uint64_t *counts) {
+// Newlines per 64 KB block (counts) and per 8 KB warp span (warp_counts).
+__global__ void k_nl_count(const uint8_t *p, uint64_t n, uint64_t *counts, uint32_t *warp_counts) {
   __shared__ uint64_t tmp[33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t base = blockIdx.x * kNlBlockBytes + warp * kNlWarpBytes + lane * 16;
-  uint64_t c = 0;
+  uint32_t c = 0;
 #pragma unroll 4
   for (int it = 0; it < kNlIters; ++it) c += __popc(nl_mask16(p, base + it * 512ull, n));
+  const uint32_t cw = warp_sum(c);
+  if (lane == 0) warp_counts[blockIdx.x * (kNlThreads / 32) + warp] = cw;
   uint64_t tot;
-  block_excl_scan<uint64_t>(c, tmp, tot);
+  block_excl_scan<uint64_t>((uint64_t)c, tmp, tot);
   if (threadIdx.x == 0) counts[blockIdx.x] = tot;
 }
 
-// Writes the positions of every '\n' in increasing order.
-__global__ void k_nl_write(const uint8_t *p, uint64_t n, const uint64_t *block_off, uint64_t *nl) {
-  __shared__ uint64_t wt[kNlThreads / 32];
+// Writes the positions of every '\n' in increasing order: each warp starts at
+// its block's offset plus the counts of the block's earlier warps, and scans
+// its lanes' counts only where some lane holds a newline.
+__global__ void k_nl_write(const uint8_t *p, uint64_t n, const uint64_t *block_off,
+                           const uint32_t *warp_counts, uint64_t *nl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint64_t wbase = blockIdx.x * kNlBlockBytes + warp * kNlWarpBytes;
-  uint32_t c = 0;
-  for (int it = 0; it < kNlIters; ++it) c += __popc(nl_mask16(p, wbase + it * 512ull + lane * 16, n));
-  c = warp_sum(c);
-  if (lane == 0) wt[warp] = c;
-  __syncthreads();
   uint64_t off = block_off[blockIdx.x];
-  for (int w = 0; w < warp; ++w) off += wt[w];
+  for (int w = 0; w < warp; ++w) off += warp_counts[blockIdx.x * (kNlThreads / 32) + w];
+  if (warp_counts[blockIdx.x * (kNlThreads / 32) + warp] == 0) return;
   for (int it = 0; it < kNlIters; ++it) {
     uint64_t at = wbase + it * 512ull + lane * 16;
     uint32_t m = nl_mask16(p, at, n);
+    if (!__any_sync(0xffffffffu, m != 0)) continue;
     uint32_t cnt = __popc(m);
     uint32_t inc = warp_incl_scan(cnt);
     uint64_t pos = off + inc - cnt;
@@ -213,8 +215,9 @@ static unsigned grid_for(uint64_t n, int threads) {
 DevBuf newline_positions(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64_t *m_nl) {
   cudaStream_t st = ctx->stream;
   const uint64_t nblk = ceil_div(nbytes ? nbytes : 1, kNlBlockBytes);
-  DevBuf counts(nblk * 8, st), offs(nblk * 8, st), total(8, st);
-  k_nl_count<<<(unsigned)nblk, kNlThreads, 0, st>>>(d, nbytes, counts.as<uint64_t>());
+  DevBuf counts(nblk * 8, st), offs(nblk * 8, st), total(8, st), wcounts(nblk * 4 * (kNlThreads / 32), st);
+  k_nl_count<<<(unsigned)nblk, kNlThreads, 0, st>>>(d, nbytes, counts.as<uint64_t>(),
+                                                     wcounts.as<uint32_t>());
   HD_LAUNCHED(ctx);
   scan_exclusive<uint64_t>(ctx, counts.as<uint64_t>(), offs.as<uint64_t>(), nblk,
                            total.as<uint64_t>());
@@ -225,7 +228,7 @@ DevBuf newline_positions(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64_
   DevBuf nl((h + 1) * 8, st);
   if (h) {
     k_nl_write<<<(unsigned)nblk, kNlThreads, 0, st>>>(d, nbytes, offs.as<uint64_t>(),
-                                                       nl.as<uint64_t>());
+                                                       wcounts.as<uint32_t>(), nl.as<uint64_t>());
     HD_LAUNCHED(ctx);
   }
   return nl;
@@ -236,9 +239,11 @@ Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_
   Records rec;
   uint64_t nblk = ceil_div(nbytes ? nbytes : 1, kNlBlockBytes);
   DevBuf counts(nblk * 8, st), offs(nblk * 8, st), total(8, st), sumbuf(sizeof(ParseSummary), st);
+  DevBuf wcounts(nblk * 4 * (kNlThreads / 32), st);
   ParseSummary *d_sum = sumbuf.as<ParseSummary>();
   HD_CUDA(cudaMemsetAsync(d_sum, 0, sizeof(ParseSummary), st));
-  k_nl_count<<<(unsigned)nblk, kNlThreads, 0, st>>>(d_file, nbytes, counts.as<uint64_t>());
+  k_nl_count<<<(unsigned)nblk, kNlThreads, 0, st>>>(d_file, nbytes, counts.as<uint64_t>(),
+                                                     wcounts.as<uint32_t>());
   HD_LAUNCHED(ctx);
   scan_exclusive<uint64_t>(ctx, counts.as<uint64_t>(), offs.as<uint64_t>(), nblk,
                            total.as<uint64_t>());
@@ -251,7 +256,7 @@ Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_
   DevBuf nl((m_nl + 1) * 8, st);
   if (m_nl) {
     k_nl_write<<<(unsigned)nblk, kNlThreads, 0, st>>>(d_file, nbytes, offs.as<uint64_t>(),
-                                                       nl.as<uint64_t>());
+                                                       wcounts.as<uint32_t>(), nl.as<uint64_t>());
     HD_LAUNCHED(ctx);
   }
   DevBuf hdr((M + 1) * 4, st), H((M + 1) * 8, st), htot(8, st);
@@ -349,7 +354,7 @@ __device__ inline uint64_t mix64(uint64_t x) {
 }
 
 constexpr unsigned long long kEmpty = ~0ull;
-constexpr int kHashU = 2;     // 512-byte blocks per warp per step of k_hash and k_tab_verify
+constexpr int kHashU = 2;     // 512-byte blocks per warp per step of k_hash and k_tab_cmp
 
 // 16 bytes at the 16-byte aligned address x, bytes outside the readable
 // range [lo, hi) read as 0 (byte loads only at the ends of the range).
@@ -369,10 +374,12 @@ __device__ inline uint32_t load4_in(uint64_t x, uint64_t lo, uint64_t hi) {
   return w;
 }
 
-// Hash of each record's bytes: a sum of position-keyed 64-bit mixes of its
-// 4-byte groups (relative to the record start; a short last group is
-// zero-filled). Any two different records collide with probability ~2^-64;
-// equal hashes are verified byte by byte. The warp reads the record with
+// Hash of each record's bytes: a sum over its 4-byte groups (relative to the
+// record start; a short last group is zero-filled) of the 64-bit product of
+// the group XORed with two position-keyed 32-bit constants, then one 64-bit
+// mix of the sum and the length. Different records rarely share a hash, and
+// equal hashes are verified byte by byte, so a collision costs a verify
+// round, never a wrong answer. The warp reads the record with
 // aligned 16-byte loads (two 512-byte blocks per step); a lane's groups start
 // at byte P mod 4 of its words and are realigned with a funnel shift and the
 // next lane's first word.
@@ -413,7 +420,10 @@ __global__ void k_hash(const uint8_t *base, uint64_t bytes, const uint64_t *rs, 
           uint32_t w = __funnelshift_r(wd[g], wd[g + 1], 8 * h4);
           const int64_t left = (int64_t)len - s;
           if (left < 4) w &= (1u << (8 * left)) - 1u;
-          h += mix64((((uint64_t)s >> 2) << 32) ^ w ^ 0x9e3779b97f4a7c15ull);
+          const uint32_t q = (uint32_t)((uint64_t)s >> 2);
+          const uint32_t x = w ^ (q * 0x9e3779b9u + 0x7f4a7c15u);
+          const uint32_t y = w ^ (q * 0x85ebca6bu + 0x165667b1u);
+          h += (uint64_t)x * y;
         }
       }
     }
@@ -505,41 +515,57 @@ __device__ inline bool warp_equal(uint64_t Pa, uint64_t Pb, uint64_t len, uint64
   return eq;
 }
 
-__global__ void k_tab_verify(const uint8_t *base, uint64_t bytes, const uint64_t *rs, const uint64_t *rl,
-                             const uint64_t *hash, const uint64_t *list, uint64_t cnt,
-                             const unsigned long long *keys, const unsigned long long *mins,
-                             uint64_t mask, uint64_t *dup, uint64_t *next,
-                             unsigned long long *next_cnt) {
+// The verify step spread over segments: warp (i, seg) compares bytes
+// [seg * seg_bytes, +seg_bytes) of list record i with the lowest-index record
+// of its hash (rep_out[i]) and marks differs[i] on a difference; k_tab_resolve
+// then files each record as unique, a duplicate of rep, or (a hash collision)
+// a record for the next round. Many warps per record keep the loads in
+// flight when there are few duplicates.
+__global__ void k_tab_cmp(const uint8_t *base, uint64_t bytes, const uint64_t *rs,
+                          const uint64_t *rl, const uint64_t *hash, const uint64_t *list,
+                          uint64_t cnt, const unsigned long long *keys,
+                          const unsigned long long *mins, uint64_t mask, uint64_t seg_bytes,
+                          uint64_t segs, uint64_t *rep_out, uint32_t *differs) {
   const int lane = threadIdx.x & 31;
-  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
-  for (uint64_t i = wid; i < cnt; i += nwarps) {
-    uint64_t r = list ? list[i] : i;
-    uint64_t rep = 0;
-    if (lane == 0) {
-      unsigned long long h = hash[r];
-      uint64_t slot = slot_of(h, mask);
-      while (keys[slot] != h) slot = (slot + 1) & mask;
-      rep = mins[slot];
-    }
-    rep = __shfl_sync(0xffffffffu, rep, 0);
-    if (rep == r) {
-      if (lane == 0) dup[r] = r;
-      continue;
-    }
-    bool eq = rl[r] == rl[rep];
-    if (eq) {
-      const uint64_t lo = reinterpret_cast<uint64_t>(base);
-      eq = warp_equal(lo + rs[r], lo + rs[rep], rl[r], lo, lo + bytes, lane);
-    }
-    if (lane == 0) {
-      if (eq) {
-        dup[r] = rep;
-      } else {
-        unsigned long long at = atomicAdd(next_cnt, 1ull);
-        next[at] = r;
-      }
-    }
+  const uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  if (wid >= cnt * segs) return;
+  const uint64_t i = wid / segs, seg = wid % segs;
+  const uint64_t r = list ? list[i] : i;
+  uint64_t rep = 0;
+  if (lane == 0) {
+    const unsigned long long h = hash[r];
+    uint64_t slot = slot_of(h, mask);
+    while (keys[slot] != h) slot = (slot + 1) & mask;
+    rep = mins[slot];
+    if (seg == 0) rep_out[i] = rep;
+  }
+  rep = __shfl_sync(0xffffffffu, rep, 0);
+  if (rep == r) return;
+  const uint64_t len = rl[r];
+  if (len != rl[rep]) {
+    if (seg == 0 && lane == 0) differs[i] = 1u;
+    return;
+  }
+  const uint64_t o = seg * seg_bytes;
+  if (o >= len) return;
+  const uint64_t sl = len - o < seg_bytes ? len - o : seg_bytes;
+  const uint64_t lo = reinterpret_cast<uint64_t>(base);
+  const bool eq = warp_equal(lo + rs[r] + o, lo + rs[rep] + o, sl, lo, lo + bytes, lane);
+  if (!eq && lane == 0) differs[i] = 1u;
+}
+
+__global__ void k_tab_resolve(const uint64_t *list, uint64_t cnt, const uint64_t *rep_out,
+                              const uint32_t *differs, uint64_t *dup, uint64_t *next,
+                              unsigned long long *next_cnt) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  const uint64_t r = list ? list[i] : i, rep = rep_out[i];
+  if (rep == r) {
+    dup[r] = r;
+  } else if (!differs[i]) {
+    dup[r] = rep;
+  } else {
+    next[atomicAdd(next_cnt, 1ull)] = r;
   }
 }
 
@@ -555,6 +581,27 @@ __global__ void k_number(const uint64_t *dup, const uint64_t *uidx, uint64_t R, 
   seqidx[r] = uidx[dup[r]];
   if (dup[r] == r) unique_rec[uidx[r]] = r;
 }
+
+namespace {
+// One verify round over `cnt` list records (k_tab_cmp + k_tab_resolve).
+void verify_round(hd_ctx *ctx, const Records &rec, const uint64_t *hash, const uint64_t *list,
+                  uint64_t cnt, const unsigned long long *keys, const unsigned long long *mins,
+                  uint64_t mask, uint64_t *dup, uint64_t *next, unsigned long long *next_cnt) {
+  if (!cnt) return;
+  cudaStream_t st = ctx->stream;
+  constexpr uint64_t kSeg = 4096;  // bytes compared per warp
+  const uint64_t segs = ceil_div(rec.max_len ? rec.max_len : 1, kSeg);
+  DevBuf rep(cnt * 8, st), differs(cnt * 4, st);
+  HD_CUDA(cudaMemsetAsync(differs.p, 0, cnt * 4, st));
+  k_tab_cmp<<<grid_for(cnt * segs * 32, 256), 256, 0, st>>>(
+      rec.base, rec.bytes, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(), hash, list, cnt,
+      keys, mins, mask, kSeg, segs, rep.as<uint64_t>(), differs.as<uint32_t>());
+  HD_LAUNCHED(ctx);
+  k_tab_resolve<<<grid_for(cnt, 256), 256, 0, st>>>(list, cnt, rep.as<uint64_t>(),
+                                                   differs.as<uint32_t>(), dup, next, next_cnt);
+  HD_LAUNCHED(ctx);
+}
+}  // namespace
 
 DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<uint64_t> &seqidx) {
   cudaStream_t st = ctx->stream;
@@ -585,11 +632,9 @@ DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<u
                                                       keys.as<unsigned long long>(),
                                                       mins.as<unsigned long long>(), T - 1);
     HD_LAUNCHED(ctx);
-    k_tab_verify<<<grid_for(todo * 32, 256), 256, 0, st>>>(
-        rec.base, rec.bytes, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(),
-        hash.as<uint64_t>(), list, todo, keys.as<unsigned long long>(), mins.as<unsigned long long>(), T - 1,
-        dup.as<uint64_t>(), next, cnt.as<unsigned long long>());
-    HD_LAUNCHED(ctx);
+    verify_round(ctx, rec, hash.as<uint64_t>(), list, todo, keys.as<unsigned long long>(),
+                 mins.as<unsigned long long>(), T - 1, dup.as<uint64_t>(), next,
+                 cnt.as<unsigned long long>());
     uint64_t left = 0;
     HD_CUDA(cudaMemcpyAsync(&left, cnt.p, 8, cudaMemcpyDeviceToHost, st));
     HD_CUDA(cudaStreamSynchronize(st));
@@ -672,11 +717,8 @@ bool IncDedupe::add(hd_ctx *ctx, const Records &rec, std::vector<uint64_t> &seqi
                                                  mins.as<unsigned long long>(), T - 1);
   HD_LAUNCHED(ctx);
   HD_CUDA(cudaMemsetAsync(cnt.p, 0, 16, st));
-  k_tab_verify<<<grid_for(m * 32, 256), 256, 0, st>>>(
-      rec.base, rec.bytes, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(), hp, lp, m,
-      keys.as<unsigned long long>(), mins.as<unsigned long long>(), T - 1, dup.as<uint64_t>(),
-      next.as<uint64_t>(), cnt.as<unsigned long long>());
-  HD_LAUNCHED(ctx);
+  verify_round(ctx, rec, hp, lp, m, keys.as<unsigned long long>(), mins.as<unsigned long long>(),
+               T - 1, dup.as<uint64_t>(), next.as<uint64_t>(), cnt.as<unsigned long long>());
   k_inc_flags<<<grid_for(m, 256), 256, 0, st>>>(dup.as<uint64_t>(), r0, m, flag.as<uint32_t>());
   HD_LAUNCHED(ctx);
   scan_exclusive<uint32_t>(ctx, flag.as<uint32_t>(), uidx.as<uint64_t>(), m,
@@ -831,14 +873,98 @@ __global__ void __launch_bounds__(kPackThreads)
   }
 }
 
+// AND-rule packer without shared memory: a warp job is one 1024-site chunk of
+// one row, and lane l builds its 32-site word l from the chunk's bytes
+// [32 l, 32 l + 32), read as aligned 16-byte vectors (two of its own and the
+// next lane's first; realigned by the row's offset mod 16 with funnel
+// shifts). Each byte is classified by its low three bits, which tell the six
+// symbols apart (A 1, C 3, G 7, T 4, '-' 5): __byte_perm looks up the
+// symbol expected for those bits and its code (A, C, G, T one-hot, '-' 1111),
+// and a byte that is not the expected symbol (N, lowercase, any other) gets
+// 0, as in src/hamming_impl.cc:23-44. Sites past L get the '-' code.
+constexpr uint32_t kExpLo = 0x43004100u, kExpHi = 0x47002D54u;   // '?', A, '?', C | T, '-', '?', G
+constexpr uint32_t kCodeLo = 0x02000100u, kCodeHi = 0x04000F08u;  // 0, 1, 0, 2 | 8, 15, 0, 4
+__device__ __forceinline__ uint32_t and_codes4(uint32_t x) {
+  const uint32_t t = x & 0x07070707u;
+  const uint32_t s = t | (t >> 4);
+  const uint32_t sel = (s & 0xFFu) | ((s >> 8) & 0xFF00u);
+  const uint32_t d = x ^ __byte_perm(kExpLo, kExpHi, sel);
+  // high bit of each byte of nz: the byte is not the expected symbol
+  const uint32_t nz = (((d & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | d) & 0x80808080u;
+  const uint32_t keep = ((nz ^ 0x80808080u) >> 7) * 0xFFu;
+  return __byte_perm(kCodeLo, kCodeHi, sel) & keep;
+}
+__global__ void __launch_bounds__(256)
+    k_pack_and(const uint8_t *base, uint64_t bytes, const uint64_t *rs, const uint64_t *rows,
+               uint64_t n_rows, uint64_t L, uint64_t words, uint4 *g0) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t lo = reinterpret_cast<uint64_t>(base), hi = lo + bytes;
+  const uint64_t chunks = (words + 31) / 32;
+  const uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t job = wid; job < n_rows * chunks; job += nwarps) {
+    const uint64_t u = job / chunks, q = job - u * chunks;
+    const uint64_t r = rows ? rows[u] : u;
+    const uint64_t P0 = lo + rs[r] + q * 1024;  // the chunk's first byte
+    const uint64_t A = P0 & ~15ull;
+    const uint32_t d = (uint32_t)(P0 - A), dw = d >> 2, db = d & 3u;
+    const int64_t rem64 = (int64_t)L - (int64_t)(q * 1024);
+    const uint32_t rem = rem64 <= 0 ? 0u : (rem64 >= 1024 ? 1024u : (uint32_t)rem64);
+    const uint64_t la = A + 32ull * lane;
+    uint32_t w[12];
+    {
+      const uint4 v0 = rem ? load16_in(la, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+      const uint4 v1 = rem ? load16_in(la + 16, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+      uint4 v2;
+      v2.x = __shfl_down_sync(0xffffffffu, v0.x, 1);
+      v2.y = __shfl_down_sync(0xffffffffu, v0.y, 1);
+      v2.z = __shfl_down_sync(0xffffffffu, v0.z, 1);
+      v2.w = __shfl_down_sync(0xffffffffu, v0.w, 1);
+      if (lane == 31) v2 = (rem && d) ? load16_in(la + 32, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+      w[0] = v0.x; w[1] = v0.y; w[2] = v0.z; w[3] = v0.w;
+      w[4] = v1.x; w[5] = v1.y; w[6] = v1.z; w[7] = v1.w;
+      w[8] = v2.x; w[9] = v2.y; w[10] = v2.z; w[11] = v2.w;
+    }
+    // the 36 bytes from byte 4 dw (dw is the same in the whole warp)
+    uint32_t x[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) x[k] = w[k];
+    if (dw == 1) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) x[k] = w[k + 1];
+    } else if (dw == 2) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) x[k] = w[k + 2];
+    } else if (dw == 3) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) x[k] = w[k + 3];
+    }
+    const uint32_t s0 = 32u * lane;  // chunk-relative site of this lane's first byte
+    uint32_t pl[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      uint32_t y = __funnelshift_r(x[k], x[k + 1], 8 * db);
+      const uint32_t sk = s0 + 4 * k;
+      if (sk + 4 > rem) {  // past the row's end: '-'
+        const uint32_t keep = sk >= rem ? 0u : (0xFFFFFFFFu >> (8 * (sk + 4 - rem)));
+        y = (y & keep) | (0x2D2D2D2Du & ~keep);
+      }
+      const uint32_t c = and_codes4(y);
+#pragma unroll
+      for (int p = 0; p < 4; ++p)
+        pl[p] |= ((((c >> p) & 0x01010101u) * 0x01020408u) >> 24) << (4 * k);
+    }
+    const uint64_t wi = q * 32 + lane;
+    if (wi < words) g0[u * words + wi] = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+  }
+}
+
 void pack_rows_and(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, uint64_t n_rows,
                    uint64_t length, uint64_t words, uint4 *g0) {
   if (!n_rows) return;
-  Table256 t;
-  code_table(kCodesAnd, t.v);
-  const uint64_t jobs = n_rows * hd::ceil_div((words + 31) / 32, (uint64_t)kPackCPG);
-  k_pack<4><<<grid_for(jobs * 32, kPackThreads), kPackThreads, 0, ctx->stream>>>(
-      rec.base, rec.rec_start.as<uint64_t>(), d_rows, n_rows, length, words, t, g0, nullptr);
+  const uint64_t jobs = n_rows * ((words + 31) / 32);
+  k_pack_and<<<grid_for(jobs * 32, 256), 256, 0, ctx->stream>>>(
+      rec.base, rec.bytes, rec.rec_start.as<uint64_t>(), d_rows, n_rows, length, words, g0);
   HD_LAUNCHED(ctx);
 }
 
@@ -928,8 +1054,8 @@ void pack_rows(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, hd_align
   uint4 *g0 = aln->plane_buf[0].as<uint4>(), *g1 = aln->plane_buf[1].as<uint4>();
   const uint64_t *rs = rec.rec_start.as<uint64_t>();
   if (aln->planes == 4)
-    k_pack<4><<<grid, kPackThreads, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
-                                             aln->words, t, g0, g1);
+    k_pack_and<<<grid_for(aln->n_rows * ((aln->words + 31) / 32) * 32, 256), 256, 0, ctx->stream>>>(
+        rec.base, rec.bytes, rs, d_rows, aln->n_rows, aln->length, aln->words, g0);
   else if (aln->planes == 5)
     k_pack<5><<<grid, kPackThreads, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
                                              aln->words, t, g0, g1);
