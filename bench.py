@@ -128,6 +128,15 @@ class Clocks:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def wait_first_sample(self, timeout=10.0):
+        t = time.perf_counter() + timeout
+        while self.proc and not self.lines and time.perf_counter() < t:
+            time.sleep(0.01)
+
+    def mark(self):
+        """Samples from here on are the timed region's."""
+        self.first = len(self.lines)
+
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -138,7 +147,9 @@ class Clocks:
             self.proc.kill()
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # the timed region's samples, and the last one before it (the region
+        # is shorter than the 200 ms sampling interval)
+        for ln in self.lines[max(0, getattr(self, "first", 0) - 1):]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -314,6 +325,12 @@ def run_ours(args):
                                         remove_duplicates=True, max_distance=255,
                                         reference_sequence=refq)
 
+        # the clock sampler starts before the warm-up and has answered once
+        # before the timed steps: nvidia-smi's start-up (NVML initialisation)
+        # can hold the driver for tens of ms, which must not fall into them
+        clocks = Clocks(local)
+        clocks.start()
+        clocks.wait_first_sample()
         for _ in range(args.warmup):
             r = step()
         assert r["nsamples"] == n_u, (r["nsamples"], n_u)
@@ -321,8 +338,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         if ws > 1:
             torch.distributed.barrier()
-        clocks = Clocks(local)
-        clocks.start()
+        clocks.mark()
         launches0 = hd._kernel_launches()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()

@@ -11,6 +11,7 @@
 #include <cerrno>
 #include <condition_variable>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <cstdio>
 #include <cstdlib>
@@ -37,6 +38,35 @@ cudaEvent_t trace_event(hd_ctx *ctx, size_t k) {
   return ctx->trace.pool[k];
 }
 }  // namespace
+
+void upload_table(hd_ctx *ctx, void *d_dst, const void *host, size_t bytes, cudaStream_t s) {
+  constexpr int kSlots = 8;
+  constexpr size_t kSlotBytes = 1u << 20;
+  if (bytes > kSlotBytes) {
+    HD_CUDA(cudaMemcpyAsync(d_dst, host, bytes, cudaMemcpyHostToDevice, s));
+    return;
+  }
+  struct Ring {
+    uint8_t *mem = nullptr;
+    cudaEvent_t ev[kSlots] = {};
+    int next = 0;
+  };
+  static std::mutex mu;
+  static std::map<int, Ring> rings;  // per device
+  std::lock_guard<std::mutex> lk(mu);
+  Ring &r = rings[ctx->device];
+  if (!r.mem) {
+    HD_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&r.mem), kSlots * kSlotBytes, cudaHostAllocDefault));
+    for (int k = 0; k < kSlots; ++k) HD_CUDA(cudaEventCreateWithFlags(&r.ev[k], cudaEventDisableTiming));
+  }
+  const int k = r.next;
+  r.next = (k + 1) % kSlots;
+  HD_CUDA(cudaEventSynchronize(r.ev[k]));  // the slot's previous copy has run
+  uint8_t *slot = r.mem + (size_t)k * kSlotBytes;
+  std::memcpy(slot, host, bytes);
+  HD_CUDA(cudaMemcpyAsync(d_dst, slot, bytes, cudaMemcpyHostToDevice, s));
+  HD_CUDA(cudaEventRecord(r.ev[k], s));
+}
 
 void trace_begin(hd_ctx *ctx, const char *call) {
   if (!ctx->trace.on) return;
@@ -427,20 +457,25 @@ hd::Records &file_records(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64
   return *rec;
 }
 
-// Writes zeros over a large host output on up to 16 threads: the first touch
-// of fresh pageable pages costs several ms per 100 MB on one thread. Called
-// after the kernel is launched, so it runs while the GPU computes and the copy
-// back then finds the pages present.
+// Writes one byte of every page of a large host output on up to 16 threads:
+// the first touch of fresh pageable pages costs several ms per 100 MB on one
+// thread, and pages already present (a recycled buffer) cost next to nothing.
+// Called after the kernel is launched, so it runs while the GPU computes and
+// the copy back then finds the pages present.
 void prefault_host(void *p, uint64_t n) {
   const uint64_t kMin = 16ull << 20, kPart = 4ull << 20;
   if (n < kMin) return;
+  static const uint64_t page = [] {
+    const long v = sysconf(_SC_PAGESIZE);
+    return (uint64_t)(v > 0 ? v : 4096);
+  }();
   const unsigned nt = (unsigned)std::min<uint64_t>(16, n / kPart);
-  const uint64_t per = hd::ceil_div(n, nt);
+  const uint64_t per = hd::round_up(hd::ceil_div(n, nt), page);
   std::vector<std::thread> th;
   for (unsigned t = 0; t < nt; ++t)
     th.emplace_back([=] {
       const uint64_t a = t * per, b = std::min(n, a + per);
-      if (a < b) std::memset(static_cast<char *>(p) + a, 0, b - a);
+      for (uint64_t off = a; off < b; off += page) static_cast<volatile char *>(p)[off] = 0;
     });
   for (auto &x : th) x.join();
 }
@@ -1168,9 +1203,22 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
                                     cudaMemcpyDeviceToHost, ctx->up));
       }
     }
+    if (ctx->trace.on) {
+      // the context's stream waits for the distance launches, then for the
+      // copies, so that the trace shows the two apart
+      for (cudaStream_t s : {ctx->side2, ctx->side}) {
+        cudaEvent_t e = sync.make();
+        HD_CUDA(cudaEventRecord(e, s));
+        HD_CUDA(cudaStreamWaitEvent(ctx->stream, e, 0));
+      }
+      hd::trace_mark(ctx, "distances");
+      cudaEvent_t e = sync.make();
+      HD_CUDA(cudaEventRecord(e, ctx->up));
+      HD_CUDA(cudaStreamWaitEvent(ctx->stream, e, 0));
+      hd::trace_mark(ctx, "rest of the copy to host");
+    }
     for (cudaStream_t s : {ctx->side2, ctx->side, ctx->up, ctx->stream})
       HD_CUDA(cudaStreamSynchronize(s));
-    hd::trace_mark(ctx, "distances + copy");
     check_status(ctx);
     // the file and its records stay for later calls on the same file
     ctx->parsed = std::make_shared<hd::Records>(std::move(all));

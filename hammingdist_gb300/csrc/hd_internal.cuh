@@ -153,6 +153,15 @@ struct hd_ctx {
 };
 
 namespace hd {
+// Copies a launch table the planners built on the host to the device on
+// stream s. A copy from pageable memory returns only once the stream has
+// reached it (after the launches queued before it), which would hold the host
+// back; tables up to 1 MB are staged in pinned memory instead (a ring of 8
+// slots per device, kept for the life of the process, each reused once the
+// copy it last staged has run), so the copy is queued like a launch. Larger
+// tables go from pageable memory.
+void upload_table(hd_ctx *ctx, void *d_dst, const void *host, size_t bytes, cudaStream_t s);
+
 // tensor-core multiply-adds counted by the planning kernels (a 64-bit counter
 // in the context's status block, after the status word)
 inline unsigned long long *mma_mac_counter(const hd_ctx *ctx) {

@@ -973,8 +973,8 @@ void prepare_mma_jobs(hd_ctx *ctx, const std::vector<PairJobSpec> &specs, cudaSt
     m.dtype = (uint32_t)sp.dtype;
   }
   std::memcpy(host.data() + tm_bytes + job_bytes, list.data(), list.size() * sizeof(MmaItem));
-  // from pageable memory: the call has consumed `host` when it returns
-  HD_CUDA(cudaMemcpyAsync(dev.p, host.data(), host.size(), cudaMemcpyHostToDevice, stream));
+  // staged in pinned memory (pageable for a large table): `host` may go when this returns
+  upload_table(ctx, dev.p, host.data(), host.size(), stream);
   k_dash_list<<<(unsigned)nj, 32, 0, stream>>>(reinterpret_cast<MmaJob *>(dev.as<uint8_t>() + tm_bytes),
                                               mma_mac_counter(ctx));
   HD_LAUNCHED(ctx);

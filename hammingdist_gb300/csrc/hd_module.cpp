@@ -26,12 +26,14 @@
 #include <fstream>
 #include <iostream>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <sstream>
 #include <stdexcept>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/hammingdist_gb300.h"
@@ -89,8 +91,67 @@ void copy_parallel(void *dst, const void *src, size_t n) {
   });
 }
 
-// Allocator whose resize() leaves new elements uninitialised; result vectors
-// are sized, zeroed in parallel and then filled by the device copy.
+// Large host results are recycled: a released result buffer keeps its pages
+// mapped and present, so that the next result of a similar size is copied
+// back without first-touch page faults (on a fresh 100 MB buffer they cost
+// milliseconds). Buffers of 16 MB or more, at most 4 GB cached, reused for a
+// request of at least half their size.
+class ResultPool {
+ public:
+  static ResultPool &get() {
+    static ResultPool *p = new ResultPool();  // outlives the arrays that return to it
+    return *p;
+  }
+  void *take(size_t bytes) {
+    if (bytes >= kMin) {
+      std::lock_guard<std::mutex> lk(mu_);
+      auto it = free_.lower_bound(bytes);
+      if (it != free_.end() && it->first / 2 <= bytes) {
+        void *p = it->second;
+        cached_ -= it->first;
+        size_[p] = it->first;
+        free_.erase(it);
+        return p;
+      }
+    }
+    void *p = std::malloc(bytes ? bytes : 1);
+    if (!p) throw std::bad_alloc();
+    if (bytes >= kMin) {
+      std::lock_guard<std::mutex> lk(mu_);
+      size_[p] = bytes;
+    }
+    return p;
+  }
+  void give(void *p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    auto s = size_.find(p);
+    if (s == size_.end()) {
+      std::free(p);
+      return;
+    }
+    const size_t bytes = s->second;
+    size_.erase(s);
+    free_.emplace(bytes, p);
+    cached_ += bytes;
+    while (cached_ > kCap && !free_.empty()) {  // drop the largest first
+      auto last = std::prev(free_.end());
+      cached_ -= last->first;
+      std::free(last->second);
+      free_.erase(last);
+    }
+  }
+
+ private:
+  static constexpr size_t kMin = 16u << 20, kCap = 4ull << 30;
+  std::mutex mu_;
+  std::multimap<size_t, void *> free_;     // size -> released buffer
+  std::unordered_map<void *, size_t> size_;  // buffer in use -> its size
+  size_t cached_ = 0;
+};
+
+// Allocator whose resize() leaves new elements uninitialised (result vectors
+// are filled by the device copy), drawing large buffers from the ResultPool.
 template <class T>
 struct NoInitAlloc : std::allocator<T> {
   using value_type = T;
@@ -101,6 +162,8 @@ struct NoInitAlloc : std::allocator<T> {
   NoInitAlloc() = default;
   template <class U>
   NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
+  T *allocate(size_t n) { return static_cast<T *>(ResultPool::get().take(n * sizeof(T))); }
+  void deallocate(T *p, size_t) noexcept { ResultPool::get().give(p); }
   template <class U>
   void construct(U *p) noexcept {
     ::new (static_cast<void *>(p)) U;

@@ -422,8 +422,8 @@ void prepare_pairwise_jobs(hd_ctx *ctx, std::vector<PairJobSpec> &specs, cudaStr
       tiles += (unsigned long long)s.tile_hi * (s.tile_hi + 1) / 2 -
                (unsigned long long)s.tile_lo * (s.tile_lo + 1) / 2;
     }
-    // from pageable memory: the call has consumed `host` when it returns
-    HD_CUDA(cudaMemcpyAsync(dev.p, host.data(), host.size(), cudaMemcpyHostToDevice, stream));
+    // staged in pinned memory (pageable for a large table): `host` may go when this returns
+    upload_table(ctx, dev.p, host.data(), host.size(), stream);
     PairLaunchPlan::Launch L;
     L.fn = reinterpret_cast<const void *>(v.fn);
     L.smem = v.smem;

@@ -71,9 +71,9 @@ __global__ void k_random_planes(uint4 *p, uint64_t n_words, uint64_t seed) {
   }
 }
 
-// Best of four timed runs (after a warm-up run) of `copies` matrices of the
-// alignment in one launch plan, with engine choice `engine` (-1 as
-// configured, 0 bit-plane only, 1 tensor cores).
+// Best of four timed runs (after a warm-up run) of the launches of `copies`
+// matrices of the alignment in one launch plan, with engine choice `engine`
+// (-1 as configured, 0 bit-plane only, 1 tensor cores).
 double time_config(hd_ctx *ctx, const hd_alignment &a, int copies, int dtype, TileConfig tc,
                    DevBuf &out, int engine = 0) {
   struct Restore {
@@ -100,9 +100,12 @@ double time_config(hd_ctx *ctx, const hd_alignment &a, int copies, int dtype, Ti
   HD_CUDA(cudaEventCreate(&e1));
   double best = 1e30;
   for (int rep = 0; rep < 5; ++rep) {
+    // the launches alone: planning (tables, operands) happens before
     std::vector<PairJobSpec> sp = specs;
+    PairLaunchPlan plan;
+    prepare_pairwise_jobs(ctx, sp, ctx->stream, &plan);
     HD_CUDA(cudaEventRecord(e0, ctx->stream));
-    run_pairwise_jobs(ctx, sp, ctx->stream, nullptr);
+    launch_pairwise_plan(ctx, plan, ctx->stream);
     HD_CUDA(cudaEventRecord(e1, ctx->stream));
     HD_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
