@@ -207,8 +207,9 @@ def measured_peaks():
 #       python bench.py --kernel-only --n 14000 --steps 1 --warmup 1
 # bench.py cannot run ncu itself, so the figure is a constant of the kernel
 # build it was measured on (KERNEL_DRAM_SOURCE).
-KERNEL_DRAM_BYTES = 20_063_901_440
-KERNEL_DRAM_SOURCE = "ncu capture of k_pairwise_mma (FP8 operand), n=14000 L=29903, one launch"
+KERNEL_DRAM_BYTES = 7_728_499_200
+KERNEL_DRAM_SOURCE = ("ncu capture of k_pairwise_mma (FP4 operand, dash products of marked "
+                      "chunks only), n=14000 L=29903, one launch: 7.628 GB read + 0.101 GB written")
 
 
 # ------------------------------------------------------------------ CPU leg
@@ -524,6 +525,38 @@ def run_kernel_only(args):
     print(json.dumps({"mode": "kernel-only", "n": n, "L": args.L, "dtype": args.dtype,
                       "kernel_ms": mean, "pair_sites_T": pairs * args.L / (mean / 1e3) / 1e12,
                       "launches": ctx.kernel_launches}), flush=True)
+    ctx.close()
+
+
+def run_ingest_only(args):
+    """Ingest alone (profiling harness): the workload's generator with --n
+    records (30% duplicates) of L sites, the FASTA resident in HBM; warmup +
+    steps of alignment_from_fasta (newline index, records, dedupe, pack) and
+    the reference distances of the root against the resident rows, each
+    step's phases traced (CUDA events on the library's stream)."""
+    import torch
+
+    from hammingdist_gb300 import abi
+
+    synth = synth_module()
+    rows, root, _ = synth.alignment(args.n, args.L, p=P_SUB, seed=SEED, dup_frac=DUP)
+    fa = synth.to_fasta(rows)
+    del rows
+    ctx = abi.Context(0)
+    d_fa = torch.frombuffer(bytearray(fa), dtype=torch.uint8).to("cuda:0")
+    torch.cuda.synchronize()
+    ctx.trace(True)
+    traces = []
+    for k in range(args.warmup + args.steps):
+        a = ctx.alignment_from_fasta(d_fa.data_ptr(), len(fa), on_device=True,
+                                     remove_duplicates=True)
+        t = ctx.trace_last()
+        ctx.alignment_reference_distances(a, root.tobytes())
+        a.free()
+        if k >= args.warmup:
+            traces.append(t)
+    print(json.dumps({"mode": "ingest-only", "records": args.n, "L": args.L,
+                      "fasta_bytes": len(fa), "trace": traces[-1]}), flush=True)
     ctx.close()
 
 
@@ -993,6 +1026,8 @@ def main():
                     help="leave out the config 1 / 4 / 5 legs of the default line")
     ap.add_argument("--extra-serve-seconds", type=float, default=15.0,
                     help="length of the paced serving stream in the default line")
+    ap.add_argument("--ingest-only", action="store_true",
+                    help="profiling harness: device ingest of --n records and reference distances")
     ap.add_argument("--kernel-only", action="store_true",
                     help="profiling harness: the pairwise kernel alone on --n distinct rows")
     ap.add_argument("--n", type=int, default=12000)
@@ -1032,6 +1067,8 @@ def main():
         run_batched(args)
     elif args.kernel_only:
         run_kernel_only(args)
+    elif args.ingest_only:
+        run_ingest_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
