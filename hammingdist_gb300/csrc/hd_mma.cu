@@ -135,7 +135,7 @@ struct MmaJob {
 struct MmaItem {
   uint32_t job;
   uint32_t I;       // first 128-row tile
-  uint32_t J;       // 256-column tile
+  uint32_t J;       // kTN-column tile
   uint32_t halves;  // row tiles in the item: 1 or 2
 };
 

@@ -237,7 +237,7 @@ int hd_write_sparse(hd_ctx *ctx, const void *lt, uint64_t nsamples,
  *    any work. The scratch is a fixed ~4.2 MB device array in the library,
  *    held on every GPU that loads it until the process exits.
  *  - The first call on a device looks up that array's device address (once
- *    per device); make that first call before any stream capture.
+ *    per device).
  *  - *text_bytes receives the text size; if it exceeds text_capacity the
  *    call fails with HD_ERR_ARG and writes no text.
  *  - All calls share the one scratch array: calls that overlap on the GPU
