@@ -673,8 +673,24 @@ void reference_distances_of(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, cons
       DevBuf d_ref(ref_len + 16, ctx->stream), d_out(rec.n * 4, ctx->stream);
       if (ref_len)
         HD_CUDA(cudaMemcpyAsync(d_ref.p, ref, ref_len, cudaMemcpyHostToDevice, ctx->stream));
-      hd::reference_distances_device(ctx, rec, d_ref.as<uint8_t>(), include_x, d_out.as<uint32_t>());
-      hd::trace_mark(ctx, "distances");
+      // Records all of the reference's length, whose dense-rule rows a
+      // from_fasta of this file left: without include_x the rule of
+      // src/hamming.cc:128-136 counts a site exactly when the two codes share
+      // no bit (a '-' shares bits with every symbol; equal symbols share
+      // theirs; every other byte has code 0), so the distances are the rows'
+      // dense distances to the packed reference
+      const hd_alignment *rows = rec.rows.get();
+      if (rows && !include_x && rec.all_equal && rec.len0 == ref_len && rows->length == ref_len &&
+          rows->n_input == rec.n) {
+        DevBuf d_rows(rows->n_rows * 4, ctx->stream);
+        hd::query_rows_to_records(ctx, rows, d_ref.as<uint8_t>(), d_rows.as<uint32_t>(),
+                                  rec.row_of.as<uint64_t>(), rec.n, d_out.as<uint32_t>());
+        hd::trace_mark(ctx, "distances from the resident rows");
+      } else {
+        hd::reference_distances_device(ctx, rec, d_ref.as<uint8_t>(), include_x,
+                                       d_out.as<uint32_t>());
+        hd::trace_mark(ctx, "distances");
+      }
       HD_CUDA(cudaMemcpyAsync(h, d_out.p, rec.n * 4, cudaMemcpyDeviceToHost, ctx->stream));
       hd::trace_mark(ctx, "copy to host");
       HD_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -954,11 +970,14 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     // first's tail), split at 90% of the rows, so that the copy of every
     // finished range to the host overlaps the rest of the distances.
     // part ends as fractions of the file (HAMMINGDIST_STREAM_SPLITS="f1,f2,...",
-    // increasing, at most 3). At n=20,000 x L=29,903 the bench step took
-    // 15.92-15.98 ms with splits at 10%, 30% and 60%, 16.2-16.5 at 20% and
-    // 50%, and 16.5-17.9 at the other three-split settings tried; a small
-    // first part shortens the ingest that nothing overlaps.
-    std::vector<double> ends = {0.1, 0.3, 0.6};
+    // increasing, at most 3). At n=20,000 x L=29,903 the file-to-host step
+    // (with the reference distances) took 8.39 ms with splits at 30% and 60%,
+    // 8.60-8.74 at 20-25% and 50-55%, 8.69 at 10%, 30% and 60%, 8.71 at 50%
+    // alone and 8.9-9.0 with a first part of 15%; without a split, 10.26 ms.
+    // Each part's ingest costs launches and host round trips whatever its
+    // size, and the tensor-core distances of the earlier parts finish before
+    // the next part is ingested, so a few large parts do best.
+    std::vector<double> ends = {0.3, 0.6};
     if (const char *e = std::getenv("HAMMINGDIST_STREAM_SPLITS")) {
       ends.clear();
       for (const char *q = e; *q && ends.size() < 3;) {
@@ -1015,6 +1034,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     };
     uint64_t L = 0, words = 0, R_max = 0, K = 0, B_prev = 0, tiles = 0;
     uint32_t T = 0, t_done = 0;
+    cudaEvent_t last_packed = nullptr;  // every row packed
     bool use_mma = false;  // tensor-core engine: 128-row tiles
     // SMs left to the next part's ingest while a band runs
     // (HAMMINGDIST_STREAM_FREE_SMS, default 16)
@@ -1114,7 +1134,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       const uint64_t *rows = iota.as<uint64_t>();
       if (remove_duplicates) {
         if (c == 0) inc.init(ctx, R_max);
-        if (inc_ok && inc.add(ctx, all, seq)) {
+        if (inc_ok && inc.add(ctx, all)) {
           Kc = inc.n_unique;
           rows = inc.unique_rec.as<uint64_t>();
         } else {
@@ -1159,12 +1179,13 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         B_prev = B;
         continue;
       }
+      last_packed = sync.make();
+      HD_CUDA(cudaEventRecord(last_packed, ctx->stream));
       const uint32_t t_end = K >= 2 ? (uint32_t)hd::ceil_div(K, T) : t_done;
       if (t_end > t_done) {
         const uint32_t t_split =
             std::max(t_done + 1, (uint32_t)std::ceil(0.9 * (double)t_end));
-        cudaEvent_t packed = sync.make();
-        HD_CUDA(cudaEventRecord(packed, ctx->stream));
+        cudaEvent_t packed = last_packed;
         if (t_split < t_end) {
           launch(t_done, t_split, K, ctx->side2, 0, packed);
           launch(t_split, t_end, K, ctx->stream, 0, nullptr);
@@ -1176,13 +1197,47 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     }
     owner->n_rows = K;
     owner->n_input = all.n;
-    owner->seqidx = std::move(seq);
-    if (!owner->seqidx.empty()) {
-      owner->d_seqidx = DevBuf(owner->seqidx.size() * 8, ctx->stream);
-      HD_CUDA(cudaMemcpyAsync(owner->d_seqidx.p, owner->seqidx.data(), owner->seqidx.size() * 8,
-                              cudaMemcpyHostToDevice, ctx->stream));
+    // each record's row: on the device (the incremental dedupe's rowid,
+    // copied to the host once the launches are done), or from the full dedupe
+    // on the host
+    const bool inc_rows = remove_duplicates && inc_ok;
+    if (remove_duplicates) {
+      owner->d_seqidx = DevBuf(all.n * 8, ctx->stream);
+      if (inc_rows) {
+        HD_CUDA(cudaMemcpyAsync(owner->d_seqidx.p, inc.rowid.p, all.n * 8, cudaMemcpyDeviceToDevice,
+                                ctx->stream));
+      } else {
+        owner->seqidx = std::move(seq);
+        HD_CUDA(cudaMemcpyAsync(owner->d_seqidx.p, owner->seqidx.data(), all.n * 8,
+                                cudaMemcpyHostToDevice, ctx->stream));
+      }
     }
     ctx->last_pair_tiles = tiles;
+    // a copy of the rows stays with the file's records, for the reference
+    // distances of the same file (fasta_reference_distances after from_fasta):
+    // copied on the upload stream while the distances run
+    if (K && last_packed) {
+      auto keep = std::make_shared<hd_alignment>();
+      keep->ctx = ctx;
+      keep->device = ctx->device;
+      keep->length = L;
+      keep->words = words;
+      keep->n_rows = K;
+      keep->n_input = all.n;
+      keep->plane_buf[0] = DevBuf(K * words * 16, ctx->up);
+      HD_CUDA(cudaStreamWaitEvent(ctx->up, last_packed, 0));
+      HD_CUDA(cudaMemcpyAsync(keep->plane_buf[0].p, g0, K * words * 16, cudaMemcpyDeviceToDevice,
+                              ctx->up));
+      if (remove_duplicates) {
+        all.row_of = DevBuf(all.n * 8, ctx->up);
+        if (inc_rows)  // last_packed follows the dedupe
+          HD_CUDA(cudaMemcpyAsync(all.row_of.p, inc.rowid.p, all.n * 8, cudaMemcpyDeviceToDevice,
+                                  ctx->up));
+        else
+          hd::upload_table(ctx, all.row_of.p, owner->seqidx.data(), all.n * 8, ctx->up);
+      }
+      all.rows = std::move(keep);
+    }
     // each finished range of rows is copied to the host on the upload stream
     // once its launch is done, while the later ones compute
     const uint64_t entries = K < 2 ? 0 : tri(K);
@@ -1220,6 +1275,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     for (cudaStream_t s : {ctx->side2, ctx->side, ctx->up, ctx->stream})
       HD_CUDA(cudaStreamSynchronize(s));
     check_status(ctx);
+    if (inc_rows) inc.rows(ctx, owner->seqidx);
     // the file and its records stay for later calls on the same file
     ctx->parsed = std::make_shared<hd::Records>(std::move(all));
     ctx->parsed_tag = tag;

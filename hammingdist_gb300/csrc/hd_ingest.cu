@@ -377,25 +377,35 @@ __device__ inline uint32_t load4_in(uint64_t x, uint64_t lo, uint64_t hi) {
 // Hash of each record's bytes: a sum over its 4-byte groups (relative to the
 // record start; a short last group is zero-filled) of the 64-bit product of
 // the group XORed with two position-keyed 32-bit constants, then one 64-bit
-// mix of the sum and the length. Different records rarely share a hash, and
-// equal hashes are verified byte by byte, so a collision costs a verify
-// round, never a wrong answer. The warp reads the record with
-// aligned 16-byte loads (two 512-byte blocks per step); a lane's groups start
-// at byte P mod 4 of its words and are realigned with a funnel shift and the
-// next lane's first word.
-__global__ void k_hash(const uint8_t *base, uint64_t bytes, const uint64_t *rs, const uint64_t *rl,
-                       uint64_t R, uint64_t *out) {
+// mix of the sum and the length (k_hash_fin). Different records rarely share
+// a hash, and equal hashes are verified byte by byte, so a collision costs a
+// verify round, never a wrong answer. The sum does not depend on the order of
+// its terms, so a record is hashed in segments of kHashSeg bytes, one warp
+// each, that add their partial sums to acc[r] (zeroed first): many warps per
+// record keep enough loads in flight however few records there are. Block
+// (x, y) takes records 8x .. 8x + 7 (one per warp) from byte y kHashSeg on.
+// The warp reads its segment with aligned 16-byte loads (two 512-byte blocks
+// per step); a lane's groups start at byte P mod 4 of its words (P the
+// record's start) and are realigned with a funnel shift and the next lane's
+// first word.
+constexpr uint64_t kHashSeg = 4096;
+constexpr int kHashWarps = 8;
+__global__ void __launch_bounds__(32 * kHashWarps)
+    k_hash(const uint8_t *base, uint64_t bytes, const uint64_t *rs, const uint64_t *rl, uint64_t R,
+           unsigned long long *acc) {
   const int lane = threadIdx.x & 31;
+  const uint64_t r = (uint64_t)blockIdx.x * kHashWarps + (threadIdx.x >> 5);
+  if (r >= R) return;  // warp-uniform
   const uint64_t lo = reinterpret_cast<uint64_t>(base), hi = lo + bytes;
-  uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
-  for (uint64_t r = wid; r < R; r += nwarps) {
-    const uint64_t P = lo + rs[r];
-    const uint64_t len = rl[r];
+  const uint64_t len = rl[r];
+  for (uint64_t s_lo = (uint64_t)blockIdx.y * kHashSeg; s_lo < len;
+       s_lo += (uint64_t)gridDim.y * kHashSeg) {
+    const uint64_t s_hi = len - s_lo < kHashSeg ? len : s_lo + kHashSeg;
+    const uint64_t P = lo + rs[r] + s_lo;  // the record's byte s_lo
     const uint64_t A = P & ~15ull;
     const uint32_t h4 = (uint32_t)(P & 3);
-    const int64_t rel0 = -(int64_t)(P - A);  // position of A relative to the record
-    const uint64_t span = P + len - A;
+    const int64_t rel0 = (int64_t)s_lo - (int64_t)(P - A);  // position of A in the record
+    const uint64_t span = P + (s_hi - s_lo) - A;
     uint64_t h = 0;
     for (uint64_t b0 = 0; b0 < span; b0 += 512 * kHashU) {
       uint4 v[kHashU];
@@ -415,8 +425,8 @@ __global__ void k_hash(const uint8_t *base, uint64_t bytes, const uint64_t *rs, 
         const int64_t lane_rel = rel0 + (int64_t)(b0 + 512 * k + 16 * lane);
 #pragma unroll
         for (int g = 0; g < 4; ++g) {
-          const int64_t s = lane_rel + h4 + 4 * g;
-          if (s < 0 || s >= (int64_t)len) continue;
+          const int64_t s = lane_rel + h4 + 4 * g;  // the group's position in the record
+          if (s < (int64_t)s_lo || s >= (int64_t)s_hi) continue;
           uint32_t w = __funnelshift_r(wd[g], wd[g + 1], 8 * h4);
           const int64_t left = (int64_t)len - s;
           if (left < 4) w &= (1u << (8 * left)) - 1u;
@@ -428,11 +438,32 @@ __global__ void k_hash(const uint8_t *base, uint64_t bytes, const uint64_t *rs, 
       }
     }
     h = warp_sum(h);
-    if (lane == 0) {
-      uint64_t v = mix64(h ^ (len * 0xd6e8feb86659fd93ull));
-      out[r] = v == kEmpty ? v - 1 : v;
-    }
+    if (lane == 0 && h) atomicAdd(&acc[r], (unsigned long long)h);
   }
+}
+// The record hashes from the sums k_hash left in h[r], in place.
+__global__ void k_hash_fin(const uint64_t *rl, uint64_t R, unsigned long long *h) {
+  const uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  const uint64_t v = mix64(h[r] ^ (rl[r] * 0xd6e8feb86659fd93ull));
+  h[r] = v == kEmpty ? v - 1 : v;
+}
+// Hashes of records [0, R) of rs/rl into out (R > 0).
+void hash_records(hd_ctx *ctx, const Records &rec, const uint64_t *rs, const uint64_t *rl,
+                  uint64_t R, uint64_t *out) {
+  cudaStream_t st = ctx->stream;
+  HD_CUDA(cudaMemsetAsync(out, 0, R * 8, st));
+  unsigned long long *h = reinterpret_cast<unsigned long long *>(out);
+  if (rec.max_len) {
+    const uint64_t X = ceil_div(R, (uint64_t)kHashWarps), S = ceil_div(rec.max_len, kHashSeg);
+    if (X > 0x7fffffffull) fail(HD_ERR_ARG, "too many records");
+    // segments past 65,535 are taken by the warps' loop
+    k_hash<<<dim3((unsigned)X, (unsigned)std::min<uint64_t>(S, 65535)), 32 * kHashWarps, 0, st>>>(
+        rec.base, rec.bytes, rs, rl, R, h);
+    HD_LAUNCHED(ctx);
+  }
+  k_hash_fin<<<grid_for(R, 256), 256, 0, st>>>(rl, R, h);
+  HD_LAUNCHED(ctx);
 }
 
 __device__ inline uint64_t slot_of(uint64_t h, uint64_t mask) { return (h ^ (h >> 29)) & mask; }
@@ -617,10 +648,8 @@ DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<u
   DevBuf hash(R * 8, st), dup(R * 8, st), keys(T * 8, st), mins(T * 8, st);
   DevBuf lists[2] = {DevBuf(R * 8, st), DevBuf(R * 8, st)};
   DevBuf cnt(8, st);
-  unsigned warps_grid = grid_for(R * 32, 256);
-  k_hash<<<warps_grid, 256, 0, st>>>(rec.base, rec.bytes, rec.rec_start.as<uint64_t>(),
-                                     rec.rec_len.as<uint64_t>(), R, hash.as<uint64_t>());
-  HD_LAUNCHED(ctx);
+  hash_records(ctx, rec, rec.rec_start.as<uint64_t>(), rec.rec_len.as<uint64_t>(), R,
+               hash.as<uint64_t>());
   uint64_t todo = R;
   const uint64_t *list = nullptr;
   for (int round = 0; todo; ++round) {
@@ -701,15 +730,14 @@ void IncDedupe::init(hd_ctx *ctx, uint64_t capacity) {
   n_unique = 0;
 }
 
-bool IncDedupe::add(hd_ctx *ctx, const Records &rec, std::vector<uint64_t> &seqidx) {
+bool IncDedupe::add(hd_ctx *ctx, const Records &rec) {
   cudaStream_t st = ctx->stream;
   const uint64_t r0 = seen, m = rec.n - seen;
   if (rec.n < seen || rec.n > cap) return false;
   if (m == 0) return true;
   uint64_t *hp = hash.as<uint64_t>(), *lp = list.as<uint64_t>();
-  k_hash<<<grid_for(m * 32, 256), 256, 0, st>>>(rec.base, rec.bytes, rec.rec_start.as<uint64_t>() + r0,
-                                                rec.rec_len.as<uint64_t>() + r0, m, hp + r0);
-  HD_LAUNCHED(ctx);
+  hash_records(ctx, rec, rec.rec_start.as<uint64_t>() + r0, rec.rec_len.as<uint64_t>() + r0, m,
+               hp + r0);
   k_iota<<<grid_for(m, 256), 256, 0, st>>>(lp, r0, m);
   HD_LAUNCHED(ctx);
   // earlier records hold the smaller indices: they stay each hash's minimum
@@ -734,13 +762,16 @@ bool IncDedupe::add(hd_ctx *ctx, const Records &rec, std::vector<uint64_t> &seqi
   HD_LAUNCHED(ctx);
   k_inc_link<<<grid_for(m, 256), 256, 0, st>>>(dup.as<uint64_t>(), r0, m, rowid.as<uint64_t>());
   HD_LAUNCHED(ctx);
-  seqidx.resize(rec.n);
-  HD_CUDA(cudaMemcpyAsync(seqidx.data() + r0, rowid.as<uint64_t>() + r0, m * 8,
-                          cudaMemcpyDeviceToHost, st));
-  HD_CUDA(cudaStreamSynchronize(st));
   n_unique += h[1];
   seen = rec.n;
   return true;
+}
+
+void IncDedupe::rows(hd_ctx *ctx, std::vector<uint64_t> &seqidx) {
+  seqidx.resize(seen);
+  if (!seen) return;
+  HD_CUDA(cudaMemcpyAsync(seqidx.data(), rowid.p, seen * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  HD_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 // -------------------------------------------------------------- consensus
@@ -1233,6 +1264,21 @@ void query_distances_async(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *
   k_query<<<grid_for(aln->n_rows * 32, 256), 256, 0, ctx->stream>>>(
       static_cast<const uint4 *>(aln->planes_ptr(0)), aln->words, aln->n_rows,
       q_planes.as<uint4>(), d_out_rows);
+  HD_LAUNCHED(ctx);
+}
+
+// out[r] = the distance of record r's row
+__global__ void k_gather_rows(const uint32_t *row_dist, const uint64_t *row_of, uint64_t n,
+                              uint32_t *out) {
+  const uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (r < n) out[r] = row_dist[row_of ? row_of[r] : r];
+}
+
+void query_rows_to_records(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
+                           uint32_t *d_rows, const uint64_t *row_of, uint64_t n, uint32_t *d_out) {
+  DevBuf q;  // freed after the kernels in stream order
+  query_distances_async(ctx, aln, d_query, d_rows, q);
+  k_gather_rows<<<grid_for(n, 256), 256, 0, ctx->stream>>>(d_rows, row_of, n, d_out);
   HD_LAUNCHED(ctx);
 }
 

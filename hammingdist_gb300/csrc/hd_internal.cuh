@@ -381,6 +381,11 @@ struct Records {
   uint64_t bytes = 0;         // readable bytes from base: [base, base + bytes)
   DevBuf rec_start, rec_len;  // uint64 [n]
   DevBuf gathered;            // concatenation when records span several lines
+  // the dense-rule rows of these records, when the call that parsed them
+  // built them (row_of[r]: device row of record r; none: row r): reference
+  // distances of the same file read these instead of the records' bytes
+  std::shared_ptr<hd_alignment> rows;
+  DevBuf row_of;
 };
 
 // Character codes of the rules (bit p = bit plane p); '-' is all ones.
@@ -402,14 +407,16 @@ DevBuf dedupe(hd_ctx *ctx, const Records &rec, uint64_t *n_unique, std::vector<u
 // verifies only the records after them. Earlier records hold the smaller
 // indices, so they stay the first occurrences and their rows keep their
 // numbers; unique_rec lists the unique rows' records (n_unique of them) and
-// seqidx receives each new record's row. A new record unlike the first
-// record of its hash (a 64-bit collision), or more records than the
-// capacity, makes add() return false: the caller runs the full dedupe.
+// rowid (device) each record's row, which rows() copies to the host. A new
+// record unlike the first record of its hash (a 64-bit collision), or more
+// records than the capacity, makes add() return false: the caller runs the
+// full dedupe.
 struct IncDedupe {
   DevBuf hash, dup, rowid, unique_rec, list, next, flag, uidx, keys, mins, cnt;
   uint64_t cap = 0, T = 0, seen = 0, n_unique = 0;
   void init(hd_ctx *ctx, uint64_t capacity);
-  bool add(hd_ctx *ctx, const Records &rec, std::vector<uint64_t> &seqidx);
+  bool add(hd_ctx *ctx, const Records &rec);
+  void rows(hd_ctx *ctx, std::vector<uint64_t> &seqidx);  // records [0, seen)
 };
 // Sum over sites of the most frequent of A/C/G/T among the given rows.
 uint64_t consensus_matches(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows,
@@ -430,6 +437,11 @@ void reference_distances_device(hd_ctx *ctx, const Records &rec, const uint8_t *
                                 int include_x, uint32_t *d_out);
 void alignment_query_distances(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
                                uint32_t *d_out_rows);
+// the query's distance to every row (d_rows, n_rows entries), then per record
+// r < n the distance of its row (row_of[r], or row r without row_of) into
+// d_out; queued on the context's stream
+void query_rows_to_records(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
+                           uint32_t *d_rows, const uint64_t *row_of, uint64_t n, uint32_t *d_out);
 // same without synchronising: q_planes holds the packed query until the caller syncs
 void query_distances_async(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *d_query,
                            uint32_t *d_out_rows, DevBuf &q_planes);

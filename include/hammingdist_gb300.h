@@ -131,7 +131,7 @@ int hd_alignment_from_fasta_file(hd_ctx *ctx, const char *path, int remove_dupli
  * alignment (sequence indices; free it with hd_alignment_free). out_fn is
  * then asked for HD_OUTPUT_MIRROR (see there). For a file of 64 MB or more
  * the distances overlap the read: the file is ingested in parts that end at
- * record headers (by default after ~10%, ~30% and ~60% of its bytes;
+ * record headers (by default after ~30% and ~60% of its bytes;
  * HAMMINGDIST_STREAM_SPLITS sets up to three splits); after each part the
  * unique rows so far (the first rows of the final result) are packed and the
  * tile rows that are complete run while the rest is read, and finished
@@ -258,7 +258,11 @@ int hd_reference_distances(hd_ctx *ctx, const char *ref, uint64_t ref_len,
                            const char *fasta, uint64_t nbytes, int include_x,
                            uint32_t **out, uint64_t *n_out);
 /* The same from a FASTA file, read as in hd_alignment_from_fasta_file
- * (reusing the device bytes of the same unchanged file). */
+ * (reusing the device bytes of the same unchanged file). After
+ * hd_pairwise_lt_fasta_file on the same unchanged file, with include_x = 0
+ * and `ref` as long as the records, the distances come from the packed rows
+ * that call left (the rule then equals the dense AND rule), not from the
+ * records' bytes; the results are the same. */
 int hd_reference_distances_file(hd_ctx *ctx, const char *ref, uint64_t ref_len,
                                 const char *path, int include_x, uint32_t **out,
                                 uint64_t *n_out);

@@ -1,6 +1,6 @@
 """from_fasta with the distances overlapping the read (hd_pairwise_lt_fasta_file):
 for files of 64 MB or more the file is ingested in parts (by default split
-after ~10%, ~30% and ~60% of its bytes; HAMMINGDIST_STREAM_SPLITS sets up to
+after ~30% and ~60% of its bytes; HAMMINGDIST_STREAM_SPLITS sets up to
 three),
 and each part's complete tile rows run while the rest is read. Every result
 must equal the plain order (read, ingest, distances) bit for bit: duplicates
@@ -95,6 +95,37 @@ def test_already_on_device_and_reference_after(ctx, big):
     a2.free()
 
 
+@pytest.mark.parametrize("dedup", [True, False])
+def test_reference_after_uses_resident_rows(ctx, big, dedup):
+    # after the streamed call, fasta_reference_distances of the same file with
+    # a reference of the records' length reads the rows that call packed; a
+    # reference with '-', N, X, lowercase and other bytes, include_x, a longer
+    # reference and a changed file take the records' bytes; every result
+    # equals the oracle's
+    path, fa, rows = big
+    _touch(path)
+    lt, aln = ctx.pairwise_lt_fasta_file(path, remove_duplicates=dedup)
+    aln.free()
+    ref = bytearray(rows[5].tobytes())
+    ref[0:40] = b"-" * 40
+    ref[100:104] = b"NXac"
+    ref[2000:2003] = b"*?-"
+    ref = bytes(ref)
+    ctx.trace(True)
+    try:
+        for r, ix, resident in ((ref, False, True), (rows[0].tobytes(), False, True),
+                                (ref, True, False), (ref + b"A", False, False)):
+            got = ctx.reference_distances_file(r, path, include_x=ix)
+            assert ("from the resident rows" in ctx.trace_last()) == resident
+            np.testing.assert_array_equal(got, o.reference_distances(r, fa, include_x=ix))
+        _touch(path)  # changed: read and parsed again, the rows are gone
+        got = ctx.reference_distances_file(ref, path)
+        assert "from the resident rows" not in ctx.trace_last()
+        np.testing.assert_array_equal(got, o.reference_distances(ref, fa))
+    finally:
+        ctx.trace(False)
+
+
 def test_multiline_falls_back(ctx, tmp_path):
     rows, _, _ = synth.alignment(2500, 29903, p=1e-3, seed=42, dup_frac=0.2)
     out = bytearray()
@@ -145,11 +176,12 @@ def test_module_from_fasta_uses_it(big):
 
 
 @pytest.mark.parametrize("where", [0.35, 0.8])
-def test_multiline_record_in_a_later_part(ctx, tmp_path, where):
+def test_multiline_record_in_a_later_part(ctx, tmp_path, monkeypatch, where):
     # the file is ingested in parts that end after 10%, 30% and 60% of its
     # bytes: one multi-line record in the third or fourth part, found after
     # earlier parts' distances have started, still gives the plain order's
     # results
+    monkeypatch.setenv("HAMMINGDIST_STREAM_SPLITS", "0.1,0.3,0.6")
     rows, _, _ = synth.alignment(2500, 29903, p=1e-3, seed=43, dup_frac=0.2)
     k0 = int(where * len(rows))
     out = bytearray()
@@ -168,11 +200,16 @@ def test_multiline_record_in_a_later_part(ctx, tmp_path, where):
     aln.free()
 
 
-@pytest.mark.parametrize("where", [0.35, 0.7])
-def test_error_in_a_part(ctx, tmp_path, big, where):
-    # a short record in the third or the fourth part (default splits at 10%,
-    # 30% and 60%)
+@pytest.mark.parametrize("splits,where", [("0.1,0.3,0.6", 0.35), ("0.1,0.3,0.6", 0.7),
+                                          ("", 0.45), ("", 0.7)])
+def test_error_in_a_part(ctx, tmp_path, big, monkeypatch, splits, where):
+    # a short record in the third or the fourth part (splits at 10%, 30% and
+    # 60%), or in the second or the last part (the default splits, 30% and
+    # 60%)
     from hammingdist_gb300 import abi
+
+    if splits:
+        monkeypatch.setenv("HAMMINGDIST_STREAM_SPLITS", splits)
 
     path, fa, rows = big
     cut = fa.index(b"\n>", int(where * len(fa))) + 1  # a record header
@@ -189,8 +226,8 @@ def test_error_in_a_part(ctx, tmp_path, big, where):
 
 @pytest.mark.parametrize("splits", ["", "0.5", "0.2,0.5", "0.25,0.5,0.75", "0.9"])
 def test_every_split_setting(ctx, big, monkeypatch, splits):
-    # no split (one part), one, two and three splits (the default is three:
-    # 10%, 30%, 60%): the same matrix and sequence indices as the plain order
+    # no split (one part), one, two and three splits (the default is two:
+    # 30%, 60%): the same matrix and sequence indices as the plain order
     path, fa, rows = big
     monkeypatch.setenv("HAMMINGDIST_STREAM_SPLITS", splits)
     _touch(path)
