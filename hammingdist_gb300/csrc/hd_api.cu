@@ -73,6 +73,9 @@ void trace_begin(hd_ctx *ctx, const char *call) {
   if (ctx->trace.call) nvtxRangePop();  // an earlier call ended by an error
   ctx->trace.call = call;
   ctx->trace.names.assign(1, nullptr);
+  ctx->trace.at_names.clear();
+  ctx->trace.host.clear();
+  ctx->trace.t0 = std::chrono::steady_clock::now();
   HD_CUDA(cudaEventRecord(trace_event(ctx, 0), ctx->stream));
   nvtxRangePushA(call);
 }
@@ -83,6 +86,27 @@ void trace_mark(hd_ctx *ctx, const char *phase) {
   HD_CUDA(cudaEventRecord(trace_event(ctx, k), ctx->stream));
   ctx->trace.names.push_back(phase);
   nvtxMarkA(phase);
+}
+
+void trace_at(hd_ctx *ctx, const std::string &what, cudaStream_t s) {
+  if (!ctx->trace.on || !ctx->trace.call) return;
+  Trace &t = ctx->trace;
+  const size_t k = t.at_names.size();
+  while (t.at_pool.size() <= k) {
+    cudaEvent_t e;
+    HD_CUDA(cudaEventCreate(&e));
+    t.at_pool.push_back(e);
+  }
+  HD_CUDA(cudaEventRecord(t.at_pool[k], s));
+  t.at_names.push_back(what);
+}
+
+void trace_host(hd_ctx *ctx, const std::string &what) {
+  if (!ctx->trace.on || !ctx->trace.call) return;
+  ctx->trace.host.emplace_back(
+      what, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
+                                                      ctx->trace.t0)
+                .count());
 }
 
 void trace_end(hd_ctx *ctx) {
@@ -104,6 +128,19 @@ void trace_end(hd_ctx *ctx) {
     char buf[64];
     std::snprintf(buf, sizeof buf, " stream time %.3f ms", total);
     text += buf;
+  }
+  for (size_t k = 0; k < t.at_names.size(); ++k) {
+    float ms = 0;
+    HD_CUDA(cudaEventSynchronize(t.at_pool[k]));
+    HD_CUDA(cudaEventElapsedTime(&ms, t.pool[0], t.at_pool[k]));
+    char buf[48];
+    std::snprintf(buf, sizeof buf, " at %.3f ms", ms);
+    text += (k ? ", " : "; ") + t.at_names[k] + buf;
+  }
+  for (size_t k = 0; k < t.host.size(); ++k) {
+    char buf[48];
+    std::snprintf(buf, sizeof buf, " at %.3f ms", t.host[k].second);
+    text += (k ? ", host: " : "; host: ") + t.host[k].first + buf;
   }
   t.last = text;
   t.call = nullptr;
@@ -469,6 +506,16 @@ void prefault_host(void *p, uint64_t n) {
     const long v = sysconf(_SC_PAGESIZE);
     return (uint64_t)(v > 0 ? v : 4096);
   }();
+  {
+    // a recycled buffer has its pages already: then starting the threads
+    // would cost more than the touches
+    const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)(page - 1);
+    const size_t len = reinterpret_cast<uintptr_t>(p) + n - a0;
+    std::vector<unsigned char> v(hd::ceil_div(len, page));
+    if (::mincore(reinterpret_cast<void *>(a0), len, v.data()) == 0 &&
+        std::all_of(v.begin(), v.end(), [](unsigned char c) { return (c & 1) != 0; }))
+      return;
+  }
   const unsigned nt = (unsigned)std::min<uint64_t>(16, n / kPart);
   const uint64_t per = hd::round_up(hd::ceil_div(n, nt), page);
   std::vector<std::thread> th;
@@ -746,7 +793,13 @@ int hd_ctx_create(int device, hd_ctx **out) {
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->up, cudaStreamNonBlocking));
-    HD_CUDA(cudaStreamCreateWithFlags(&ctx->side2, cudaStreamNonBlocking));
+    // side2 carries the second launch of a streamed call's last part, at the
+    // least priority: the CTAs of the first launch (on ctx->stream, right
+    // after the pack) take the SMs first, and those of the second fill its
+    // tail
+    int least = 0, greatest = 0;
+    HD_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    HD_CUDA(cudaStreamCreateWithPriority(&ctx->side2, cudaStreamNonBlocking, least));
     // files are copied from their page-cache mapping where the device reads
     // pageable memory through the host's page tables (Grace: NVLink-C2C);
     // HAMMINGDIST_READ_MODE=pread keeps the pread + pinned staging order
@@ -1002,7 +1055,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     };
     std::vector<std::unique_ptr<Band>> bands;
     hd::Records all;
-    DevBuf uniq, iota, d_lt;
+    DevBuf uniq, iota, d_lt, keep_planes;
     std::vector<uint64_t> seq;
     std::unique_ptr<hd_alignment> owner;
     // each part's new records only, while that resolves them (else the full
@@ -1034,7 +1087,6 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     };
     uint64_t L = 0, words = 0, R_max = 0, K = 0, B_prev = 0, tiles = 0;
     uint32_t T = 0, t_done = 0;
-    cudaEvent_t last_packed = nullptr;  // every row packed
     bool use_mma = false;  // tensor-core engine: 128-row tiles
     // SMs left to the next part's ingest while a band runs
     // (HAMMINGDIST_STREAM_FREE_SMS, default 16)
@@ -1055,6 +1107,9 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       b->row_lo = (uint64_t)t_lo * T;
       b->row_hi = std::min<uint64_t>((uint64_t)t_hi * T, rows);
       if (after) HD_CUDA(cudaStreamWaitEvent(s, after, 0));
+      const std::string rows_text =
+          "rows " + std::to_string(b->row_lo) + "-" + std::to_string(b->row_hi);
+      hd::trace_at(ctx, rows_text + " start", s);
       ctx->last_pair_tiles = 0;
       // the tensor-core engine (its operand rows were expanded after the
       // pack, on ctx->stream), else the bit-plane engine
@@ -1072,6 +1127,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         hd::launch_pairwise_plan(ctx, b->plan, s);
       }
       tiles += ctx->last_pair_tiles;
+      hd::trace_at(ctx, rows_text + " done", s);
       b->done = sync.make();
       HD_CUDA(cudaEventRecord(b->done, s));
       bands.push_back(std::move(b));
@@ -1121,6 +1177,10 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         owner->planes = 4;
         owner->plane_buf[0] = DevBuf(R_max * words * 16, ctx->stream);
         g0 = owner->plane_buf[0].as<uint4>();
+        // a second copy of the rows, written by the same packs, stays with
+        // the file's records for the reference distances of the same file
+        // (fasta_reference_distances after from_fasta)
+        keep_planes = DevBuf(R_max * words * 16, ctx->stream);
         d_lt = DevBuf((R_max < 2 ? 1 : tri(R_max)) * dtype_bytes, ctx->stream);
         if (!remove_duplicates) {
           std::vector<uint64_t> h(R_max);
@@ -1159,7 +1219,8 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
           if (!hd::tile_config_valid(cfg.tile, cfg.stages)) cfg.stages = 3;
         }
       }
-      hd::pack_rows_and(ctx, all, rows + K, Kc - K, L, words, g0 + K * words);
+      hd::pack_rows_and(ctx, all, rows + K, Kc - K, L, words, g0 + K * words,
+                        keep_planes.as<uint4>() + K * words);
       // the new rows' tensor-core operand, before the launches of any stream read it
       if (use_mma && Kc >= 2 && !hd::ensure_operand(ctx, owner.get(), Kc, ctx->stream, R_max)) {
         use_mma = false;
@@ -1176,25 +1237,26 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
           launch(t_done, t_end, K, ctx->side, std::max(1, ctx->sm_count - free_sms), packed);
           t_done = t_end;
         }
+        hd::trace_host(ctx, "part " + std::to_string(c + 1) + " queued");
         B_prev = B;
         continue;
       }
-      last_packed = sync.make();
-      HD_CUDA(cudaEventRecord(last_packed, ctx->stream));
       const uint32_t t_end = K >= 2 ? (uint32_t)hd::ceil_div(K, T) : t_done;
       if (t_end > t_done) {
         const uint32_t t_split =
             std::max(t_done + 1, (uint32_t)std::ceil(0.9 * (double)t_end));
-        cudaEvent_t packed = last_packed;
+        cudaEvent_t packed = sync.make();
+        HD_CUDA(cudaEventRecord(packed, ctx->stream));
         if (t_split < t_end) {
-          launch(t_done, t_split, K, ctx->side2, 0, packed);
-          launch(t_split, t_end, K, ctx->stream, 0, nullptr);
+          launch(t_done, t_split, K, ctx->stream, 0, nullptr);
+          launch(t_split, t_end, K, ctx->side2, 0, packed);
         } else {
           launch(t_done, t_end, K, ctx->side2, 0, packed);
         }
       }
       break;
     }
+    hd::trace_host(ctx, "launches queued");
     owner->n_rows = K;
     owner->n_input = all.n;
     // each record's row: on the device (the incremental dedupe's rowid,
@@ -1213,10 +1275,9 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       }
     }
     ctx->last_pair_tiles = tiles;
-    // a copy of the rows stays with the file's records, for the reference
-    // distances of the same file (fasta_reference_distances after from_fasta):
-    // copied on the upload stream while the distances run
-    if (K && last_packed) {
+    // the second copy of the rows stays with the file's records, with each
+    // record's row
+    if (K && keep_planes.p) {
       auto keep = std::make_shared<hd_alignment>();
       keep->ctx = ctx;
       keep->device = ctx->device;
@@ -1224,29 +1285,29 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       keep->words = words;
       keep->n_rows = K;
       keep->n_input = all.n;
-      keep->plane_buf[0] = DevBuf(K * words * 16, ctx->up);
-      HD_CUDA(cudaStreamWaitEvent(ctx->up, last_packed, 0));
-      HD_CUDA(cudaMemcpyAsync(keep->plane_buf[0].p, g0, K * words * 16, cudaMemcpyDeviceToDevice,
-                              ctx->up));
+      keep->plane_buf[0] = std::move(keep_planes);
       if (remove_duplicates) {
-        all.row_of = DevBuf(all.n * 8, ctx->up);
-        if (inc_rows)  // last_packed follows the dedupe
+        all.row_of = DevBuf(all.n * 8, ctx->stream);
+        if (inc_rows)
           HD_CUDA(cudaMemcpyAsync(all.row_of.p, inc.rowid.p, all.n * 8, cudaMemcpyDeviceToDevice,
-                                  ctx->up));
+                                  ctx->stream));
         else
-          hd::upload_table(ctx, all.row_of.p, owner->seqidx.data(), all.n * 8, ctx->up);
+          hd::upload_table(ctx, all.row_of.p, owner->seqidx.data(), all.n * 8, ctx->stream);
       }
       all.rows = std::move(keep);
     }
     // each finished range of rows is copied to the host on the upload stream
     // once its launch is done, while the later ones compute
+    hd::trace_host(ctx, "rows kept");
     const uint64_t entries = K < 2 ? 0 : tri(K);
     void *host = out_fn(user, 0, K, entries);
     if (!host && entries) fail(HD_ERR_ARG, "output callback returned no buffer");
     void *mirror = entries ? out_fn(user, HD_OUTPUT_MIRROR, K, entries) : nullptr;
+    hd::trace_host(ctx, "outputs");
     if (entries) {
       prefault_host(host, entries * dtype_bytes);  // while the kernels run
       if (mirror) prefault_host(mirror, entries * dtype_bytes);
+      hd::trace_host(ctx, "outputs touched");
       for (const auto &b : bands) {
         const uint64_t e0 = tri(b->row_lo), e1 = tri(b->row_hi);
         if (e1 <= e0) continue;
@@ -1256,7 +1317,11 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
             HD_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(dst) + e0 * dtype_bytes,
                                     d_lt.as<uint8_t>() + e0 * dtype_bytes, (e1 - e0) * dtype_bytes,
                                     cudaMemcpyDeviceToHost, ctx->up));
+        hd::trace_at(ctx, "rows " + std::to_string(b->row_lo) + "-" + std::to_string(b->row_hi) +
+                              " copied",
+                     ctx->up);
       }
+      hd::trace_host(ctx, "copies queued");
     }
     if (ctx->trace.on) {
       // the context's stream waits for the distance launches, then for the

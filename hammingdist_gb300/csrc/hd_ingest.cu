@@ -927,7 +927,7 @@ __device__ __forceinline__ uint32_t and_codes4(uint32_t x) {
 }
 __global__ void __launch_bounds__(256)
     k_pack_and(const uint8_t *base, uint64_t bytes, const uint64_t *rs, const uint64_t *rows,
-               uint64_t n_rows, uint64_t L, uint64_t words, uint4 *g0) {
+               uint64_t n_rows, uint64_t L, uint64_t words, uint4 *g0, uint4 *g1) {
   const int lane = threadIdx.x & 31;
   const uint64_t lo = reinterpret_cast<uint64_t>(base), hi = lo + bytes;
   const uint64_t chunks = (words + 31) / 32;
@@ -986,16 +986,20 @@ __global__ void __launch_bounds__(256)
         pl[p] |= ((((c >> p) & 0x01010101u) * 0x01020408u) >> 24) << (4 * k);
     }
     const uint64_t wi = q * 32 + lane;
-    if (wi < words) g0[u * words + wi] = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+    if (wi < words) {
+      const uint4 v = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+      g0[u * words + wi] = v;
+      if (g1) g1[u * words + wi] = v;
+    }
   }
 }
 
 void pack_rows_and(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, uint64_t n_rows,
-                   uint64_t length, uint64_t words, uint4 *g0) {
+                   uint64_t length, uint64_t words, uint4 *g0, uint4 *g1) {
   if (!n_rows) return;
   const uint64_t jobs = n_rows * ((words + 31) / 32);
   k_pack_and<<<grid_for(jobs * 32, 256), 256, 0, ctx->stream>>>(
-      rec.base, rec.bytes, rec.rec_start.as<uint64_t>(), d_rows, n_rows, length, words, g0);
+      rec.base, rec.bytes, rec.rec_start.as<uint64_t>(), d_rows, n_rows, length, words, g0, g1);
   HD_LAUNCHED(ctx);
 }
 
@@ -1086,7 +1090,7 @@ void pack_rows(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, hd_align
   const uint64_t *rs = rec.rec_start.as<uint64_t>();
   if (aln->planes == 4)
     k_pack_and<<<grid_for(aln->n_rows * ((aln->words + 31) / 32) * 32, 256), 256, 0, ctx->stream>>>(
-        rec.base, rec.bytes, rs, d_rows, aln->n_rows, aln->length, aln->words, g0);
+        rec.base, rec.bytes, rs, d_rows, aln->n_rows, aln->length, aln->words, g0, nullptr);
   else if (aln->planes == 5)
     k_pack<5><<<grid, kPackThreads, 0, ctx->stream>>>(rec.base, rs, d_rows, aln->n_rows, aln->length,
                                              aln->words, t, g0, g1);

@@ -10,6 +10,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <chrono>
 #include <memory>
 #include <string>
 #include <utility>
@@ -93,6 +94,12 @@ struct Trace {
   const char *call = nullptr;
   std::vector<cudaEvent_t> pool;
   std::vector<const char *> names;  // phase ending at event k (k >= 1)
+  // points on other streams (trace_at): reported as times since the call began
+  std::vector<cudaEvent_t> at_pool;
+  std::vector<std::string> at_names;
+  // host-side points (trace_host): milliseconds since the call began
+  std::chrono::steady_clock::time_point t0;
+  std::vector<std::pair<std::string, double>> host;
   std::string last;                 // text of the last traced call
 };
 // Kernel configuration of one matrix (autotuned per n, L and dtype bucket).
@@ -423,10 +430,10 @@ uint64_t consensus_matches(hd_ctx *ctx, const Records &rec, const uint64_t *d_ro
                            uint64_t n_rows);
 // Packs rows (record ids d_rows, or identity if null) into bit planes.
 void pack_rows(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, hd_alignment *aln);
-// AND-rule planes of n_rows records (d_rows: record indices) into g0
-// (n_rows x words uint4, already allocated)
+// AND-rule planes of n_rows records (d_rows: record indices) into g0, and
+// into g1 too unless it is null (n_rows x words uint4 each, already allocated)
 void pack_rows_and(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, uint64_t n_rows,
-                   uint64_t length, uint64_t words, uint4 *g0);
+                   uint64_t length, uint64_t words, uint4 *g0, uint4 *g1 = nullptr);
 // b without its first record, with len0 / max_len / all_equal recomputed
 Records drop_first_record(hd_ctx *ctx, Records &&b);
 // records of a then b (b's starts shifted by b_off), one base; b parsed from
@@ -568,6 +575,11 @@ void measure_int_peaks(hd_ctx *ctx, double *lop3, double *popc, double *mix);
 // phase tracing of one API call (no-ops unless ctx->trace.on)
 void trace_begin(hd_ctx *ctx, const char *call);
 void trace_mark(hd_ctx *ctx, const char *phase);
+// a point on stream s (e.g. a launch's end on a side stream), listed after the
+// phases with its time since the call began
+void trace_at(hd_ctx *ctx, const std::string &what, cudaStream_t s);
+// a point of the host thread, listed with its time since the call began
+void trace_host(hd_ctx *ctx, const std::string &what);
 void trace_end(hd_ctx *ctx);
 
 }  // namespace hd
