@@ -458,6 +458,8 @@ void query_distances_async(hd_ctx *ctx, const hd_alignment *aln, const uint8_t *
 void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint32_t max_dist,
                     void *d_out, uint64_t out_base, uint32_t tile_lo, uint32_t tile_hi);
 constexpr uint32_t kTile = 128;
+// columns of a tensor-core work item (the N of its MMAs)
+constexpr uint32_t kMmaCols = 240;
 
 // Kernel configuration of one job: tile edge (64 or 128 rows; 4 or 8 rows
 // per thread) and TMA staging depth.

@@ -36,21 +36,22 @@
 // serving window) gets one of its own rows.
 //
 // One launch serves a job table of matrices. Persistent CTAs (320 threads,
-// one per SM) walk a list of items: 224 columns J x one or two 128-row tiles
+// one per SM) walk a list of items: 240 columns J x one or two 128-row tiles
 // I of one job, in bands of 16 tile rows, column-major within a band, so
 // resident CTAs share operands in L2; the list ends with single-row-tile items
 // so that every CTA gets the same work to within a row tile.
 //  * warp 0 (one thread) issues TMA loads (128-byte swizzle) per stage of
-//    one 128-byte K block (256 sites) of the item's 128 or 256 rows and 224
-//    columns, 3 stages of 60 KB with full/empty mbarriers; warp 0 also
+//    one 128-byte K block (256 sites) of the item's 128 or 256 rows and 240
+//    columns, 3 stages of 62 KB with full/empty mbarriers; warp 0 also
 //    allocates and frees the TMEM;
 //  * warp 1 (one thread) issues tcgen05.mma.cta_group::1.kind::mxf4
-//    .block_scale (M=128, N=224, K=64), four per row tile per stage, into
+//    .block_scale (M=128, N=240, K=64), four per row tile per stage, into
 //    TMEM (row tile h of the item at columns 256 h); the unit scale factors
-//    sit in TMEM columns 224-255, written once per CTA. Each stage's MMAs are
+//    sit in the columns the accumulators leave, 240-255 (rows) and 496-511
+//    (columns), written once per CTA. Each stage's MMAs are
 //    committed to its empty barrier, an item's last ones to `done`;
-//  * warps 2-9, two per TMEM lane quarter, each read 32 rows x 128 or 96
-//    columns of each accumulator (tcgen05.ld, 64 or 32 columns at a time),
+//  * warps 2-9, two per TMEM lane quarter, each read 32 rows x 128 or 112
+//    columns of each accumulator (tcgen05.ld, 64, 32 or 16 columns at a time),
 //    form min(L - matches, max_dist) (safe_int_cast,
 //    include/hamming/hamming_impl.hh:37-45), turn each 32 x 32 chunk around
 //    in a padded shared buffer and store it row by row, 32 consecutive
@@ -75,17 +76,23 @@ constexpr int kEpiWarps = 8;      // two per TMEM lane quarter
 constexpr int kMmaThreads = 64 + 32 * kEpiWarps;  // warp 0: TMA, warp 1: MMA, warps 2-9: epilogue
 constexpr int kEpiThreads = 32 * kEpiWarps;
 constexpr int kMmaStages = 3;
-constexpr int kTM = 128, kTN = 224;                   // MMA tile: rows x columns
+constexpr int kTM = 128, kTN = (int)kMmaCols;          // MMA tile: rows x columns (240)
 constexpr uint32_t kEpiSplit = 128;                   // epilogue halves: [0, 128), [128, kTN)
-constexpr uint32_t kSfCol = 224;                      // TMEM columns 224-255: scale factors
+// unit scale factors in the TMEM columns the two accumulators (columns
+// [0, kTN) and [256, 256 + kTN)) leave: the rows' at kTN, the columns' at
+// 256 + kTN, 16 columns each
+constexpr uint32_t kSfColA = kTN, kSfColB = 256 + kTN;
 constexpr uint32_t kSfWord = 0x7F7F7F7Fu;             // four UE8M0 scale factors of 2^0
 constexpr uint32_t kHalfBytes = kTM * 128;            // one 128-byte K block of 128 rows
 constexpr uint32_t kABytes = 2 * kHalfBytes;          // up to two row tiles
 constexpr uint32_t kBBytes = kTN * 128;
-constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 60 KB
+constexpr uint32_t kStageBytes = kABytes + kBBytes;   // 62 KB, a multiple of 1 KB
 constexpr uint32_t kEpiPitch = 33;                    // words per row of an epilogue chunk
 constexpr uint32_t kEpiBytes = kEpiWarps * 32 * kEpiPitch * 4;  // 32 x 32 words per epilogue warp
 constexpr int kMmaSmem = kMmaStages * kStageBytes + kEpiBytes + 1024;
+static_assert(kStageBytes % 1024 == 0, "stages must stay 1 KB aligned for the 128-byte swizzle");
+static_assert(kMmaSmem <= 232448, "dynamic shared memory above the per-block limit");
+static_assert(kTN % 16 == 0 && kTN <= 240, "N of an M=128 MMA; 16 TMEM columns left for scales");
 constexpr uint32_t kTmemCols = 512;                   // row tile h at columns 256 h
 constexpr uint64_t kMmaWaitNs = 1000000000ull;        // 1 s
 constexpr uint32_t kMmaBand = 16;  // tile rows per L2 band (HAMMINGDIST_MMA_BAND overrides)
@@ -234,12 +241,13 @@ __device__ __forceinline__ void mma_f4(uint32_t d_tmem, uint64_t a_desc, uint64_
       "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate), "r"(sfa), "r"(sfb)
       : "memory");
 }
-// The unit scale factors: this warp writes kSfWord to the 32 TMEM columns
+// The unit scale factors: this warp writes kSfWord to the NC TMEM columns
 // from col0 in its lane quarter (lane base `t_lane`) and waits for the
 // stores; the caller fences before the MMAs read them.
+template <uint32_t NC>
 __device__ __forceinline__ void write_unit_scales(uint32_t t_lane, uint32_t col0) {
 #pragma unroll
-  for (uint32_t c = col0; c < col0 + 32; c += 4)
+  for (uint32_t c = col0; c < col0 + NC; c += 4)
     asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(t_lane + c),
                  "r"(kSfWord), "r"(kSfWord), "r"(kSfWord), "r"(kSfWord)
                  : "memory");
@@ -292,40 +300,54 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
       : "r"(taddr)
       : "memory");
 }
+// 32 lanes x 16 consecutive 32-bit columns
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {"
+      "%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15 "
+      "}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+}
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// min(sites - matches, max_dist) of accumulator columns OFF .. OFF + 31
+// min(sites - matches, max_dist) of accumulator columns OFF .. OFF + W - 1
 // (FP32 integers) into the warp's buffer, row `lane` at words 33 lane
-template <int OFF, int N>
+template <int OFF, int N, int W = 32>
 __device__ __forceinline__ void turn_chunk(uint32_t *buf, const uint32_t (&d)[N], uint32_t sites,
                                            uint32_t max_dist, uint32_t lane) {
+  static_assert(OFF + W <= N, "columns outside the loaded registers");
 #pragma unroll
-  for (uint32_t j = 0; j < 32; ++j) {
+  for (uint32_t j = 0; j < W; ++j) {
     const uint32_t mism = sites - (uint32_t)__uint_as_float(d[OFF + j]);
     buf[lane * kEpiPitch + j] = mism < max_dist ? mism : max_dist;
   }
 }
 
-// The buffered chunk of rows i0 .. i0 + rows - 1, columns j0 .. j0 + 31, row
-// by row: lane l stores column j0 + l of row i0 + r, lower-triangle entry
-// tri(i0 + r) + j0 + l = e0 + r i0 + r (r - 1) / 2, where it is below the
-// diagonal (j0 + l < i0 + r). The row loop is unrolled so that several rows'
-// loads and stores are in flight.
-template <typename T>
+// The buffered chunk of rows i0 .. i0 + rows - 1, columns j0 .. j0 + W - 1,
+// row by row: lane l < W stores column j0 + l of row i0 + r, lower-triangle
+// entry tri(i0 + r) + j0 + l = e0 + r i0 + r (r - 1) / 2, where it is below
+// the diagonal (j0 + l < i0 + r). The row loop is unrolled so that several
+// rows' loads and stores are in flight.
+template <typename T, uint32_t W = 32>
 __device__ __forceinline__ void store_chunk(T *out, unsigned long long e0, uint32_t i0,
                                             uint32_t rows, uint32_t j0, const uint32_t *buf,
                                             uint32_t lane) {
 #pragma unroll 8
   for (uint32_t r = 0; r < 32; ++r)
-    if (r < rows && j0 + lane < i0 + r)
+    if (r < rows && lane < W && j0 + lane < i0 + r)
       out[e0 + (unsigned long long)r * i0 + r * (r - 1) / 2] = (T)buf[r * kEpiPitch + lane];
 }
 
 // One epilogue warp's share of an item: TMEM lanes of its quarter (rows
 // 32 sub + lane of each row tile) x its columns [c_lo, c_hi), read 64
-// columns at a time (32 for a last piece of 32).
+// columns at a time, then a last piece of 32 and one of 16 where the share
+// leaves them (112 = 64 + 32 + 16).
 template <typename T>
 __device__ __forceinline__ void epilogue_share(const MmaItem &tl, const MmaJob &job,
                                                uint32_t t_lane, uint32_t c_lo, uint32_t c_hi,
@@ -338,11 +360,21 @@ __device__ __forceinline__ void epilogue_share(const MmaItem &tl, const MmaJob &
     const uint32_t rows = n - i0 < 32u ? n - i0 : 32u;
     const unsigned long long t0 = (unsigned long long)i0 * (i0 - 1) / 2 - job.out_base + lane;
 #pragma unroll 1
-    for (uint32_t c = c_lo; c < c_hi; c += 64) {
+    for (uint32_t c = c_lo; c < c_hi;) {
       const uint32_t j0 = tl.J * kTN + c;  // first column of this group
       if (j0 + 1 >= i0 + rows) break;      // no row reaches column j0 (warp-uniform)
       __syncwarp();
-      if (c + 64 > c_hi) {  // a last piece of 32 columns
+      if (c + 32 > c_hi) {  // a last piece of 16 columns
+        uint32_t d[16];
+        tmem_ld16(t_lane + 256u * h + c, d);
+        tmem_ld_wait();
+        turn_chunk<0, 16, 16>(buf, d, sites, max_dist, lane);
+        __syncwarp();
+        store_chunk<T, 16>(out, t0 + j0, i0, rows, j0, buf, lane);
+        __syncwarp();
+        break;
+      }
+      if (c + 64 > c_hi) {  // a piece of 32 columns
         uint32_t d[32];
         tmem_ld32(t_lane + 256u * h + c, d);
         tmem_ld_wait();
@@ -350,7 +382,8 @@ __device__ __forceinline__ void epilogue_share(const MmaItem &tl, const MmaJob &
         __syncwarp();
         store_chunk<T>(out, t0 + j0, i0, rows, j0, buf, lane);
         __syncwarp();
-        break;
+        c += 32;
+        continue;
       }
       uint32_t d[64];
       tmem_ld64(t_lane + 256u * h + c, d);
@@ -364,6 +397,7 @@ __device__ __forceinline__ void epilogue_share(const MmaItem &tl, const MmaJob &
       __syncwarp();
       store_chunk<T>(out, t0 + j0 + 32, i0, rows, j0 + 32, buf, lane);
       __syncwarp();
+      c += 64;
     }
   }
 }
@@ -405,7 +439,10 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   tc_after_sync();
   const uint32_t tmem = s_tmem;
   // the unit scale factors, once per CTA: warps 2-5 cover the lane quarters
-  if (warp >= 2 && warp < 6) write_unit_scales(tmem + (((warp & 3u) * 32) << 16), kSfCol);
+  if (warp >= 2 && warp < 6) {
+    write_unit_scales<16>(tmem + (((warp & 3u) * 32) << 16), kSfColA);
+    write_unit_scales<16>(tmem + (((warp & 3u) * 32) << 16), kSfColB);
+  }
   tc_before_sync();
   __syncthreads();
   tc_after_sync();
@@ -514,7 +551,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
 #pragma unroll
             for (uint32_t k = 0; k < 4; ++k)  // 32 bytes of K per MMA: +2 in 16-byte units
               mma_f4(tmem + 256u * h, ad + 2 * k, bd + 2 * k, kIdesc, (kb | k) ? 1u : 0u,
-                     tmem + kSfCol, tmem + kSfCol + 16);
+                     tmem + kSfColA, tmem + kSfColB);
           }
           mma_commit(&empty[s]);
           ++g;
@@ -618,7 +655,7 @@ __global__ void __launch_bounds__(128, 1) k_peak_mma(uint32_t rounds, int *statu
   __syncthreads();
   tc_after_sync();
   const uint32_t tmem = s_tmem;
-  write_unit_scales(tmem + (((threadIdx.x >> 5) * 32) << 16), kPeakSf);
+  write_unit_scales<32>(tmem + (((threadIdx.x >> 5) * 32) << 16), kPeakSf);
   tc_before_sync();
   __syncthreads();
   tc_after_sync();

@@ -43,7 +43,8 @@ int l_bucket(uint64_t L) {
 // single-row-tile items of the tensor-core engine for one matrix of n rows
 uint64_t mma_items_of(uint64_t n) {
   uint64_t items = 0;
-  for (uint64_t I = 0; I < ceil_div(n, 128); ++I) items += ((I + 1) * 128 - 2) / 224 + 1;
+  for (uint64_t I = 0; I < ceil_div(n, (uint64_t)kTile); ++I)
+    items += ((I + 1) * kTile - 2) / kMmaCols + 1;
   return items;
 }
 uint32_t key_of(int nb, int lb, int dtype) { return (uint32_t)(nb * 100 + lb * 10 + dtype); }

@@ -2,7 +2,7 @@
 matches = <planes> - (P - 1) <dash>)
 against the bit-plane engine (HAMMINGDIST_KERNEL=lop3) and the oracle, bit
 for bit: lengths at and around the 32/256-site blocks, row counts around the
-128 x 224 tiles, every dtype and saturation, '-' against '-', N and other
+128 x 240 tiles, every dtype and saturation, '-' against '-', N and other
 bytes, the row ranges of the text writer and views."""
 import os
 
@@ -43,7 +43,8 @@ def _both(ctx, aln, **kw):
 
 @pytest.mark.parametrize("n,L", [(2, 1), (3, 33), (5, 127), (17, 128), (129, 129), (255, 257),
                                  (256, 1000), (257, 513), (300, 5000), (130, 29903), (224, 256),
-                                 (225, 255), (449, 511), (448, 769)])
+                                 (225, 255), (449, 511), (448, 769), (240, 300), (241, 64),
+                                 (481, 1000), (480, 257), (719, 2049)])
 def test_mma_equals_lop3_and_oracle(ctx, n, L):
     seqs = synth.random_strings(n, L, b"ACGT-N", seed=n * 7 + L)
     aln = ctx.alignment_from_sequences(seqs)

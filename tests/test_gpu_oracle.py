@@ -175,11 +175,11 @@ def test_launches_and_device_output(ctx, monkeypatch):
     ctx.pairwise_lt(aln, dtype=np.uint8, max_distance=255, out=out.data_ptr(), out_on_device=True)
     assert ctx.kernel_launches > before
     np.testing.assert_array_equal(out.cpu().numpy(), o.lt_dense(seqs))
-    # the tensor-core engine: 128-row x 224-column tiles, a short list split
+    # the tensor-core engine: 128-row x 240-column tiles, a short list split
     # into single row tiles, each with the column tiles its rows reach
     ms, tiles = ctx.last_pairwise_timing()
     nb = -(-n // 128)
-    assert ms > 0 and tiles == sum((128 * (i + 1) - 2) // 224 + 1 for i in range(nb))
+    assert ms > 0 and tiles == sum((128 * (i + 1) - 2) // 240 + 1 for i in range(nb))
     # the bit-plane engine: square tiles of the autotuned edge
     import os
 
