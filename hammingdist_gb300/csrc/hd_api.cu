@@ -793,13 +793,6 @@ int hd_ctx_create(int device, hd_ctx **out) {
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
     HD_CUDA(cudaStreamCreateWithFlags(&ctx->up, cudaStreamNonBlocking));
-    // side2 carries the second launch of a streamed call's last part, at the
-    // least priority: the CTAs of the first launch (on ctx->stream, right
-    // after the pack) take the SMs first, and those of the second fill its
-    // tail
-    int least = 0, greatest = 0;
-    HD_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    HD_CUDA(cudaStreamCreateWithPriority(&ctx->side2, cudaStreamNonBlocking, least));
     // files are copied from their page-cache mapping where the device reads
     // pageable memory through the host's page tables (Grace: NVLink-C2C);
     // HAMMINGDIST_READ_MODE=pread keeps the pread + pinned staging order
@@ -866,7 +859,6 @@ void hd_ctx_destroy(hd_ctx *ctx) {
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->up) cudaStreamDestroy(ctx->up);
-  if (ctx->side2) cudaStreamDestroy(ctx->side2);
   delete ctx;
 }
 
@@ -1019,9 +1011,9 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     // order, so earlier unique rows keep their positions) and the new unique
     // rows are packed; the tile rows that are complete then run on the side
     // stream, with 16 SMs left for the next part's ingest. The last part's
-    // tile rows run as two launches on two streams (the second fills the
-    // first's tail), split at 90% of the rows, so that the copy of every
-    // finished range to the host overlaps the rest of the distances.
+    // tile rows run as two launches, split at 90% of the tile rows, so that
+    // the copy of every finished range to the host overlaps the rest of the
+    // distances.
     // part ends as fractions of the file (HAMMINGDIST_STREAM_SPLITS="f1,f2,...",
     // increasing, at most 3). At n=20,000 x L=29,903 the file-to-host step
     // (with the reference distances) took 8.39 ms with splits at 30% and 60%,
@@ -1075,12 +1067,12 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         return e;
       }
       ~Sync() {
-        for (cudaStream_t s : {c->stream, c->side, c->side2, c->up}) cudaStreamSynchronize(s);
+        for (cudaStream_t s : {c->stream, c->side, c->up}) cudaStreamSynchronize(s);
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
       }
     } sync{ctx, {}};
     auto fallback = [&] {  // the whole matrix after the whole file
-      for (cudaStream_t s : {ctx->side, ctx->side2}) HD_CUDA(cudaStreamSynchronize(s));
+      HD_CUDA(cudaStreamSynchronize(ctx->side));
       read_all();
       whole();
       hd::trace_end(ctx);
@@ -1245,14 +1237,12 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       if (t_end > t_done) {
         const uint32_t t_split =
             std::max(t_done + 1, (uint32_t)std::ceil(0.9 * (double)t_end));
-        cudaEvent_t packed = sync.make();
-        HD_CUDA(cudaEventRecord(packed, ctx->stream));
-        if (t_split < t_end) {
-          launch(t_done, t_split, K, ctx->stream, 0, nullptr);
-          launch(t_split, t_end, K, ctx->side2, 0, packed);
-        } else {
-          launch(t_done, t_end, K, ctx->side2, 0, packed);
-        }
+        // one after the other on the context's stream: launched on two
+        // streams at once, the block scheduler sometimes gave the SMs to the
+        // second launch's CTAs first, and the first launch (whose CTAs walk
+        // fixed item lists) then ended up to 0.8 ms later
+        launch(t_done, t_split < t_end ? t_split : t_end, K, ctx->stream, 0, nullptr);
+        if (t_split < t_end) launch(t_split, t_end, K, ctx->stream, 0, nullptr);
       }
       break;
     }
@@ -1326,7 +1316,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     if (ctx->trace.on) {
       // the context's stream waits for the distance launches, then for the
       // copies, so that the trace shows the two apart
-      for (cudaStream_t s : {ctx->side2, ctx->side}) {
+      for (cudaStream_t s : {ctx->side}) {
         cudaEvent_t e = sync.make();
         HD_CUDA(cudaEventRecord(e, s));
         HD_CUDA(cudaStreamWaitEvent(ctx->stream, e, 0));
@@ -1337,7 +1327,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       HD_CUDA(cudaStreamWaitEvent(ctx->stream, e, 0));
       hd::trace_mark(ctx, "rest of the copy to host");
     }
-    for (cudaStream_t s : {ctx->side2, ctx->side, ctx->up, ctx->stream})
+    for (cudaStream_t s : {ctx->side, ctx->up, ctx->stream})
       HD_CUDA(cudaStreamSynchronize(s));
     check_status(ctx);
     if (inc_rows) inc.rows(ctx, owner->seqidx);

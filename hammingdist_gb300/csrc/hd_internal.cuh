@@ -123,7 +123,6 @@ struct hd_ctx {
   int sm_count = 0;
   cudaStream_t stream = nullptr;  // compute
   cudaStream_t side = nullptr;    // copies that overlap compute
-  cudaStream_t side2 = nullptr;   // a second launch stream (streamed from_fasta)
   std::string err;
   int *d_status = nullptr;        // kernel status word
   uint64_t launches = 0;

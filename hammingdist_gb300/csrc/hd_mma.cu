@@ -770,7 +770,7 @@ bool ensure_operand(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStr
       HD_CUDA(cudaMemcpyAsync(grown.p, o->op.p, o->op_rows * rb, cudaMemcpyDeviceToDevice, stream));
       // launches on the context's other streams may still read the old
       // operand: they finish before it is freed
-      for (cudaStream_t st : {ctx->side, ctx->side2, ctx->stream}) HD_CUDA(cudaStreamSynchronize(st));
+      for (cudaStream_t st : {ctx->side, ctx->stream}) HD_CUDA(cudaStreamSynchronize(st));
     }
     o->op = std::move(grown);
     o->op_cap = cap;
