@@ -374,20 +374,22 @@ __device__ inline uint32_t load4_in(uint64_t x, uint64_t lo, uint64_t hi) {
   return w;
 }
 
-// Hash of each record's bytes: a sum over its 4-byte groups (relative to the
-// record start; a short last group is zero-filled) of the 64-bit product of
-// the group XORed with two position-keyed 32-bit constants, then one 64-bit
-// mix of the sum and the length (k_hash_fin). Different records rarely share
-// a hash, and equal hashes are verified byte by byte, so a collision costs a
-// verify round, never a wrong answer. The sum does not depend on the order of
-// its terms, so a record is hashed in segments of kHashSeg bytes, one warp
-// each, that add their partial sums to acc[r] (zeroed first): many warps per
-// record keep enough loads in flight however few records there are. Block
-// (x, y) takes records 8x .. 8x + 7 (one per warp) from byte y kHashSeg on.
-// The warp reads its segment with aligned 16-byte loads (two 512-byte blocks
-// per step); a lane's groups start at byte P mod 4 of its words (P the
-// record's start) and are realigned with a funnel shift and the next lane's
-// first word.
+// Hash of each record's bytes: a sum over its 8-byte groups (at record
+// positions 8q; a short last group is zero-filled) of the 64-bit product of
+// the group's two 4-byte halves, each XORed with a position-keyed 32-bit
+// constant, then one 64-bit mix of the sum and the length (k_hash_fin).
+// Different records rarely share a hash, and equal hashes are verified byte
+// by byte, so a collision costs a verify round, never a wrong answer. The sum
+// does not depend on the order of its terms, so a record is hashed in
+// segments of kHashSeg bytes, one warp each, that add their partial sums to
+// acc[r] (zeroed first): many warps per record keep enough loads in flight
+// however few records there are. Block (x, y) takes records 8x .. 8x + 7
+// (one per warp) from byte y kHashSeg on. A lane reads 16 aligned bytes per
+// step (two 512-byte blocks per warp and step) and the next lane's first 8;
+// the two groups starting in its 16 bytes start at byte d0 mod 8 of them (d0
+// = the segment's start mod 16) and are realigned with funnel shifts. Index
+// arithmetic within a segment is 32-bit, so that a 16-byte step costs about
+// 40 instructions.
 constexpr uint64_t kHashSeg = 4096;
 constexpr int kHashWarps = 8;
 __global__ void __launch_bounds__(32 * kHashWarps)
@@ -400,40 +402,52 @@ __global__ void __launch_bounds__(32 * kHashWarps)
   const uint64_t len = rl[r];
   for (uint64_t s_lo = (uint64_t)blockIdx.y * kHashSeg; s_lo < len;
        s_lo += (uint64_t)gridDim.y * kHashSeg) {
-    const uint64_t s_hi = len - s_lo < kHashSeg ? len : s_lo + kHashSeg;
+    const uint32_t seg = (uint32_t)(len - s_lo < kHashSeg ? len - s_lo : kHashSeg);
     const uint64_t P = lo + rs[r] + s_lo;  // the record's byte s_lo
     const uint64_t A = P & ~15ull;
-    const uint32_t h4 = (uint32_t)(P & 3);
-    const int64_t rel0 = (int64_t)s_lo - (int64_t)(P - A);  // position of A in the record
-    const uint64_t span = P + (s_hi - s_lo) - A;
+    const uint32_t d0 = (uint32_t)(P - A), h8 = d0 & 7u, sh = 8u * (d0 & 3u);
+    const bool hi_word = h8 >= 4u;  // the groups start in the lane's second word
+    const uint32_t span = d0 + seg, q0 = (uint32_t)(s_lo >> 3);
     uint64_t h = 0;
-    for (uint64_t b0 = 0; b0 < span; b0 += 512 * kHashU) {
+    for (uint32_t b0 = 0; b0 < span; b0 += 512 * kHashU) {
       uint4 v[kHashU];
-      uint32_t nx[kHashU];
+      uint2 nx[kHashU];
 #pragma unroll
       for (int k = 0; k < kHashU; ++k) {
-        const uint64_t off = b0 + 512 * k + 16 * lane;
+        const uint32_t off = b0 + 512 * k + 16 * lane;
         v[k] = off < span ? load16_in(A + off, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
-        const uint64_t noff = b0 + 512 * k + 512;  // lane 31: the word after its 16 bytes
-        nx[k] = (lane == 31 && noff < span) ? load4_in(A + noff, lo, hi) : 0u;
+        const uint32_t noff = b0 + 512 * k + 512;  // lane 31: the 8 bytes after its 16
+        nx[k] = (lane == 31 && noff < span)
+                    ? make_uint2(load4_in(A + noff, lo, hi), load4_in(A + noff + 4, lo, hi))
+                    : make_uint2(0u, 0u);
       }
 #pragma unroll
       for (int k = 0; k < kHashU; ++k) {
-        uint32_t nxt = __shfl_down_sync(0xffffffffu, v[k].x, 1);
-        if (lane == 31) nxt = nx[k];
-        const uint32_t wd[5] = {v[k].x, v[k].y, v[k].z, v[k].w, nxt};
-        const int64_t lane_rel = rel0 + (int64_t)(b0 + 512 * k + 16 * lane);
+        uint32_t n0 = __shfl_down_sync(0xffffffffu, v[k].x, 1);
+        uint32_t n1 = __shfl_down_sync(0xffffffffu, v[k].y, 1);
+        if (lane == 31) {
+          n0 = nx[k].x;
+          n1 = nx[k].y;
+        }
+        // words from the one the first group starts in
+        const uint32_t wd[5] = {hi_word ? v[k].y : v[k].x, hi_word ? v[k].z : v[k].y,
+                                hi_word ? v[k].w : v[k].z, hi_word ? n0 : v[k].w,
+                                hi_word ? n1 : n0};
+        const int32_t t0 = (int32_t)(b0 + 512 * k + 16 * lane + h8) - (int32_t)d0;
 #pragma unroll
-        for (int g = 0; g < 4; ++g) {
-          const int64_t s = lane_rel + h4 + 4 * g;  // the group's position in the record
-          if (s < (int64_t)s_lo || s >= (int64_t)s_hi) continue;
-          uint32_t w = __funnelshift_r(wd[g], wd[g + 1], 8 * h4);
-          const int64_t left = (int64_t)len - s;
-          if (left < 4) w &= (1u << (8 * left)) - 1u;
-          const uint32_t q = (uint32_t)((uint64_t)s >> 2);
-          const uint32_t x = w ^ (q * 0x9e3779b9u + 0x7f4a7c15u);
-          const uint32_t y = w ^ (q * 0x85ebca6bu + 0x165667b1u);
-          h += (uint64_t)x * y;
+        for (int g = 0; g < 2; ++g) {
+          const int32_t t = t0 + 8 * g;  // the group's position in the segment
+          uint32_t x = __funnelshift_r(wd[2 * g], wd[2 * g + 1], sh);
+          uint32_t y = __funnelshift_r(wd[2 * g + 1], wd[2 * g + 2], sh);
+          const uint32_t rem = (uint32_t)((int32_t)seg - t);  // > 0 where valid
+          if (rem < 8u) {  // the record's last group: bytes from rem on are 0
+            y = rem > 4u ? y & ((1u << (8u * (rem - 4u))) - 1u) : 0u;
+            if (rem < 4u) x &= (1u << (8u * rem)) - 1u;
+          }
+          const uint32_t q = q0 + ((uint32_t)t >> 3);
+          x ^= q * 0x9e3779b9u + 0x7f4a7c15u;
+          y ^= q * 0x85ebca6bu + 0x165667b1u;
+          if ((uint32_t)t < seg) h += (uint64_t)x * y;
         }
       }
     }
