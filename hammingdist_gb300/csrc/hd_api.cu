@@ -1031,13 +1031,12 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
     // distances.
     // part ends as fractions of the file (HAMMINGDIST_STREAM_SPLITS="f1,f2,...",
     // increasing, at most 3). At n=20,000 x L=29,903 the file-to-host step
-    // (with the reference distances) took 8.39 ms with splits at 30% and 60%,
-    // 8.60-8.74 at 20-25% and 50-55%, 8.69 at 10%, 30% and 60%, 8.71 at 50%
-    // alone and 8.9-9.0 with a first part of 15%; without a split, 10.26 ms.
-    // Each part's ingest costs launches and host round trips whatever its
-    // size, and the tensor-core distances of the earlier parts finish before
-    // the next part is ingested, so a few large parts do best.
-    std::vector<double> ends = {0.3, 0.6};
+    // (with the reference distances) took 7.17-7.21 ms with splits at 35% and
+    // 65%, 7.28-7.37 at 30% and 60%, 7.53 at 40% and 70%, and 7.55-7.81 with
+    // three splits (10-20%, 35-45%, 65-70%); without a split, 10.26 ms (with
+    // older kernels). Each part's ingest costs launches and host round trips
+    // whatever its size, so a few large parts do best.
+    std::vector<double> ends = {0.35, 0.65};
     if (const char *e = std::getenv("HAMMINGDIST_STREAM_SPLITS")) {
       ends.clear();
       for (const char *q = e; *q && ends.size() < 3;) {

@@ -131,7 +131,7 @@ int hd_alignment_from_fasta_file(hd_ctx *ctx, const char *path, int remove_dupli
  * alignment (sequence indices; free it with hd_alignment_free). out_fn is
  * then asked for HD_OUTPUT_MIRROR (see there). For a file of 64 MB or more
  * the distances overlap the read: the file is ingested in parts that end at
- * record headers (by default after ~30% and ~60% of its bytes;
+ * record headers (by default after ~35% and ~65% of its bytes;
  * HAMMINGDIST_STREAM_SPLITS sets up to three splits); after each part the
  * unique rows so far (the first rows of the final result) are packed and the
  * tile rows that are complete run while the rest is read, and finished

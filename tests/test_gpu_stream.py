@@ -1,6 +1,6 @@
 """from_fasta with the distances overlapping the read (hd_pairwise_lt_fasta_file):
 for files of 64 MB or more the file is ingested in parts (by default split
-after ~30% and ~60% of its bytes; HAMMINGDIST_STREAM_SPLITS sets up to
+after ~35% and ~65% of its bytes; HAMMINGDIST_STREAM_SPLITS sets up to
 three),
 and each part's complete tile rows run while the rest is read. Every result
 must equal the plain order (read, ingest, distances) bit for bit: duplicates
@@ -204,8 +204,8 @@ def test_multiline_record_in_a_later_part(ctx, tmp_path, monkeypatch, where):
                                           ("", 0.45), ("", 0.7)])
 def test_error_in_a_part(ctx, tmp_path, big, monkeypatch, splits, where):
     # a short record in the third or the fourth part (splits at 10%, 30% and
-    # 60%), or in the second or the last part (the default splits, 30% and
-    # 60%)
+    # 60%), or in the second or the last part (the default splits, 35% and
+    # 65%)
     from hammingdist_gb300 import abi
 
     if splits:
@@ -227,7 +227,7 @@ def test_error_in_a_part(ctx, tmp_path, big, monkeypatch, splits, where):
 @pytest.mark.parametrize("splits", ["", "0.5", "0.2,0.5", "0.25,0.5,0.75", "0.9"])
 def test_every_split_setting(ctx, big, monkeypatch, splits):
     # no split (one part), one, two and three splits (the default is two:
-    # 30%, 60%): the same matrix and sequence indices as the plain order
+    # 35%, 65%): the same matrix and sequence indices as the plain order
     path, fa, rows = big
     monkeypatch.setenv("HAMMINGDIST_STREAM_SPLITS", splits)
     _touch(path)
