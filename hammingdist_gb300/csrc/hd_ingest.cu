@@ -501,63 +501,65 @@ __global__ void k_tab_insert(const uint64_t *hash, const uint64_t *list, uint64_
 
 // Each record against the lowest-index record of equal hash: equal bytes ->
 // duplicate; different bytes (a hash collision) -> next round.
-// Whether records a and b (equal length len, at addresses Pa and Pb inside
-// [lo, hi)) hold the same bytes; called by a whole warp, same result in every
-// lane. a is read with aligned 16-byte loads; b's bytes at the same relative
-// positions come from b's aligned loads shifted by d = (Pb - Pa) mod 16 with
-// funnel shifts over its words and the next lane's words.
-__device__ inline bool warp_equal(uint64_t Pa, uint64_t Pb, uint64_t len, uint64_t lo, uint64_t hi,
+// Whether the len bytes (len < 2^31) at Pa and at Pb, both inside [lo, hi),
+// are equal; called by a whole warp, same result in every lane. a is read
+// with aligned 16-byte loads; b's bytes at the same relative positions come
+// from b's aligned loads and the next lane's, shifted by d = (Pb - Pa) mod 16:
+// whole words by a warp-uniform switch, the rest by funnel shifts. Offsets
+// inside the span are 32-bit, and only the windows at its two ends mask
+// bytes.
+__device__ inline bool warp_equal(uint64_t Pa, uint64_t Pb, uint32_t len, uint64_t lo, uint64_t hi,
                                   int lane) {
   const uint64_t Aa = Pa & ~15ull;
-  const uint64_t Bs = Pb + Aa - Pa;  // b's byte at a's aligned start (may precede b)
+  const uint32_t da = (uint32_t)(Pa - Aa);  // a's first byte in its first window
+  const uint64_t Bs = Pb - da;              // b's byte at a's window start (may precede b)
   const uint64_t Ab = Bs & ~15ull;
-  const uint32_t d = (uint32_t)(Bs - Ab), dw = d >> 2, db = d & 3;
-  const uint64_t span = Pa + len - Aa;
-  const int64_t rel0 = -(int64_t)(Pa - Aa);
-  bool eq = true;
-  for (uint64_t b0 = 0; b0 < span && eq; b0 += 512 * kHashU) {
+  const uint32_t d = (uint32_t)(Bs - Ab), dw = d >> 2, sh = 8u * (d & 3u);
+  const uint32_t span = da + len;                    // a's windows cover [0, span) from Aa
+  const uint32_t b_end = (uint32_t)(Pb + len - Ab);  // b's bytes end there, from Ab
+  for (uint32_t b0 = 0; b0 < span; b0 += 512 * kHashU) {
     uint32_t diff = 0;
 #pragma unroll
     for (int k = 0; k < kHashU; ++k) {
-      const uint64_t off = b0 + 512 * k + 16 * lane;
+      const uint32_t off = b0 + 512 * k + 16 * lane;
       const bool in = off < span;
       const uint4 va = in ? load16_in(Aa + off, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
-      // b's 16 bytes are needed while they start before b's end: the window
-      // of the lane before reaches into them when d > 0
-      const uint4 vb = Ab + off < Pb + len ? load16_in(Ab + off, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+      const uint4 vb = off < b_end ? load16_in(Ab + off, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
       uint4 vn;
       vn.x = __shfl_down_sync(0xffffffffu, vb.x, 1);
       vn.y = __shfl_down_sync(0xffffffffu, vb.y, 1);
       vn.z = __shfl_down_sync(0xffffffffu, vb.z, 1);
       vn.w = __shfl_down_sync(0xffffffffu, vb.w, 1);
       if (lane == 31)
-        vn = (d && Ab + off + 16 < Pb + len) ? load16_in(Ab + off + 16, lo, hi)
-                                              : make_uint4(0u, 0u, 0u, 0u);
-      const uint32_t bw[8] = {vb.x, vb.y, vb.z, vb.w, vn.x, vn.y, vn.z, vn.w};
-      const uint32_t aw[4] = {va.x, va.y, va.z, va.w};
-      const int64_t rel = rel0 + (int64_t)off;  // position of aw[0] relative to the records
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        uint32_t blo = bw[j], bhi = bw[j + 1];
-#pragma unroll
-        for (int t = 1; t < 4; ++t)
-          if (dw == (uint32_t)t) {
-            blo = bw[j + t];
-            bhi = bw[j + t + 1];
-          }
-        const uint32_t al = __funnelshift_r(blo, bhi, 8 * db);
-        // compare only the bytes at relative positions [0, len)
-        const int64_t s = rel + 4 * j;
-        uint32_t m = in ? 0xffffffffu : 0u;
-        if (s < 0) m &= s <= -4 ? 0u : (0xffffffffu << (8 * (uint32_t)(-s)));
-        if (s + 4 > (int64_t)len)
-          m &= s >= (int64_t)len ? 0u : (0xffffffffu >> (8 * (uint32_t)(s + 4 - (int64_t)len)));
-        diff |= (aw[j] ^ al) & m;
+        vn = (d && off + 16 < b_end) ? load16_in(Ab + off + 16, lo, hi) : make_uint4(0u, 0u, 0u, 0u);
+      // words dw .. dw + 4 of b's 32 bytes (vb, vn)
+      uint32_t w0, w1, w2, w3, w4;
+      switch (dw) {  // warp-uniform
+        case 0: w0 = vb.x; w1 = vb.y; w2 = vb.z; w3 = vb.w; w4 = vn.x; break;
+        case 1: w0 = vb.y; w1 = vb.z; w2 = vb.w; w3 = vn.x; w4 = vn.y; break;
+        case 2: w0 = vb.z; w1 = vb.w; w2 = vn.x; w3 = vn.y; w4 = vn.z; break;
+        default: w0 = vb.w; w1 = vn.x; w2 = vn.y; w3 = vn.z; w4 = vn.w; break;
       }
+      uint32_t x[4] = {va.x ^ __funnelshift_r(w0, w1, sh), va.y ^ __funnelshift_r(w1, w2, sh),
+                       va.z ^ __funnelshift_r(w2, w3, sh), va.w ^ __funnelshift_r(w3, w4, sh)};
+      if (!(off >= da && off + 16 <= span)) {
+        // a window at an end of the span: only the bytes at positions
+        // [0, len) from a's first byte count
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int32_t p = (int32_t)(off + 4 * j) - (int32_t)da;  // the word's first byte
+          uint32_t m = in ? 0xffffffffu : 0u;
+          if (p < 0) m &= p <= -4 ? 0u : (0xffffffffu << (8 * (uint32_t)(-p)));
+          if (p + 4 > (int32_t)len)
+            m &= p >= (int32_t)len ? 0u : (0xffffffffu >> (8 * (uint32_t)(p + 4 - (int32_t)len)));
+          x[j] &= m;
+        }
+      }
+      diff |= x[0] | x[1] | x[2] | x[3];
     }
-    eq = !__any_sync(0xffffffffu, diff != 0);
+    if (__any_sync(0xffffffffu, diff != 0)) return false;
   }
-  return eq;
+  return true;
 }
 
 // The verify step spread over segments: warp (i, seg) compares bytes
@@ -595,7 +597,7 @@ __global__ void k_tab_cmp(const uint8_t *base, uint64_t bytes, const uint64_t *r
   if (o >= len) return;
   const uint64_t sl = len - o < seg_bytes ? len - o : seg_bytes;
   const uint64_t lo = reinterpret_cast<uint64_t>(base);
-  const bool eq = warp_equal(lo + rs[r] + o, lo + rs[rep] + o, sl, lo, lo + bytes, lane);
+  const bool eq = warp_equal(lo + rs[r] + o, lo + rs[rep] + o, (uint32_t)sl, lo, lo + bytes, lane);
   if (!eq && lane == 0) differs[i] = 1u;
 }
 
