@@ -987,8 +987,12 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       }
       *aln_out = own.release();
     };
-    // small files, or a file already on the device: nothing to overlap
-    if (n < (64ull << 20) || (!ctx->file_tag.empty() && ctx->file_tag == tag)) {
+    // small files (below 64 MB, or HAMMINGDIST_STREAM_MIN_BYTES), or a file
+    // already on the device: nothing to overlap
+    uint64_t min_bytes = 64ull << 20;
+    if (const char *e = std::getenv("HAMMINGDIST_STREAM_MIN_BYTES"))
+      min_bytes = std::strtoull(e, nullptr, 10);
+    if (n < min_bytes || (!ctx->file_tag.empty() && ctx->file_tag == tag)) {
       whole();
       hd::trace_end(ctx);
       return;
@@ -1155,11 +1159,12 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       hd::trace_mark(ctx, kUp[c]);
       // parse_fasta reads 16-byte vectors from a 16-byte aligned start: a
       // later part is parsed from B_prev rounded down. The bytes before B_prev
-      // end the previous part's last line; parsed as a FASTA's first line
-      // they are skipped and give an empty record 0, which is dropped.
+      // (up to 15) end the previous part; the records they hold or end (the
+      // empty record before the first header, and any short record whose
+      // header starts there) are the previous part's, and the parse leaves
+      // them out.
       const uint64_t C = B_prev & ~15ull;
-      hd::Records rec = hd::parse_fasta(ctx, dev + C, B - C, 0);
-      if (!rec.gathered.p && C < B_prev) rec = hd::drop_first_record(ctx, std::move(rec));
+      hd::Records rec = hd::parse_fasta(ctx, dev + C, B - C, 0, B_prev - C);
       // multi-line records, or a first part the whole path reports on
       if (rec.gathered.p || (c == 0 && (rec.n == 0 || rec.len0 == 0 || !rec.all_equal)))
         return fallback();
@@ -1173,6 +1178,18 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         // rows that can still come: a record of L sites takes at least L + 2
         // bytes (">\n" and the sites; the last one may lack its '\n')
         R_max = all.n + (n - B) / (L + 2) + 1;
+        // the buffers are sized for R_max rows: the output for R_max (R_max -
+        // 1) / 2 entries. Where that does not fit in half the free device
+        // memory (short records, many of them duplicates), the plain order
+        // runs: it sizes them for the unique rows
+        {
+          size_t free_b = 0, total_b = 0;
+          HD_CUDA(cudaMemGetInfo(&free_b, &total_b));
+          const double need = (double)(R_max < 2 ? 1 : tri(R_max)) * dtype_bytes +
+                              2.0 * (double)R_max * (double)words * 16.0 +
+                              (double)R_max * (double)words * (double)hd::kMmaOperandBytesPerWord;
+          if (need > 0.5 * (double)free_b) return fallback();
+        }
         owner = std::make_unique<hd_alignment>();
         owner->ctx = ctx;
         owner->device = ctx->device;

@@ -113,6 +113,7 @@ struct ParseSummary {
   unsigned long long Rk;        // records kept
   unsigned long long max_len;
   unsigned long long len0;
+  unsigned long long skip;      // records left out at the start
   unsigned int unterminated;    // the last line has no '\n'
   unsigned int unequal;
   unsigned int multi;           // some record spans several non-empty lines
@@ -144,25 +145,45 @@ __global__ void k_lines(const uint8_t *p, uint64_t n, const uint64_t *nl, uint64
 // Number of records the getline loop of read_fasta produces
 // (src/hamming_impl.cc:216-233): the first line is skipped; every later
 // header closes a record; the loop ends when the stream reaches its end,
-// which happens on reading an unterminated last line.
-__global__ void k_rec_count(const uint64_t *H_total, const uint32_t *hdr, uint64_t n_limit,
+// which happens on reading an unterminated last line. first > 0: the bytes
+// before `first` (which follows a '\n') belong to records parsed before,
+// so the records up to the header that starts there are left out (s->skip:
+// record 0 and those whose header line starts before `first`).
+__global__ void k_rec_count(const uint64_t *H_total, const uint32_t *hdr, const uint64_t *H,
+                            const uint64_t *nl, uint64_t first, uint64_t n_limit,
                             ParseSummary *s) {
   uint64_t M = s->lines, R;
   if (M == 0) R = 0;
   else if (M == 1) R = s->unterminated ? 0 : 1;
   else R = *H_total + 1 - ((hdr[M - 1] && s->unterminated) ? 1 : 0);
   s->R = R;
-  s->Rk = (n_limit && n_limit < R) ? n_limit : R;
+  uint64_t skip = 0;
+  if (first) {
+    // the line that starts at `first` follows the newline at first - 1
+    uint64_t lo = 0, hi = s->m_nl;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) / 2;
+      if (nl[mid] < first - 1) lo = mid + 1;
+      else hi = mid;
+    }
+    const uint64_t k0 = lo + 1;  // that line
+    skip = k0 < M ? H[k0] + 1 : R;
+  }
+  s->skip = skip;
+  const uint64_t after = R > skip ? R - skip : 0;
+  s->Rk = (n_limit && n_limit < after) ? n_limit : after;
 }
 
 __global__ void k_records(const uint8_t *p, uint64_t n, const uint64_t *nl, uint64_t m_nl,
-                          uint64_t M, const uint32_t *hdr, const uint64_t *H, const ParseSummary *s,
-                          unsigned long long *rec_len, unsigned int *rec_nseg,
-                          uint64_t *rec_start) {
+                          uint64_t M, const uint32_t *hdr, const uint64_t *H,
+                          const ParseSummary *s, unsigned long long *rec_len,
+                          unsigned int *rec_nseg, uint64_t *rec_start) {
   uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (k == 0 || k >= M || hdr[k]) return;
   uint64_t r = H[k];
-  if (r >= s->Rk) return;
+  const uint64_t skip = s->skip;
+  if (r < skip || r - skip >= s->Rk) return;
+  r -= skip;
   uint64_t st, e;
   line_range(k, nl, m_nl, n, st, e);
   if (e == st) return;
@@ -190,7 +211,8 @@ __global__ void k_seqline_len(const uint64_t *nl, uint64_t m_nl, uint64_t n, uin
   if (k >= M) return;
   uint64_t st, e;
   line_range(k, nl, m_nl, n, st, e);
-  len[k] = (k >= 1 && !hdr[k] && H[k] < s->Rk) ? e - st : 0;
+  const uint64_t skip = s->skip;
+  len[k] = (k >= 1 && !hdr[k] && H[k] >= skip && H[k] - skip < s->Rk) ? e - st : 0;
 }
 
 __global__ void k_gather_lines(const uint8_t *p, const uint64_t *nl, uint64_t m_nl, uint64_t n,
@@ -234,7 +256,8 @@ DevBuf newline_positions(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64_
   return nl;
 }
 
-Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_t n_limit) {
+Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_t n_limit,
+                    uint64_t first) {
   cudaStream_t st = ctx->stream;
   Records rec;
   uint64_t nblk = ceil_div(nbytes ? nbytes : 1, kNlBlockBytes);
@@ -267,7 +290,8 @@ Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_
     HD_LAUNCHED(ctx);
     scan_exclusive<uint32_t>(ctx, hdr.as<uint32_t>(), H.as<uint64_t>(), M, htot.as<uint64_t>());
   }
-  k_rec_count<<<1, 1, 0, st>>>(htot.as<uint64_t>(), hdr.as<uint32_t>(), n_limit, d_sum);
+  k_rec_count<<<1, 1, 0, st>>>(htot.as<uint64_t>(), hdr.as<uint32_t>(), H.as<uint64_t>(),
+                               nl.as<uint64_t>(), first, n_limit, d_sum);
   HD_LAUNCHED(ctx);
   const uint64_t cap = M + 1;  // records <= lines
   rec.rec_len = DevBuf(cap * 8, st);
@@ -1049,45 +1073,6 @@ Records concat_records(hd_ctx *ctx, const Records &a, const Records &b, uint64_t
       HD_CUDA(cudaMemcpyAsync(r.rec_len.as<uint64_t>() + a.n, b.rec_len.p, b.n * 8,
                               cudaMemcpyDeviceToDevice, st));
   }
-  return r;
-}
-
-__global__ void k_len_range(const uint64_t *len, uint64_t n, unsigned long long *mn,
-                            unsigned long long *mx) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    atomicMin(mn, (unsigned long long)len[i]);
-    atomicMax(mx, (unsigned long long)len[i]);
-  }
-}
-
-Records drop_first_record(hd_ctx *ctx, Records &&b) {
-  cudaStream_t st = ctx->stream;
-  Records r;
-  r.base = b.base;
-  r.bytes = b.bytes;
-  r.n = b.n ? b.n - 1 : 0;
-  r.rec_start = DevBuf((r.n ? r.n : 1) * 8, st);
-  r.rec_len = DevBuf((r.n ? r.n : 1) * 8, st);
-  r.gathered = std::move(b.gathered);
-  if (!r.n) return r;
-  HD_CUDA(cudaMemcpyAsync(r.rec_start.p, b.rec_start.as<uint64_t>() + 1, r.n * 8,
-                          cudaMemcpyDeviceToDevice, st));
-  HD_CUDA(cudaMemcpyAsync(r.rec_len.p, b.rec_len.as<uint64_t>() + 1, r.n * 8,
-                          cudaMemcpyDeviceToDevice, st));
-  DevBuf mm(16, st);
-  const unsigned long long init[2] = {~0ull, 0ull};
-  HD_CUDA(cudaMemcpyAsync(mm.p, init, 16, cudaMemcpyHostToDevice, st));
-  k_len_range<<<grid_for(r.n, 256) > 4096 ? 4096 : grid_for(r.n, 256), 256, 0, st>>>(
-      r.rec_len.as<uint64_t>(), r.n, mm.as<unsigned long long>(), mm.as<unsigned long long>() + 1);
-  HD_LAUNCHED(ctx);
-  unsigned long long h[3] = {0, 0, 0};
-  HD_CUDA(cudaMemcpyAsync(h, mm.p, 16, cudaMemcpyDeviceToHost, st));
-  HD_CUDA(cudaMemcpyAsync(h + 2, r.rec_len.p, 8, cudaMemcpyDeviceToHost, st));
-  HD_CUDA(cudaStreamSynchronize(st));
-  r.max_len = h[1];
-  r.len0 = h[2];
-  r.all_equal = h[0] == h[1];
   return r;
 }
 

@@ -402,7 +402,11 @@ inline int planes_of(int rule) { return rule == HD_RULE_AND ? 4 : rule == HD_RUL
 // ----------------------------------------------------- stage launchers
 // ingest.cu
 // d_file must be 16-byte aligned (the newline scan reads 16-byte vectors)
-Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_t n_limit);
+// first > 0: the bytes before offset `first` (a '\n' precedes it, and a
+// header starts there) end records parsed before, from an earlier part of the
+// same file; the records up to that header are left out
+Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_t n_limit,
+                    uint64_t first = 0);
 Records records_from_offsets(hd_ctx *ctx, const uint8_t *d_bytes, const uint64_t *h_offsets,
                              uint64_t n);
 // Deduplicates: returns the unique records (first-occurrence order) as a list
@@ -433,8 +437,6 @@ void pack_rows(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, hd_align
 // into g1 too unless it is null (n_rows x words uint4 each, already allocated)
 void pack_rows_and(hd_ctx *ctx, const Records &rec, const uint64_t *d_rows, uint64_t n_rows,
                    uint64_t length, uint64_t words, uint4 *g0, uint4 *g1 = nullptr);
-// b without its first record, with len0 / max_len / all_equal recomputed
-Records drop_first_record(hd_ctx *ctx, Records &&b);
 // records of a then b (b's starts shifted by b_off), one base; b parsed from
 // bytes that follow a's in the same buffer
 Records concat_records(hd_ctx *ctx, const Records &a, const Records &b, uint64_t b_off,
@@ -459,6 +461,9 @@ void pairwise_tiles(hd_ctx *ctx, const hd_alignment *aln, int dtype_bytes, uint3
 constexpr uint32_t kTile = 128;
 // columns of a tensor-core work item (the N of its MMAs)
 constexpr uint32_t kMmaCols = 240;
+// bytes of the tensor-core engine's E2M1 operand per 32-site word of a row
+// of the dense AND rule (6 blocks of 16 bytes: 4 planes and 2 dash blocks)
+constexpr uint32_t kMmaOperandBytesPerWord = 96;
 
 // Kernel configuration of one job: tile edge (64 or 128 rows; 4 or 8 rows
 // per thread) and TMA staging depth.

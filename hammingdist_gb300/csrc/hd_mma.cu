@@ -107,6 +107,7 @@ __host__ __device__ constexpr uint32_t op_blocks(uint32_t planes) {
 __host__ __device__ constexpr uint64_t row_bytes_per_word(uint32_t planes) {
   return (uint64_t)op_blocks(planes) * 16;
 }
+static_assert(row_bytes_per_word(4) == kMmaOperandBytesPerWord, "operand size of the AND rule");
 // E2M1 codes: 1.0, and the column side's -(P - 1): -3 for P = 4, -4 else
 // (then -1 for P = 6)
 constexpr uint32_t kE2M1One = 0x2u, kE2M1Neg1 = 0xAu;

@@ -224,6 +224,41 @@ def test_error_in_a_part(ctx, tmp_path, big, monkeypatch, splits, where):
     aln.free()
 
 
+@pytest.mark.parametrize("n_rec,streamed", [(80_000, True), (5_000_000, False)])
+def test_short_records(ctx, tmp_path, monkeypatch, n_rec, streamed):
+    # records of 13 bytes (">\n", 10 sites, "\n") drawn from 1,000 distinct
+    # rows. Streamed (the threshold lowered to 1 MB), with the parts' ends at
+    # the headers of records 16,011 and 48,006: the 15 and 14 bytes before
+    # them, which the next part is parsed from, hold a '\n' (and the '>') and
+    # then the whole previous record, which must not be counted twice.
+    # 5,000,000 records (65 MB): buffers sized for every record to be unique
+    # would not fit, so the plain order runs
+    rec_bytes = 13
+    n = n_rec * rec_bytes
+    if streamed:
+        monkeypatch.setenv("HAMMINGDIST_STREAM_MIN_BYTES", "1000000")
+        ends = [(rec_bytes * k - 5) / n for k in (16_011, 48_006)]
+        assert [(rec_bytes * k) % 16 for k in (16_011, 48_006)] == [15, 14]
+        monkeypatch.setenv("HAMMINGDIST_STREAM_SPLITS", ",".join("%.9f" % f for f in ends))
+    rng = np.random.default_rng(99)
+    acgt = np.frombuffer(b"ACGT-N", np.uint8)
+    distinct = acgt[rng.integers(0, 6, (1000, 10))]
+    pick = rng.integers(0, 1000, n_rec)
+    recs = np.empty((n_rec, rec_bytes), np.uint8)
+    recs[:, 0:2] = np.frombuffer(b">\n", np.uint8)
+    recs[:, 2:12] = distinct[pick]
+    recs[:, 12] = ord("\n")
+    p = tmp_path / "short.fasta"
+    p.write_bytes(recs.tobytes())
+    lt, aln = ctx.pairwise_lt_fasta_file(str(p), remove_duplicates=True)
+    want, want_idx = _plain(ctx, str(p), np.uint8, 255, True)
+    assert aln.n_input == n_rec
+    assert aln.n_rows == len({distinct[k].tobytes() for k in np.unique(pick)})
+    np.testing.assert_array_equal(aln.sequence_indices(), want_idx)
+    np.testing.assert_array_equal(lt, want)
+    aln.free()
+
+
 @pytest.mark.parametrize("splits", ["", "0.5", "0.2,0.5", "0.25,0.5,0.75", "0.9"])
 def test_every_split_setting(ctx, big, monkeypatch, splits):
     # no split (one part), one, two and three splits (the default is two:
