@@ -61,3 +61,18 @@ def test_noalloc_limits_are_reported():
         assert int(d_text.sum().item()) == 0
     finally:
         ctx.close()
+
+
+def test_noalloc_limit_is_checked_first():
+    # nsamples above the fixed scratch's 262,144 fails before any device
+    # memory is touched (the buffers here are null); fewer than 2 samples
+    # give no text
+    from hammingdist_gb300 import abi
+
+    ctx = abi.Context(0)
+    try:
+        with pytest.raises(abi.HDError, match="fixed scratch limit of 262144"):
+            ctx.lower_triangular_text_noalloc(0, 262_145, np.uint8, 0, 0)
+        assert ctx.lower_triangular_text_noalloc(0, 1, np.uint8, 0, 0) == 0
+    finally:
+        ctx.close()
