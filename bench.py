@@ -147,7 +147,7 @@ class Clocks:
             self.proc.kill()
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        # the timed regions' samples, and the last one before them
+        # the timed region's samples (every 50 ms), and the last one before it
         for ln in self.lines[max(0, getattr(self, "first", 0) - 1):]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
@@ -350,6 +350,9 @@ def run_ours(args):
             pair_ms.append(r["kernel_ms"])
         ev1.record(stream)
         torch.cuda.synchronize()
+        # nvidia-smi stops here: sampling during the e2e steps slowed them
+        # (9.4 against 7.2 ms per step), its queries holding the driver
+        clk = clocks.stop()
         launches = hd._kernel_launches() - launches0
         elapsed = replica_elapsed(ev0.elapsed_time(ev1) / 1e3, ws, dev)
         ms_step = elapsed / args.steps * 1e3
@@ -384,9 +387,6 @@ def run_ours(args):
             d2h = lt_arr.nbytes + 8 * N + rd2.nbytes
         e2e_mean = sum(e2e_times) / len(e2e_times)
         e2e_value = ws * pairs * L / e2e_mean / 1e9
-        # the clocks from the device-resident timed steps to the end of the
-        # e2e steps (sampled every 50 ms)
-        clk = clocks.stop()
 
         # parity at full size: the oracle port computes the whole workload
         # (every one of the 97,993,000 distances, the 20,000 sequence indices
