@@ -186,6 +186,10 @@ def make_workload(tmpdir):
     path = os.path.join(tmpdir, "bench.fasta")
     with open(path, "wb") as f:
         f.write(fa)
+        # written back now: a writeback of the 598 MB starting during the
+        # timed file-to-host steps would compete with their reads
+        f.flush()
+        os.fsync(f.fileno())
     return fa, root.tobytes(), path, rows
 
 
