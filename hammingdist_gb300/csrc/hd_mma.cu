@@ -174,11 +174,11 @@ __device__ __forceinline__ void put16(uint8_t *dst, uint32_t w, uint32_t v) {
 __global__ void k_expand_op(const uint4 *__restrict__ g0, const uint4 *__restrict__ g1,
                             uint32_t planes, uint64_t words, uint64_t row_lo, uint64_t row_hi,
                             uint64_t L, uint8_t *__restrict__ x, uint32_t *dash_chunk) {
-  const uint64_t total = (row_hi - row_lo) * words;
   const uint32_t nb = op_blocks(planes);  // 128-byte blocks per 256 sites
-  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
-       t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t r = row_lo + t / words, w = t % words;
+  // thread (x, y): word x of rows row_lo + y, row_lo + y + gridDim.y, ...
+  const uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (w >= words) return;
+  for (uint64_t r = row_lo + blockIdx.y; r < row_hi; r += gridDim.y) {
     const uint4 p = g0[r * words + w];
     const uint4 p1 = planes > 4 ? g1[r * words + w] : make_uint4(0u, 0u, 0u, 0u);
     const uint64_t s0 = w * 32;
@@ -780,9 +780,9 @@ bool ensure_operand(hd_ctx *ctx, const hd_alignment *aln, uint64_t rows, cudaStr
     o->op_dash = DevBuf(words / 8 * 4, stream);
     HD_CUDA(cudaMemsetAsync(o->op_dash.p, 0, words / 8 * 4, stream));
   }
-  const uint64_t total = (rows - o->op_rows) * words;
-  const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
-  k_expand_op<<<(unsigned)grid, 256, 0, stream>>>(
+  const dim3 grid((unsigned)ceil_div(words, (uint64_t)256),
+                  (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(rows - o->op_rows, 65535)));
+  k_expand_op<<<grid, 256, 0, stream>>>(
       o->plane_buf[0].as<uint4>(), P > 4 ? o->plane_buf[1].as<uint4>() : nullptr, P, words,
       o->op_rows, rows, o->length, o->op.as<uint8_t>(), o->op_dash.as<uint32_t>());
   HD_LAUNCHED(ctx);
@@ -846,9 +846,9 @@ bool operand_for(hd_ctx *ctx, const hd_alignment *a, cudaStream_t stream, PairLa
   }
   uint32_t *flags = reinterpret_cast<uint32_t *>(tmp.as<uint8_t>() + bytes);
   HD_CUDA(cudaMemsetAsync(flags, 0, flag_bytes, stream));
-  const uint64_t total = a->n_rows * o->words;
-  const uint64_t grid = std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->sm_count * 16);
-  k_expand_op<<<(unsigned)grid, 256, 0, stream>>>(
+  const dim3 grid((unsigned)ceil_div(o->words, (uint64_t)256),
+                  (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(a->n_rows, 65535)));
+  k_expand_op<<<grid, 256, 0, stream>>>(
       static_cast<const uint4 *>(a->planes_ptr(0)),
       P > 4 ? static_cast<const uint4 *>(a->planes_ptr(1)) : nullptr, P, o->words, 0, a->n_rows,
       o->length, tmp.as<uint8_t>(), flags);
