@@ -944,30 +944,25 @@ __global__ void __launch_bounds__(kPackThreads)
   }
 }
 
-// AND-rule packer without shared memory: a warp job is one 1024-site chunk of
-// one row, and lane l builds its 32-site word l from the chunk's bytes
-// [32 l, 32 l + 32), read as aligned 16-byte vectors (two of its own and the
-// next lane's first; realigned by the row's offset mod 16 with funnel
-// shifts). Each byte is classified by its low three bits, which tell the six
-// symbols apart (A 1, C 3, G 7, T 4, '-' 5): __byte_perm looks up the
-// symbol expected for those bits and its code (A, C, G, T one-hot, '-' 1111),
-// and a byte that is not the expected symbol (N, lowercase, any other) gets
-// 0, as in src/hamming_impl.cc:23-44. Sites past L get the '-' code.
-constexpr uint32_t kExpLo = 0x43004100u, kExpHi = 0x47002D54u;   // '?', A, '?', C | T, '-', '?', G
-constexpr uint32_t kCodeLo = 0x02000100u, kCodeHi = 0x04000F08u;  // 0, 1, 0, 2 | 8, 15, 0, 4
-__device__ __forceinline__ uint32_t and_codes4(uint32_t x) {
-  const uint32_t t = x & 0x07070707u;
-  const uint32_t s = t | (t >> 4);
-  const uint32_t sel = (s & 0xFFu) | ((s >> 8) & 0xFF00u);
-  const uint32_t d = x ^ __byte_perm(kExpLo, kExpHi, sel);
-  // high bit of each byte of nz: the byte is not the expected symbol
-  const uint32_t nz = (((d & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | d) & 0x80808080u;
-  const uint32_t keep = ((nz ^ 0x80808080u) >> 7) * 0xFFu;
-  return __byte_perm(kCodeLo, kCodeHi, sel) & keep;
-}
+// AND-rule packer: a warp job is one 1024-site chunk of one row, and lane l
+// builds its 32-site word l from the chunk's bytes [32 l, 32 l + 32), read as
+// aligned 16-byte vectors (two of its own and the next lane's first;
+// realigned by the row's offset mod 16 with funnel shifts). A 256-entry table
+// in shared memory gives each byte its code (A, C, G, T one-hot, '-' 1111,
+// every other byte 0, as in src/hamming_impl.cc:23-44) with plane p's bit at
+// bit 8 p. Summed with weights 1, 2, 4, 8 over 4 sites, and 16 for the next 4,
+// byte p of the sum holds plane p's bits of 8 sites; four such sums give each
+// plane word by byte permutes. Sites past L get the '-' code.
 __global__ void __launch_bounds__(256)
     k_pack_and(const uint8_t *base, uint64_t bytes, const uint64_t *rs, const uint64_t *rows,
                uint64_t n_rows, uint64_t L, uint64_t words, uint4 *g0, uint4 *g1) {
+  __shared__ uint32_t spread[256];
+  {
+    const uint32_t b = threadIdx.x;  // the block has 256 threads
+    const uint32_t c = b == 'A' ? 1u : b == 'C' ? 2u : b == 'G' ? 4u : b == 'T' ? 8u : b == '-' ? 15u : 0u;
+    spread[b] = (c & 1u) | ((c & 2u) << 7) | ((c & 4u) << 14) | ((c & 8u) << 21);
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const uint64_t lo = reinterpret_cast<uint64_t>(base), hi = lo + bytes;
   const uint64_t chunks = (words + 31) / 32;
@@ -1011,19 +1006,31 @@ __global__ void __launch_bounds__(256)
       for (int k = 0; k < 9; ++k) x[k] = w[k + 3];
     }
     const uint32_t s0 = 32u * lane;  // chunk-relative site of this lane's first byte
-    uint32_t pl[4] = {0u, 0u, 0u, 0u};
+    uint32_t pair[4];  // byte p: plane p's bits of sites 8 m .. 8 m + 7
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      uint32_t y = __funnelshift_r(x[k], x[k + 1], 8 * db);
-      const uint32_t sk = s0 + 4 * k;
-      if (sk + 4 > rem) {  // past the row's end: '-'
-        const uint32_t keep = sk >= rem ? 0u : (0xFFFFFFFFu >> (8 * (sk + 4 - rem)));
-        y = (y & keep) | (0x2D2D2D2Du & ~keep);
+    for (int m = 0; m < 4; ++m) {
+      uint32_t e2 = 0;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = 2 * m + h;
+        uint32_t y = __funnelshift_r(x[k], x[k + 1], 8 * db);
+        const uint32_t sk = s0 + 4 * k;
+        if (sk + 4 > rem) {  // past the row's end: '-'
+          const uint32_t keep = sk >= rem ? 0u : (0xFFFFFFFFu >> (8 * (sk + 4 - rem)));
+          y = (y & keep) | (0x2D2D2D2Du & ~keep);
+        }
+        const uint32_t e = spread[y & 0xFFu] + 2u * spread[(y >> 8) & 0xFFu] +
+                           4u * spread[(y >> 16) & 0xFFu] + 8u * spread[y >> 24];
+        e2 += e << (4 * h);
       }
-      const uint32_t c = and_codes4(y);
+      pair[m] = e2;
+    }
+    uint32_t pl[4];
 #pragma unroll
-      for (int p = 0; p < 4; ++p)
-        pl[p] |= ((((c >> p) & 0x01010101u) * 0x01020408u) >> 24) << (4 * k);
+    for (int p = 0; p < 4; ++p) {
+      const uint32_t lo2 = __byte_perm(pair[0], pair[1], (uint32_t)p | ((uint32_t)(4 + p) << 4));
+      const uint32_t hi2 = __byte_perm(pair[2], pair[3], (uint32_t)p | ((uint32_t)(4 + p) << 4));
+      pl[p] = __byte_perm(lo2, hi2, 0x5410u);
     }
     const uint64_t wi = q * 32 + lane;
     if (wi < words) {
