@@ -455,7 +455,11 @@ def run_ours(args):
                                                         32 * peaks["popc_per_s"]) / 1e12,
                              "lop3_mix_ceiling_T": peaks["mix_pair_sites_per_s"] / 1e12},
                 "e2e": {"value": e2e_value, "unit": "Gpair-sites/s", "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": d2h, "ms_per_step": e2e_mean * 1e3},
+                        "d2h_bytes_per_step": d2h, "ms_per_step": e2e_mean * 1e3,
+                        # each timed step (host clock): the host is shared, and
+                        # a step it delays shows here rather than only in the mean
+                        "steps_ms": [round(t * 1e3, 3) for t in e2e_times],
+                        "median_ms": statistics.median(e2e_times) * 1e3},
                 "gpu_launches": launches,
                 "clocks": clk,
             }
