@@ -28,6 +28,124 @@ using hd::fail;
 
 namespace hd {
 
+// ------------------------------------------------- large device buffers
+namespace {
+struct BigBlock {
+  void *p;
+  size_t size;        // bytes allocated
+  int device;
+  cudaEvent_t freed;  // recorded on the releasing stream at the release
+};
+struct BigCache {
+  std::mutex mu;
+  std::deque<BigBlock> released;             // oldest first
+  std::map<void *, std::pair<size_t, int>> live;  // handed out: size, device
+  std::map<int, size_t> cached;               // released bytes per device
+  std::map<int, size_t> cap;                  // per device
+};
+BigCache &big_cache() {
+  static BigCache *c = new BigCache();  // outlives the buffers that return to it
+  return *c;
+}
+bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+}
+// Frees the released blocks of `device` (all of them, or the oldest until
+// its cached bytes are at most `keep`) on stream s after their release
+// events. Called with the lock held.
+void big_evict(BigCache &c, int device, size_t keep, cudaStream_t s) {
+  for (auto it = c.released.begin(); it != c.released.end() && c.cached[device] > keep;) {
+    if (it->device != device) {
+      ++it;
+      continue;
+    }
+    cudaStreamWaitEvent(s, it->freed, 0);
+    cudaFreeAsync(it->p, s);
+    cudaEventDestroy(it->freed);
+    c.cached[device] -= it->size;
+    it = c.released.erase(it);
+  }
+}
+}  // namespace
+
+void *big_alloc(size_t n, cudaStream_t s) {
+  int dev = 0;
+  HD_CUDA(cudaGetDevice(&dev));
+  BigCache &c = big_cache();
+  // a stream being captured into a graph allocates graph-owned memory, as before
+  const bool cap = capturing(s);
+  std::lock_guard<std::mutex> lk(c.mu);
+  if (!cap) {
+    auto best = c.released.end();
+    for (auto it = c.released.begin(); it != c.released.end(); ++it)
+      if (it->device == dev && it->size >= n && it->size - n <= n / 8 &&
+          (best == c.released.end() || it->size < best->size))
+        best = it;
+    if (best != c.released.end()) {
+      const BigBlock b = *best;
+      c.released.erase(best);
+      c.cached[dev] -= b.size;
+      // the work that used the block before its release comes first
+      const cudaError_t e = cudaStreamWaitEvent(s, b.freed, 0);
+      cudaEventDestroy(b.freed);
+      if (e != cudaSuccess) {
+        cudaFreeAsync(b.p, s);
+        HD_CUDA(e);
+      }
+      c.live[b.p] = {b.size, dev};
+      return b.p;
+    }
+  }
+  void *p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, n, s);
+  if (e == cudaErrorMemoryAllocation && !cap) {
+    cudaGetLastError();
+    big_evict(c, dev, 0, s);  // the released blocks first
+    e = cudaMallocAsync(&p, n, s);
+  }
+  HD_CUDA(e);
+  if (!cap) c.live[p] = {n, dev};
+  return p;
+}
+
+void big_release(void *p, cudaStream_t s) {
+  BigCache &c = big_cache();
+  const bool cap = capturing(s);
+  std::lock_guard<std::mutex> lk(c.mu);
+  auto it = c.live.find(p);
+  if (it == c.live.end()) {  // graph-owned memory
+    cudaFreeAsync(p, s);
+    return;
+  }
+  const size_t size = it->second.first;
+  const int dev = it->second.second;
+  c.live.erase(it);
+  cudaEvent_t ev = nullptr;
+  int cur = -1;
+  cudaGetDevice(&cur);
+  if (cur != dev) cudaSetDevice(dev);
+  const bool kept = !cap && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess &&
+                    cudaEventRecord(ev, s) == cudaSuccess;
+  if (!kept) {
+    if (ev) cudaEventDestroy(ev);
+    cudaGetLastError();
+    cudaFreeAsync(p, s);
+  } else {
+    c.released.push_back({p, size, dev, ev});
+    c.cached[dev] += size;
+    auto cp = c.cap.find(dev);
+    if (cp == c.cap.end()) {
+      // at most 16 GB or 1/8 of the device's memory waits for reuse
+      size_t free_b = 0, total_b = 0;
+      cudaMemGetInfo(&free_b, &total_b);
+      cp = c.cap.emplace(dev, std::min<size_t>(16ull << 30, total_b / 8)).first;
+    }
+    if (c.cached[dev] > cp->second) big_evict(c, dev, cp->second, s);
+  }
+  if (cur != dev && cur >= 0) cudaSetDevice(cur);
+}
+
 namespace {
 cudaEvent_t trace_event(hd_ctx *ctx, size_t k) {
   while (ctx->trace.pool.size() <= k) {
@@ -1164,7 +1282,9 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       // header starts there) are the previous part's, and the parse leaves
       // them out.
       const uint64_t C = B_prev & ~15ull;
+      hd::trace_host(ctx, "part " + std::to_string(c + 1) + " on the device");
       hd::Records rec = hd::parse_fasta(ctx, dev + C, B - C, 0, B_prev - C);
+      hd::trace_host(ctx, "part " + std::to_string(c + 1) + " parsed");
       // multi-line records, or a first part the whole path reports on
       if (rec.gathered.p || (c == 0 && (rec.n == 0 || rec.len0 == 0 || !rec.all_equal)))
         return fallback();
@@ -1205,6 +1325,7 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
         // (fasta_reference_distances after from_fasta)
         keep_planes = DevBuf(R_max * words * 16, ctx->stream);
         d_lt = DevBuf((R_max < 2 ? 1 : tri(R_max)) * dtype_bytes, ctx->stream);
+        hd::trace_host(ctx, "row buffers allocated");
         if (!remove_duplicates) {
           std::vector<uint64_t> h(R_max);
           for (uint64_t i = 0; i < R_max; ++i) h[i] = i;
@@ -1217,7 +1338,9 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       const uint64_t *rows = iota.as<uint64_t>();
       if (remove_duplicates) {
         if (c == 0) inc.init(ctx, R_max);
-        if (inc_ok && inc.add(ctx, all)) {
+        const bool added = inc_ok && inc.add(ctx, all);
+        hd::trace_host(ctx, "part " + std::to_string(c + 1) + " deduplicated");
+        if (added) {
           Kc = inc.n_unique;
           rows = inc.unique_rec.as<uint64_t>();
         } else {
@@ -1244,12 +1367,14 @@ int hd_pairwise_lt_fasta_file(hd_ctx *ctx, const char *path, int remove_duplicat
       }
       hd::pack_rows_and(ctx, all, rows + K, Kc - K, L, words, g0 + K * words,
                         keep_planes.as<uint4>() + K * words);
+      hd::trace_host(ctx, "part " + std::to_string(c + 1) + " packing queued");
       // the new rows' tensor-core operand, before the launches of any stream read it
       if (use_mma && Kc >= 2 && !hd::ensure_operand(ctx, owner.get(), Kc, ctx->stream, R_max)) {
         use_mma = false;
         T = (uint32_t)cfg.tile;
         if (t_done) fail(HD_ERR_OOM, "no memory for the tensor-core operand of a streamed call");
       }
+      hd::trace_host(ctx, "part " + std::to_string(c + 1) + " operand queued");
       hd::trace_mark(ctx, kPacked[c]);
       K = Kc;
       if (!last) {

@@ -65,31 +65,69 @@ __device__ inline uint32_t nl_mask16(const uint8_t *p, uint64_t off, uint64_t n)
   return m;
 }
 
-// Newlines per 64 KB block (counts) and per 8 KB warp span (warp_counts).
+// Newlines per 64 KB block (counts) and per 8 KB warp span (warp_counts[w]).
+// A span with one or two newlines also records their offsets in the span
+// (warp_counts[W + 2 w] and [W + 2 w + 1], W = the launch's warps), so that
+// the write pass need not read it again: a FASTA line is usually longer than
+// a span. Each lane keeps the first two newlines of its own 16-byte slices,
+// which it visits in increasing order; the span's first newline is the least
+// of the lanes' first ones, and its second the least of the rest.
 __global__ void k_nl_count(const uint8_t *p, uint64_t n, uint64_t *counts, uint32_t *warp_counts) {
   __shared__ uint64_t tmp[33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t base = blockIdx.x * kNlBlockBytes + warp * kNlWarpBytes + lane * 16;
-  uint32_t c = 0;
+  constexpr uint32_t kNone = 0xFFFFFFFFu;
+  uint32_t c = 0, o0 = kNone, o1 = kNone;
 #pragma unroll 4
-  for (int it = 0; it < kNlIters; ++it) c += __popc(nl_mask16(p, base + it * 512ull, n));
+  for (int it = 0; it < kNlIters; ++it) {
+    const uint32_t m = nl_mask16(p, base + it * 512ull, n);
+    if (m && c < 2) {
+      const uint32_t rel = (uint32_t)it * 512u + (uint32_t)lane * 16u;
+      const uint32_t a = rel + (uint32_t)(__ffs(m) - 1), m2 = m & (m - 1);
+      if (c == 0) {
+        o0 = a;
+        if (m2) o1 = rel + (uint32_t)(__ffs(m2) - 1);
+      } else {
+        o1 = a;
+      }
+    }
+    c += __popc(m);
+  }
   const uint32_t cw = warp_sum(c);
-  if (lane == 0) warp_counts[blockIdx.x * (kNlThreads / 32) + warp] = cw;
+  const uint32_t wid = blockIdx.x * (kNlThreads / 32) + warp;
+  if (lane == 0) warp_counts[wid] = cw;
+  if (cw >= 1 && cw <= 2) {  // warp-uniform
+    const uint32_t q1 = __reduce_min_sync(0xffffffffu, o0);
+    const uint32_t q2 = __reduce_min_sync(0xffffffffu, o0 == q1 ? o1 : o0);
+    if (lane == 0) {
+      uint32_t *pos = warp_counts + gridDim.x * (kNlThreads / 32) + 2ull * wid;
+      pos[0] = q1;
+      pos[1] = q2;
+    }
+  }
   uint64_t tot;
   block_excl_scan<uint64_t>((uint64_t)c, tmp, tot);
   if (threadIdx.x == 0) counts[blockIdx.x] = tot;
 }
 
 // Writes the positions of every '\n' in increasing order: each warp starts at
-// its block's offset plus the counts of the block's earlier warps, and scans
-// its lanes' counts only where some lane holds a newline.
+// its block's offset plus the counts of the block's earlier warps; a span
+// with one or two newlines takes their offsets from the count pass, a span
+// with more scans its lanes' counts where some lane holds a newline.
 __global__ void k_nl_write(const uint8_t *p, uint64_t n, const uint64_t *block_off,
                            const uint32_t *warp_counts, uint64_t *nl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint64_t wbase = blockIdx.x * kNlBlockBytes + warp * kNlWarpBytes;
+  const uint32_t wid = blockIdx.x * (kNlThreads / 32) + warp;
   uint64_t off = block_off[blockIdx.x];
   for (int w = 0; w < warp; ++w) off += warp_counts[blockIdx.x * (kNlThreads / 32) + w];
-  if (warp_counts[blockIdx.x * (kNlThreads / 32) + warp] == 0) return;
+  const uint32_t cw = warp_counts[wid];
+  if (cw == 0) return;
+  if (cw <= 2) {
+    const uint32_t *pos = warp_counts + gridDim.x * (kNlThreads / 32) + 2ull * wid;
+    if (lane < (int)cw) nl[off + lane] = wbase + pos[lane];
+    return;
+  }
   for (int it = 0; it < kNlIters; ++it) {
     uint64_t at = wbase + it * 512ull + lane * 16;
     uint32_t m = nl_mask16(p, at, n);
@@ -237,7 +275,7 @@ static unsigned grid_for(uint64_t n, int threads) {
 DevBuf newline_positions(hd_ctx *ctx, const uint8_t *d, uint64_t nbytes, uint64_t *m_nl) {
   cudaStream_t st = ctx->stream;
   const uint64_t nblk = ceil_div(nbytes ? nbytes : 1, kNlBlockBytes);
-  DevBuf counts(nblk * 8, st), offs(nblk * 8, st), total(8, st), wcounts(nblk * 4 * (kNlThreads / 32), st);
+  DevBuf counts(nblk * 8, st), offs(nblk * 8, st), total(8, st), wcounts(nblk * 12 * (kNlThreads / 32), st);
   k_nl_count<<<(unsigned)nblk, kNlThreads, 0, st>>>(d, nbytes, counts.as<uint64_t>(),
                                                      wcounts.as<uint32_t>());
   HD_LAUNCHED(ctx);
@@ -262,7 +300,7 @@ Records parse_fasta(hd_ctx *ctx, const uint8_t *d_file, uint64_t nbytes, uint64_
   Records rec;
   uint64_t nblk = ceil_div(nbytes ? nbytes : 1, kNlBlockBytes);
   DevBuf counts(nblk * 8, st), offs(nblk * 8, st), total(8, st), sumbuf(sizeof(ParseSummary), st);
-  DevBuf wcounts(nblk * 4 * (kNlThreads / 32), st);
+  DevBuf wcounts(nblk * 12 * (kNlThreads / 32), st);
   ParseSummary *d_sum = sumbuf.as<ParseSummary>();
   HD_CUDA(cudaMemsetAsync(d_sum, 0, sizeof(ParseSummary), st));
   k_nl_count<<<(unsigned)nblk, kNlThreads, 0, st>>>(d_file, nbytes, counts.as<uint64_t>(),
