@@ -1,7 +1,7 @@
 // Internal declarations shared by the libhd translation units: the context and
-// alignment objects behind the C ABI, device buffers from the stream-ordered
-// pool, a device-wide exclusive scan, and the PTX helpers (mbarrier, TMA) used
-// by the pairwise kernel.
+// alignment objects behind the C ABI, device buffers (the stream-ordered pool,
+// large ones recycled by the library), a device-wide exclusive scan, and the
+// PTX helpers (mbarrier, TMA) used by the pairwise kernel.
 #pragma once
 
 #include <cuda.h>
