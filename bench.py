@@ -194,7 +194,8 @@ def make_workload(tmpdir):
 
 
 def measured_peaks():
-    """The generated peaks of this machine's GPUs, if present."""
+    """The measured HBM copy and bf16 GEMM peaks of this GPU kind
+    (MEASURED_PEAKS.json at the repository root), if present."""
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         return json.load(open(p))
@@ -332,7 +333,7 @@ def run_ours(args):
 
         # the clock sampler starts before the warm-up and has answered once
         # before the timed steps: nvidia-smi's start-up (NVML initialisation)
-        # can hold the driver for tens of ms, which must not fall into them
+        # can hold the NVIDIA driver for tens of ms, which must not fall into them
         clocks = Clocks(local)
         clocks.start()
         clocks.wait_first_sample()
@@ -355,7 +356,7 @@ def run_ours(args):
         ev1.record(stream)
         torch.cuda.synchronize()
         # nvidia-smi stops here: sampling during the e2e steps slowed them
-        # (9.4 against 7.2 ms per step), its queries holding the driver
+        # (9.4 against 7.2 ms per step), its queries holding the NVIDIA driver
         clk = clocks.stop()
         launches = hd._kernel_launches() - launches0
         elapsed = replica_elapsed(ev0.elapsed_time(ev1) / 1e3, ws, dev)
