@@ -96,6 +96,11 @@ void *big_alloc(size_t n, cudaStream_t s) {
       c.live[b.p] = {b.size, dev};
       return b.p;
     }
+    // a request of another size: the released blocks go back to the pool,
+    // which can split and reuse their memory. Kept for requests of other
+    // sizes (calls on alignments of varying shapes), they made the pool map
+    // new memory instead: 64 plain calls took 63.6 ms against 40.0.
+    big_evict(c, dev, 0, s);
   }
   void *p = nullptr;
   cudaError_t e = cudaMallocAsync(&p, n, s);
