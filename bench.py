@@ -36,6 +36,7 @@ request stream over resident alignments).
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -369,9 +370,14 @@ def run_ours(args):
         ctx = abi.Context(local)
         phases = value_phases(ctx, d_fa, nbytes, root, d_lt)
 
-        # e2e: the public API with host buffers (file -> device -> host)
+        # e2e: the public API with host buffers (file -> device -> host).
+        # Python's cyclic garbage collector is off while these steps run, as
+        # timeit does: a collection pass over the harness's own objects would
+        # otherwise land in whichever step crosses its allocation threshold
         e2e_times = []
         h2d = d2h = 0
+        gc.collect()
+        gc.disable()
         for k in range(args.warmup + args.steps):
             # a new modification time: from_fasta reads and uploads the file
             # again every step; fasta_reference_distances then finds the same
@@ -390,6 +396,7 @@ def run_ours(args):
                 e2e_times.append(dt)
             h2d = nbytes  # the FASTA goes up once per step
             d2h = lt_arr.nbytes + 8 * N + rd2.nbytes
+        gc.enable()
         e2e_mean = sum(e2e_times) / len(e2e_times)
         e2e_value = ws * pairs * L / e2e_mean / 1e9
 
