@@ -356,8 +356,8 @@ def run_ours(args):
             pair_ms.append(r["kernel_ms"])
         ev1.record(stream)
         torch.cuda.synchronize()
-        # nvidia-smi stops here: sampling during the e2e steps slowed them
-        # (9.4 against 7.2 ms per step), its queries holding the NVIDIA driver
+        # nvidia-smi stops here, before the e2e steps: their host-clock time
+        # would include any wait behind its queries to the NVIDIA driver
         clk = clocks.stop()
         launches = hd._kernel_launches() - launches0
         elapsed = replica_elapsed(ev0.elapsed_time(ev1) / 1e3, ws, dev)
